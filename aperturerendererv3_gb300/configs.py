@@ -1,0 +1,189 @@
+"""Seeded synthetic scenes for the benchmark and test workloads.
+
+  cornell_triangles()   Cornell box from 6 unit quads (12 triangles) and two
+                        boxes (0.3^3 and 0.3x0.6x0.3, rotated -18/+18 degrees
+                        about y; 12 triangles each), Lambertian albedos, one
+                        0.25 x 0.25 ceiling area light (emission 17/12/4), camera
+                        inside the box, fov 40: the 256x256 / 16 spp / depth 8
+                        workload.  The area light is a thin box so the
+                        reference's box-light sampler can sample it.
+  reference_cornell()   the reference's own SceneHelper::CreateCornellBox
+                        (core/helper/scene_helper.h:10-91): seven thin boxes,
+                        GGX floor and metal back wall.
+  random_triangles()    n triangles, centroids U[0,1]^3, vertices offset by
+                        N(0, 0.005^2) per axis: the 1M-triangle BVH stress scene.
+  terrain_scene()       2048^2 fBm heightfield (8 octaves, amplitude 0.2), 64
+                        emissive spheres, a distant sun sphere, GGX materials
+                        with roughness U[0.05, 0.6].
+No dataset is involved; every scene is generated from its seed.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .scene import Material, SceneObject, TriangleMesh
+from ._lib import OBJECT_CUBE, OBJECT_SPHERE
+
+GREY = (0.73, 0.73, 0.73)
+RED = (0.63, 0.065, 0.05)
+GREEN = (0.14, 0.45, 0.09)
+
+
+def _quad(a, b, c, d, mat):
+    return [SceneObject.Triangle(a, b, c, mat), SceneObject.Triangle(a, c, d, mat)]
+
+
+def _box_tris(center, half, rot_y_deg, mat):
+    """12 triangles of an oriented box (rotation about +y)."""
+    cy, sy = math.cos(math.radians(rot_y_deg)), math.sin(math.radians(rot_y_deg))
+
+    def p(x, y, z):
+        x, y, z = x * half[0], y * half[1], z * half[2]
+        return (float(np.float32(center[0] + cy * x + sy * z)), float(np.float32(center[1] + y)),
+                float(np.float32(center[2] - sy * x + cy * z)))
+
+    c = {(i, j, k): p(i, j, k) for i in (-1, 1) for j in (-1, 1) for k in (-1, 1)}
+    faces = [((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1)),
+             ((-1, -1, 1), (-1, 1, 1), (1, 1, 1), (1, -1, 1)),
+             ((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1)),
+             ((1, -1, -1), (1, -1, 1), (1, 1, 1), (1, 1, -1)),
+             ((-1, -1, -1), (-1, -1, 1), (1, -1, 1), (1, -1, -1)),
+             ((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1))]
+    out = []
+    for f in faces:
+        out += _quad(c[f[0]], c[f[1]], c[f[2]], c[f[3]], mat)
+    return out
+
+
+CORNELL_CAMERA = dict(origin=(0.0, 0.0, 0.49), direction=(0.0, 0.0, -1.0), fov=40.0)
+
+
+def cornell_triangles() -> list[SceneObject]:
+    grey = Material.CreateDiffusePureColor(GREY)
+    red = Material.CreateDiffusePureColor(RED)
+    green = Material.CreateDiffusePureColor(GREEN)
+    h = 0.5
+    objs = []
+    objs += _quad((-h, -h, -h), (h, -h, -h), (h, -h, h), (-h, -h, h), grey)      # floor
+    objs += _quad((-h, h, -h), (-h, h, h), (h, h, h), (h, h, -h), grey)          # ceiling
+    objs += _quad((-h, -h, -h), (-h, h, -h), (h, h, -h), (h, -h, -h), grey)      # back
+    objs += _quad((-h, -h, h), (h, -h, h), (h, h, h), (-h, h, h), grey)          # front
+    objs += _quad((-h, -h, -h), (-h, -h, h), (-h, h, h), (-h, h, -h), red)       # left
+    objs += _quad((h, -h, -h), (h, h, -h), (h, h, h), (h, -h, h), green)         # right
+    objs += _box_tris((0.18, -0.35, 0.12), (0.15, 0.15, 0.15), -18.0, grey)      # short box
+    objs += _box_tris((-0.17, -0.2, -0.15), (0.15, 0.3, 0.15), 18.0, grey)       # tall box
+    objs.append(SceneObject((0.0, 0.5 - 0.005, 0.0), (0.125, 0.005, 0.125), Material.CreateLight((17.0, 12.0, 4.0)),
+                            (0.0, 0.0, 0.0), OBJECT_CUBE))
+    return objs
+
+
+REFERENCE_CORNELL_CAMERA = dict(origin=(0.0, 0.0, 1.1), direction=(0.0, 0.0, -1.0), fov=60.0)
+
+
+def reference_cornell(light=(10.0, 10.0, 10.0)) -> list[SceneObject]:
+    """SceneHelper::CreateCornellBox with its default arguments."""
+    T = 0.01
+    white = (1.0, 1.0, 1.0)
+    dark = (0.75, 0.75, 0.75)  # WhiteDarken(0.25)
+    objs = [
+        SceneObject((0.0, -0.5 - T, 0.0), (0.5, T, 0.5), Material.CreateGGXPureColor(dark, 0.05, 0.0, 0.5)),
+        SceneObject((0.0, 0.5 + T, 0.0), (0.5, T, 0.5), Material.CreateDiffusePureColor(white)),
+        SceneObject((0.0, 0.5 - T, 0.0), (0.125 * 0.25, T, 0.125 * 0.25), Material.CreateLight(light)),
+        SceneObject((0.0, 0.0, -0.5 - T), (0.5, 0.5, T), Material.CreateGGXPureColor(dark, 0.25, 1.0, 0.5)),
+        SceneObject((-0.5, 0.0, 0.0), (T, 0.5, 0.5), Material.CreateDiffusePureColor((1.0, 0.0, 0.0))),
+        SceneObject((0.5, 0.0, 0.0), (T, 0.5, 0.5), Material.CreateDiffusePureColor((0.0, 1.0, 0.0))),
+    ]
+    return objs
+
+
+def random_triangles(n: int, seed: int = 1) -> np.ndarray:
+    """(n, 9) float32 triangle vertices."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 1, 3), dtype=np.float64)
+    v = c + rng.normal(0.0, 0.005, size=(n, 3, 3))
+    return v.astype(np.float32).reshape(n, 9)
+
+
+def pinhole_rays(width: int, height: int, origin, direction, fov: float) -> np.ndarray:
+    """(W*H, 8) float32 rays through pixel centres: (o, tmin=0, d, tmax=inf)."""
+    o = np.asarray(origin, np.float64)
+    d = np.asarray(direction, np.float64)
+    d /= np.linalg.norm(d)
+    right = np.cross(d, [0.0, 1.0, 0.0])
+    right /= np.linalg.norm(right)
+    up = np.cross(d, right)
+    up /= np.linalg.norm(up)
+    th = math.tan(math.radians(fov) * 0.5)
+    aspect = width / max(1.0, height)
+    j, i = np.mgrid[0:height, 0:width]
+    sx = ((i + 0.5) / width * 2.0 - 1.0) * th * aspect
+    sy = ((1.0 - (j + 0.5) / height) * 2.0 - 1.0) * th
+    dirs = d[None, None] + right[None, None] * sx[..., None] + up[None, None] * sy[..., None]
+    dirs /= np.linalg.norm(dirs, axis=-1, keepdims=True)
+    rays = np.zeros((height * width, 8), np.float32)
+    rays[:, 0:3] = o
+    rays[:, 3] = 0.0
+    rays[:, 4:7] = dirs.reshape(-1, 3)
+    rays[:, 7] = np.inf
+    return rays
+
+
+BVH_STRESS_CAMERA = dict(origin=(0.5, 0.5, 2.0), direction=(0.0, 0.0, -1.0), fov=40.0)
+
+
+def _fbm_heightfield(res: int, octaves: int, amplitude: float, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    h = np.zeros((res, res), np.float64)
+    amp, total = 1.0, 0.0
+    for o in range(octaves):
+        cells = 2 ** (o + 2)
+        g = rng.random((cells + 1, cells + 1))
+        x = np.linspace(0.0, cells, res)
+        i0 = np.minimum(x.astype(np.int64), cells - 1)
+        f = x - i0
+        f = f * f * (3.0 - 2.0 * f)
+        a = g[i0][:, i0] * (1 - f)[None, :] + g[i0][:, i0 + 1] * f[None, :]
+        b = g[i0 + 1][:, i0] * (1 - f)[None, :] + g[i0 + 1][:, i0 + 1] * f[None, :]
+        h += amp * (a * (1 - f)[:, None] + b * f[:, None])
+        total += amp
+        amp *= 0.5
+    return (h / total - 0.5) * amplitude
+
+
+TERRAIN_CAMERA = dict(origin=(0.5, 0.45, 1.55), direction=(0.0, -0.35, -1.0), fov=40.0)
+
+
+def terrain_scene(res: int = 2048, n_spheres: int = 64, seed: int = 7):
+    """Returns (objects, mesh): spheres + sun as objects, the heightfield as a mesh."""
+    rng = np.random.default_rng(seed)
+    hf = _fbm_heightfield(res, 8, 0.2, seed)
+    xs = np.linspace(0.0, 1.0, res)
+    X, Z = np.meshgrid(xs, xs, indexing="xy")
+    verts = np.stack([X, hf, Z], -1).reshape(-1, 3).astype(np.float32)
+    ii, jj = np.mgrid[0:res - 1, 0:res - 1]
+    a = (jj * res + ii).reshape(-1)
+    b = a + 1
+    c = a + res
+    d = c + 1
+    idx = np.concatenate([np.stack([a, c, b], 1), np.stack([b, c, d], 1)]).astype(np.uint32)
+    n_mat = 16
+    mats = [Material.CreateGGXPureColor(tuple(rng.uniform(0.3, 0.8, 3)), float(r), 0.0, 0.5)
+            for r in rng.uniform(0.05, 0.6, n_mat)]
+    mat_ids = rng.integers(0, n_mat, len(idx)).astype(np.int32)
+    mesh = TriangleMesh(verts, idx, mat_ids, mats)
+    objs = []
+    for _ in range(n_spheres):
+        r = float(rng.uniform(0.005, 0.02))
+        x, z = rng.uniform(0.05, 0.95, 2)
+        gi, gj = int(z * (res - 1)), int(x * (res - 1))
+        y = float(hf[gi, gj]) + r + 0.01
+        le = float(rng.uniform(5.0, 50.0))
+        col = rng.uniform(0.5, 1.0, 3)
+        objs.append(SceneObject((float(x), y, float(z)), (r, r, r), Material.CreateLight(tuple(le * col)),
+                                (0.0, 0.0, 0.0), OBJECT_SPHERE))
+    # small distant sun
+    objs.append(SceneObject((-20.0, 40.0, -30.0), (1.0, 1.0, 1.0), Material.CreateLight((400.0, 380.0, 330.0)),
+                            (0.0, 0.0, 0.0), OBJECT_SPHERE))
+    return objs, mesh

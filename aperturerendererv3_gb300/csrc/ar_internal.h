@@ -1,0 +1,157 @@
+// Internal state shared by the C-ABI layer (capi.cu) and the kernel
+// translation units.  Not part of the public interface.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "ar_bvh_build.h"
+#include "ar_shade.h"
+#include "ar_traverse.cuh"
+
+namespace ar
+{
+// Device-side scene as the kernels see it (passed by value).
+struct DevScene
+{
+    TravScene trav;
+    const Material* materials;
+    const int* prim_material;  // per primitive id
+    const int* prim_light;     // per primitive id, -1 when not a light
+    const int* prim_slot;      // per primitive id: its slot in the BVH leaf array
+    const Light* lights;
+    int light_count;
+    const float* lut_rgb;      // RES^3 x 4
+    const float* lut_lambda;   // 840 x 4
+    const float* cie_cmf;      // 421 x 3
+    const float* d65;          // 421
+    int camera_inside;         // camera origin overlaps an object
+    // profiling counters (null unless profiling): extend visits, extend tests,
+    // shadow visits, shadow tests, extend rays, shadow rays
+    unsigned long long* stats;
+};
+
+// stage ids for the per-stage profile
+enum Stage
+{
+    ST_RAYGEN = 0,
+    ST_EXTEND = 1,
+    ST_SHADE = 2,
+    ST_SHADOW = 3,
+    ST_FINAL = 4,
+    ST_COUNT = 5
+};
+
+struct StageEvent
+{
+    int stage;
+    cudaEvent_t a, b;
+};
+
+// Per-path state of the wavefront integrator (structure of arrays).
+struct PathState
+{
+    uint64_t* rng;
+    uint32_t* pixel;
+    uint32_t* frame;
+    float4* ray_o;      // xyz origin, w = lambda
+    float4* ray_d;      // xyz direction, w = lambda pdf
+    float* radiance;
+    float* mask;
+    uint32_t* depths;   // depth | nonDeltaDepth << 16
+    uint32_t* flags;    // bit0 inside media, bit1 previous NEE valid
+    float4* media_v;    // xyz media vertex, w = bits(media object index)
+    int* media_depth;
+    float4* prev;       // xyz last vertex, w = last BSDF pdf
+    float* hit_t;
+    int* hit_slot;
+    float* out_xyz;     // 3 per path
+    int capacity;
+};
+
+struct ShadowQueue
+{
+    int* path;
+    float4* o;      // xyz origin, w = tmax
+    float4* d;      // xyz direction, w = contribution if unoccluded
+    float* v_occ;   // contribution if occluded
+    uint8_t* valid_unocc;
+};
+
+struct RenderLaunch
+{
+    int width, height, spp, max_depth;
+    float cam_o[3], cam_d[3];
+    float fov_deg;
+    int use_nee;
+    uint64_t seed;
+    int first_frame;
+    int profile;
+};
+
+struct Ctx
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    // host scene description
+    std::vector<Material> materials;
+    std::vector<Object> objects;         // one per scene object (any type)
+    std::vector<int> object_material;
+    std::vector<int> object_type;
+    std::vector<float> object_tri;       // 9 per object (triangles)
+    std::vector<float> mesh_v;           // 9 per mesh triangle
+    std::vector<int> mesh_material;
+    // built scene
+    arbvh::WideBVH bvh;
+    std::vector<Light> lights;
+    bool built = false;
+    int camera_inside = 0;
+    // device buffers
+    void* d_nodes = nullptr;
+    void* d_slots = nullptr;
+    Object* d_objects = nullptr;
+    Material* d_materials = nullptr;
+    int* d_prim_material = nullptr;
+    int* d_prim_light = nullptr;
+    int* d_prim_slot = nullptr;
+    Light* d_lights = nullptr;
+    float* d_lut_rgb = nullptr;
+    float* d_lut_lambda = nullptr;
+    float* d_cie = nullptr;
+    float* d_d65 = nullptr;
+    unsigned int* d_err = nullptr;
+    int* d_counters = nullptr;
+    // wavefront buffers
+    PathState ps{};
+    ShadowQueue sq{};
+    int* d_queue[2] = {nullptr, nullptr};
+    double* d_accum = nullptr;
+    size_t accum_pixels = 0;
+    int wave_capacity = 0;
+    // timing of the last render (device ms) and launch count
+    float last_render_ms = 0.0f;
+    long long last_launches = 0;
+    // profiling
+    bool profile = false;
+    unsigned long long* d_stats = nullptr;  // 8 counters
+    std::vector<StageEvent> stage_events;
+    float stage_ms[ST_COUNT] = {0, 0, 0, 0, 0};
+    long long stage_launches[ST_COUNT] = {0, 0, 0, 0, 0};
+    unsigned long long stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+DevScene dev_scene(const Ctx& c);
+
+// kernel launchers (render.cu / trace.cu)
+cudaError_t launch_build_rgb_lut(float* lut, const float* weights_dev, cudaStream_t s);
+cudaError_t launch_prepare_materials(Material* mats, int n, const float* lut, cudaStream_t s);
+cudaError_t launch_trace(const DevScene& sc, const float* rays, int n, int any, int* prim_id, float* t,
+                         unsigned int* err, cudaStream_t s, long long* launches);
+cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_path, int n_paths,
+                               float* per_sample_out, long long* launches);
+cudaError_t launch_accumulate(Ctx& c, const RenderLaunch& rl, long long first_path, int n_paths, double* accum,
+                              long long* launches);
+} // namespace ar

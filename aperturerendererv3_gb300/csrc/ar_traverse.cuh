@@ -1,0 +1,203 @@
+// Device traversal of the 8-wide compressed BVH (layout: ar_bvh.h).
+//
+// One ray per thread; the traversal stack holds node groups (child base +
+// bitmask of the still-unvisited hit children, in the ray's octant order), so
+// its depth is bounded by the tree depth (AR_TRAV_STACK entries, checked at
+// build time) and it stays in registers / L1-resident local memory.
+//
+// Closest hit keeps the reference's acceptance window [tmin, tmax)
+// (core/render/intersection.cuh:73) and resolves exact ties in t to the
+// smallest primitive id, so the answer is independent of traversal order.
+// Any hit returns the first primitive with t in [tmin, tmax)
+// (core/render/intersection.cuh:254-261).
+#pragma once
+#include "ar_bvh.h"
+#include "ar_geom.h"
+#include "ar_shade.h"
+
+#define AR_TRAV_STACK 40
+#define AR_BOX_SLACK 1.0000004f  // >= 1 + 2*gamma_3 (Ize, "Robust BVH Ray Traversal", JCGT 2013)
+
+namespace ar
+{
+struct TravScene
+{
+    const uint4* __restrict__ nodes;       // 5 uint4 per node
+    const float4* __restrict__ slots;      // 3 float4 per primitive slot
+    const Object* __restrict__ objects;    // analytic object table, indexed by primitive id
+    int node_count;
+};
+
+struct TravResult
+{
+    float t;
+    int slot;  // primitive slot index, -1 on miss
+    int id;    // primitive id, -1 on miss
+};
+
+__device__ __forceinline__ uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, int s)
+{
+    const uint32_t w = (s < 4) ? lo_word : hi_word;
+    return (w >> (8 * (s & 3))) & 0xffu;
+}
+
+// Intersects one primitive slot; returns t (or -1 on miss) and the id.
+__device__ __forceinline__ float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3 d, int* id_out)
+{
+    const float4 a = __ldg(&sc.slots[3 * (size_t)slot + 0]);
+    const uint32_t tag = __float_as_uint(a.w);
+    const uint32_t kind = tag >> AR_PRIM_KIND_SHIFT;
+    const int id = (int)(tag & AR_PRIM_ID_MASK);
+    *id_out = id;
+    if (kind == AR_PRIM_KIND_TRI)
+    {
+        const float4 b = __ldg(&sc.slots[3 * (size_t)slot + 1]);
+        const float4 c = __ldg(&sc.slots[3 * (size_t)slot + 2]);
+        float t, b0, b1, b2;
+        if (tri_intersect(sh, o, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &t, &b0, &b1, &b2)) return t;
+        return -1.0f;
+    }
+    const Object ob = sc.objects[id];
+    Hit h;
+    h.hit = false;
+    const bool ok = (kind == AR_PRIM_KIND_BOX) ? intersect_box(o, d, ob, &h, false) : intersect_sphere(o, d, ob, &h, false);
+    return ok ? h.dist : -1.0f;
+}
+
+// error bits written to the context's device status word
+#define AR_DEVERR_STACK 1u
+#define AR_DEVERR_QUEUE 2u
+
+template <bool AnyHit>
+__device__ __forceinline__ TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,
+                                                    unsigned int* err, uint32_t& n_visits, uint32_t& n_tests)
+{
+    TravResult res;
+    res.t = tmax;
+    res.slot = -1;
+    res.id = -1;
+    if (sc.node_count <= 0) return res;
+    const RayShear sh = make_shear(d);
+    const V3 inv = v3(inv_safe(d.x), inv_safe(d.y), inv_safe(d.z));
+    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    uint2 stack[AR_TRAV_STACK];
+    int sp = 0;
+    int node = 0;
+    while (true)
+    {
+        if (node >= 0)
+        {
+            ++n_visits;
+            const uint4* np = sc.nodes + 5 * (size_t)node;
+            const uint4 w0 = __ldg(np + 0);
+            const uint4 w1 = __ldg(np + 1);
+            const uint4 w2 = __ldg(np + 2);
+            const uint4 w3 = __ldg(np + 3);
+            const uint4 w4 = __ldg(np + 4);
+            const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+            const float sx = __uint_as_float((w0.w & 0xffu) << 23);
+            const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+            const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+            const uint32_t imask = w0.w >> 24;
+            const uint32_t child_base = w1.x;
+            const uint32_t prim_base = w1.y;
+            uint32_t hit_int = 0, hit_leaf = 0;
+#pragma unroll
+            for (int s = 0; s < 8; ++s)
+            {
+                const uint32_t meta = byte_of(w1.z, w1.w, s);
+                if (meta == 0u) continue;
+                const float lx = fmaf((float)byte_of(w2.x, w2.y, s), sx, px);
+                const float ly = fmaf((float)byte_of(w2.z, w2.w, s), sy, py);
+                const float lz = fmaf((float)byte_of(w3.x, w3.y, s), sz, pz);
+                const float hx = fmaf((float)byte_of(w3.z, w3.w, s), sx, px);
+                const float hy = fmaf((float)byte_of(w4.x, w4.y, s), sy, py);
+                const float hz = fmaf((float)byte_of(w4.z, w4.w, s), sz, pz);
+                const float t0x = (lx - o.x) * inv.x, t1x = (hx - o.x) * inv.x;
+                const float t0y = (ly - o.y) * inv.y, t1y = (hy - o.y) * inv.y;
+                const float t0z = (lz - o.z) * inv.z, t1z = (hz - o.z) * inv.z;
+                const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+                const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z)) * AR_BOX_SLACK;
+                if (tn <= fminf(tf, res.t))
+                {
+                    const uint32_t bit = 1u << ((uint32_t)s ^ oct);
+                    if (meta & 0x80u) hit_int |= bit;
+                    else hit_leaf |= bit;
+                }
+            }
+            while (hit_leaf)
+            {
+                const uint32_t i = __ffs(hit_leaf) - 1;
+                hit_leaf &= hit_leaf - 1;
+                const int s = (int)(i ^ oct);
+                const uint32_t meta = byte_of(w1.z, w1.w, s);
+                const int cnt = (int)(meta >> 5);
+                const int first = (int)(prim_base + (meta & 31u));
+                for (int k = 0; k < cnt; ++k)
+                {
+                    int id;
+                    ++n_tests;
+                    const float t = prim_hit(sc, first + k, sh, o, d, &id);
+                    if (!(t >= tmin)) continue;  // also rejects misses (-1)
+                    if (AnyHit)
+                    {
+                        if (t < res.t)
+                        {
+                            res.t = t;
+                            res.slot = first + k;
+                            res.id = id;
+                            return res;
+                        }
+                    }
+                    else if (t < res.t || (t == res.t && res.id >= 0 && id < res.id))
+                    {
+                        res.t = t;
+                        res.slot = first + k;
+                        res.id = id;
+                    }
+                }
+            }
+            node = -1;
+            if (hit_int)
+            {
+                const uint32_t i = __ffs(hit_int) - 1;
+                hit_int &= hit_int - 1;
+                const uint32_t s = i ^ oct;
+                node = (int)(child_base + __popc(imask & ((1u << s) - 1u)));
+                if (hit_int)
+                {
+                    if (sp < AR_TRAV_STACK) stack[sp++] = make_uint2(child_base, hit_int | (imask << 8));
+                    else if (err) atomicOr(err, AR_DEVERR_STACK);
+                }
+                continue;
+            }
+        }
+        if (sp == 0) break;
+        uint2 e = stack[--sp];
+        uint32_t m = e.y & 0xffu;
+        const uint32_t im = e.y >> 8;
+        const uint32_t i = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t s = i ^ oct;
+        node = (int)(e.x + __popc(im & ((1u << s) - 1u)));
+        if (m) stack[sp++] = make_uint2(e.x, m | (im << 8));
+    }
+    if (res.slot < 0) res.t = tmax;
+    return res;
+}
+
+// stats (optional): [0] += node visits, [1] += primitive tests
+template <bool AnyHit>
+__device__ __forceinline__ TravResult traverse(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,
+                                               unsigned int* err, unsigned long long* stats = nullptr)
+{
+    uint32_t n_visits = 0, n_tests = 0;
+    TravResult res = traverse_impl<AnyHit>(sc, o, d, tmin, tmax, err, n_visits, n_tests);
+    if (stats)
+    {
+        atomicAdd(&stats[0], (unsigned long long)n_visits);
+        atomicAdd(&stats[1], (unsigned long long)n_tests);
+    }
+    return res;
+}
+} // namespace ar

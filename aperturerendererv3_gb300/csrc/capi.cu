@@ -1,0 +1,736 @@
+// C-ABI implementation: context lifetime, scene upload, BVH / light-table /
+// spectral-LUT setup, the render loop over waves, and the raw ray queries.
+//
+// Host-side logic mirrors SceneRenderer (core/scene.cu): the light table of
+// UpdateSceneToDeviceIfDirty (core/scene.cu:677-706), the material factories
+// (core/render/object.cuh:119-206), SceneObject's frame and bounds
+// (core/render/object.cuh:249-315), and the headless Render loop
+// (core/scene.cu:210-238) with FP64 accumulation instead of an FP32 running mean.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "../../include/aperture/ar.h"
+#include "ar_internal.h"
+#include "spectral_tables.inc"
+
+struct ar_ctx
+{
+    ar::Ctx c;
+};
+
+namespace ar
+{
+DevScene dev_scene(const Ctx& c)
+{
+    DevScene s;
+    s.trav.nodes = reinterpret_cast<const uint4*>(c.d_nodes);
+    s.trav.slots = reinterpret_cast<const float4*>(c.d_slots);
+    s.trav.objects = c.d_objects;
+    s.trav.node_count = (int)c.bvh.nodes.size();
+    s.materials = c.d_materials;
+    s.prim_material = c.d_prim_material;
+    s.prim_light = c.d_prim_light;
+    s.prim_slot = c.d_prim_slot;
+    s.lights = c.d_lights;
+    s.light_count = (int)c.lights.size();
+    s.lut_rgb = c.d_lut_rgb;
+    s.lut_lambda = c.d_lut_lambda;
+    s.cie_cmf = c.d_cie;
+    s.d65 = c.d_d65;
+    s.camera_inside = c.camera_inside;
+    s.stats = c.profile ? c.d_stats : nullptr;
+    return s;
+}
+} // namespace ar
+
+namespace
+{
+using namespace ar;
+
+ar_status fail(ar_ctx* ctx, ar_status code, const std::string& msg)
+{
+    if (ctx) ctx->c.last_error = msg;
+    return code;
+}
+
+ar_status cuda_fail(ar_ctx* ctx, cudaError_t e, const char* where)
+{
+    return fail(ctx, AR_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define AR_CUDA(ctx, call)                                              \
+    do                                                                  \
+    {                                                                   \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);      \
+    } while (0)
+
+template <typename T>
+void free_dev(T*& p)
+{
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+void free_scene(Ctx& c)
+{
+    free_dev(c.d_nodes);
+    free_dev(c.d_slots);
+    free_dev(c.d_objects);
+    free_dev(c.d_materials);
+    free_dev(c.d_prim_material);
+    free_dev(c.d_prim_light);
+    free_dev(c.d_prim_slot);
+    free_dev(c.d_lights);
+    c.built = false;
+}
+
+void free_waves(Ctx& c)
+{
+    PathState& p = c.ps;
+    free_dev(p.rng); free_dev(p.pixel); free_dev(p.frame); free_dev(p.ray_o); free_dev(p.ray_d);
+    free_dev(p.radiance); free_dev(p.mask); free_dev(p.depths); free_dev(p.flags); free_dev(p.media_v);
+    free_dev(p.media_depth); free_dev(p.prev); free_dev(p.hit_t); free_dev(p.hit_slot); free_dev(p.out_xyz);
+    free_dev(c.sq.path); free_dev(c.sq.o); free_dev(c.sq.d); free_dev(c.sq.v_occ); free_dev(c.sq.valid_unocc);
+    free_dev(c.d_queue[0]);
+    free_dev(c.d_queue[1]);
+    c.wave_capacity = 0;
+    p.capacity = 0;
+}
+
+template <typename T>
+cudaError_t alloc_dev(T*& p, size_t count)
+{
+    return cudaMalloc((void**)&p, std::max<size_t>(count, 1) * sizeof(T));
+}
+
+ar_status ensure_waves(ar_ctx* ctx, int cap)
+{
+    Ctx& c = ctx->c;
+    if (c.wave_capacity >= cap) return AR_OK;
+    free_waves(c);
+    PathState& p = c.ps;
+    const size_t n = (size_t)cap;
+    AR_CUDA(ctx, alloc_dev(p.rng, n));
+    AR_CUDA(ctx, alloc_dev(p.pixel, n));
+    AR_CUDA(ctx, alloc_dev(p.frame, n));
+    AR_CUDA(ctx, alloc_dev(p.ray_o, n));
+    AR_CUDA(ctx, alloc_dev(p.ray_d, n));
+    AR_CUDA(ctx, alloc_dev(p.radiance, n));
+    AR_CUDA(ctx, alloc_dev(p.mask, n));
+    AR_CUDA(ctx, alloc_dev(p.depths, n));
+    AR_CUDA(ctx, alloc_dev(p.flags, n));
+    AR_CUDA(ctx, alloc_dev(p.media_v, n));
+    AR_CUDA(ctx, alloc_dev(p.media_depth, n));
+    AR_CUDA(ctx, alloc_dev(p.prev, n));
+    AR_CUDA(ctx, alloc_dev(p.hit_t, n));
+    AR_CUDA(ctx, alloc_dev(p.hit_slot, n));
+    AR_CUDA(ctx, alloc_dev(p.out_xyz, 3 * n));
+    AR_CUDA(ctx, alloc_dev(c.sq.path, n));
+    AR_CUDA(ctx, alloc_dev(c.sq.o, n));
+    AR_CUDA(ctx, alloc_dev(c.sq.d, n));
+    AR_CUDA(ctx, alloc_dev(c.sq.v_occ, n));
+    AR_CUDA(ctx, alloc_dev(c.sq.valid_unocc, n));
+    AR_CUDA(ctx, alloc_dev(c.d_queue[0], n));
+    AR_CUDA(ctx, alloc_dev(c.d_queue[1], n));
+    p.capacity = cap;
+    c.wave_capacity = cap;
+    return AR_OK;
+}
+
+// Material::Create* semantics: which fields each shading model keeps, clamps.
+Material make_material(const ar_material& m)
+{
+    Material r;
+    std::memset(&r, 0, sizeof(r));
+    r.shading = m.shading;
+    r.albedo = v3(1.0f, 1.0f, 1.0f);
+    r.emissive = v3(0.0f, 0.0f, 0.0f);
+    r.specular = 0.0f;
+    r.metallic = 0.0f;
+    r.roughness = 0.0f;
+    r.ior = 1.5f;
+    r.sigma_a = 100.0f;
+    r.abbe = 20.0f;
+    r.tilt = 0.0f;
+    const V3 alb = v3(m.albedo[0], m.albedo[1], m.albedo[2]);
+    const V3 emi = v3(m.emissive[0], m.emissive[1], m.emissive[2]);
+    switch (m.shading)
+    {
+        case AR_SHADING_LIGHT:
+            r.albedo = v3(0.0f, 0.0f, 0.0f);
+            r.emissive = emi;
+            break;
+        case AR_SHADING_GLASS:
+            r.albedo = alb;
+            r.ior = m.ior;
+            r.sigma_a = m.sigma_a;
+            r.abbe = m.abbe;
+            r.tilt = m.tilt;
+            break;
+        case AR_SHADING_GGX:
+            r.albedo = alb;
+            r.roughness = clampf(m.roughness, 0.01f, 1.0f);
+            r.metallic = clampf(m.metallic, 0.0f, 1.0f);
+            r.specular = clampf(m.specular, 0.0f, 1.0f);
+            r.emissive = emi;
+            break;
+        default:
+            r.shading = AR_SHADING_DIFFUSE;
+            r.albedo = alb;
+            r.emissive = emi;
+            break;
+    }
+    return r;
+}
+
+float luminance(V3 c) { return dot(c, v3(0.2126f, 0.7152f, 0.0722f)); }
+
+// SceneObject::GetArea (core/render/object.cuh:240-255)
+float object_area(const Object& o)
+{
+    if (o.type == AR_OBJ_CUBE)
+    {
+        const float ex = fabsf(o.extent.x), ey = fabsf(o.extent.y), ez = fabsf(o.extent.z);
+        return 8.0f * (ex * ey + ex * ez + ey * ez);
+    }
+    if (o.type == AR_OBJ_SPHERE)
+    {
+        const float r = fabsf(o.extent.x);
+        return 4.0f * AR_PI_F * r * r;
+    }
+    return 0.0f;
+}
+
+// SceneObject::UpdateProxy bounds (core/render/object.cuh:262-293), widened by a
+// relative 1e-6 so the BVH boxes enclose the intersection routine's rounding.
+void object_bounds(const Object& o, float lo[3], float hi[3])
+{
+    V3 half;
+    if (o.type == AR_OBJ_CUBE)
+    {
+        const V3 ax = mul(o.o2w, v3(1, 0, 0)), ay = mul(o.o2w, v3(0, 1, 0)), az = mul(o.o2w, v3(0, 0, 1));
+        half.x = fabsf(ax.x) * o.extent.x + fabsf(ay.x) * o.extent.y + fabsf(az.x) * o.extent.z;
+        half.y = fabsf(ax.y) * o.extent.x + fabsf(ay.y) * o.extent.y + fabsf(az.y) * o.extent.z;
+        half.z = fabsf(ax.z) * o.extent.x + fabsf(ay.z) * o.extent.y + fabsf(az.z) * o.extent.z;
+    }
+    else
+    {
+        const float r = max3(o.extent);
+        half = v3(r, r, r);
+    }
+    const float c[3] = {o.center.x, o.center.y, o.center.z};
+    const float h[3] = {half.x, half.y, half.z};
+    for (int k = 0; k < 3; ++k)
+    {
+        const float pad = 1e-6f * (fabsf(c[k]) + h[k]) + 1e-30f;
+        lo[k] = c[k] - h[k] - pad;
+        hi[k] = c[k] + h[k] + pad;
+    }
+}
+
+bool cuda_device_ok(int device, std::string* why)
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n <= device || device < 0)
+    {
+        *why = std::string("no CUDA device ") + std::to_string(device) + (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e) : std::string());
+        return false;
+    }
+    return true;
+}
+} // namespace
+
+extern "C" {
+
+int ar_abi_version(void) { return 1; }
+
+ar_status ar_create(ar_ctx** out, int device)
+{
+    if (!out) return AR_ERR_INVALID;
+    *out = nullptr;
+    std::string why;
+    if (!cuda_device_ok(device, &why)) return AR_ERR_CUDA;
+    ar_ctx* ctx = new (std::nothrow) ar_ctx();
+    if (!ctx) return AR_ERR_NOMEM;
+    Ctx& c = ctx->c;
+    c.device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_err, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(c.d_err, 0, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_counters, 8 * sizeof(int));
+    // spectral tables: CIE CMFs, D65, lambda LUT (built on the host: 840 encoder runs)
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_cie, sizeof(AR_TAB_CMF));
+    if (e == cudaSuccess) e = cudaMemcpy(c.d_cie, AR_TAB_CMF, sizeof(AR_TAB_CMF), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_d65, sizeof(AR_TAB_D65));
+    if (e == cudaSuccess) e = cudaMemcpy(c.d_d65, AR_TAB_D65, sizeof(AR_TAB_D65), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+    {
+        std::vector<float> lam(AR_LAMBDA_LUT_RES * 4);
+        const float step = (780.0f - 360.0f) / static_cast<float>(AR_LAMBDA_LUT_RES);
+        for (int i = 0; i < AR_LAMBDA_LUT_RES; ++i) lambda_encode(360.0f + (i + 0.5f) * step, &lam[4 * i], AR_TAB_LAM_MLP);
+        e = cudaMalloc((void**)&c.d_lut_lambda, lam.size() * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemcpy(c.d_lut_lambda, lam.data(), lam.size() * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess)
+    {
+        ar_destroy(ctx);
+        return AR_ERR_CUDA;
+    }
+    *out = ctx;
+    return AR_OK;
+}
+
+ar_status ar_destroy(ar_ctx* ctx)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    cudaSetDevice(c.device);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    free_scene(c);
+    free_waves(c);
+    free_dev(c.d_lut_rgb);
+    free_dev(c.d_lut_lambda);
+    free_dev(c.d_cie);
+    free_dev(c.d_d65);
+    free_dev(c.d_err);
+    free_dev(c.d_counters);
+    free_dev(c.d_accum);
+    free_dev(c.d_stats);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete ctx;
+    return AR_OK;
+}
+
+const char* ar_last_error(ar_ctx* ctx) { return ctx ? ctx->c.last_error.c_str() : "null context"; }
+
+ar_status ar_scene_set_materials(ar_ctx* ctx, const ar_material* m, int n)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    if (n < 0 || (n > 0 && !m)) return fail(ctx, AR_ERR_INVALID, "materials: bad pointer or count");
+    Ctx& c = ctx->c;
+    c.materials.resize(n);
+    for (int i = 0; i < n; ++i) c.materials[i] = make_material(m[i]);
+    c.built = false;
+    return AR_OK;
+}
+
+ar_status ar_scene_set_objects(ar_ctx* ctx, const ar_object* o, int n)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    if (n < 0 || (n > 0 && !o)) return fail(ctx, AR_ERR_INVALID, "objects: bad pointer or count");
+    Ctx& c = ctx->c;
+    c.objects.assign(n, Object{});
+    c.object_material.resize(n);
+    c.object_type.resize(n);
+    c.object_tri.assign((size_t)n * 9, 0.0f);
+    for (int i = 0; i < n; ++i)
+    {
+        const ar_object& s = o[i];
+        if (s.type != AR_OBJECT_CUBE && s.type != AR_OBJECT_SPHERE && s.type != AR_OBJECT_TRIANGLE)
+            return fail(ctx, AR_ERR_INVALID, "objects: unsupported type " + std::to_string(s.type));
+        Object& ob = c.objects[i];
+        std::memset(&ob, 0, sizeof(ob));
+        ob.type = s.type;
+        ob.center = v3(s.center[0], s.center[1], s.center[2]);
+        ob.extent = v3(fabsf(s.extent[0]), fabsf(s.extent[1]), fabsf(s.extent[2]));
+        object_frame(v3(s.rotation_deg[0], s.rotation_deg[1], s.rotation_deg[2]), &ob.o2w, &ob.w2o);
+        c.object_material[i] = s.material;
+        c.object_type[i] = s.type;
+        if (s.type == AR_OBJECT_TRIANGLE)
+        {
+            for (int k = 0; k < 3; ++k)
+            {
+                c.object_tri[9 * (size_t)i + k] = s.v0[k];
+                c.object_tri[9 * (size_t)i + 3 + k] = s.v1[k];
+                c.object_tri[9 * (size_t)i + 6 + k] = s.v2[k];
+            }
+        }
+    }
+    c.built = false;
+    return AR_OK;
+}
+
+ar_status ar_scene_set_mesh(ar_ctx* ctx, const float* v, int nv, const uint32_t* idx, int nt, const int32_t* mat)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    if (nt < 0 || nv < 0 || (nt > 0 && (!v || !idx || !mat))) return fail(ctx, AR_ERR_INVALID, "mesh: bad pointer or count");
+    Ctx& c = ctx->c;
+    c.mesh_v.resize((size_t)nt * 9);
+    c.mesh_material.resize(nt);
+    for (int t = 0; t < nt; ++t)
+    {
+        for (int j = 0; j < 3; ++j)
+        {
+            const uint32_t vi = idx[3 * (size_t)t + j];
+            if (vi >= (uint32_t)nv) return fail(ctx, AR_ERR_INVALID, "mesh: vertex index out of range");
+            for (int k = 0; k < 3; ++k) c.mesh_v[9 * (size_t)t + 3 * j + k] = v[3 * (size_t)vi + k];
+        }
+        c.mesh_material[t] = mat[t];
+    }
+    c.built = false;
+    return AR_OK;
+}
+
+ar_status ar_scene_build(ar_ctx* ctx)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    const int nobj = (int)c.objects.size();
+    const int nmesh = (int)c.mesh_material.size();
+    const long long nprim = (long long)nobj + nmesh;
+    const int nmat = (int)c.materials.size();
+    if (nprim == 0) return fail(ctx, AR_ERR_INVALID, "scene is empty");
+    for (int i = 0; i < nobj; ++i)
+        if (c.object_material[i] < 0 || c.object_material[i] >= nmat) return fail(ctx, AR_ERR_INVALID, "object material index out of range");
+    for (int i = 0; i < nmesh; ++i)
+        if (c.mesh_material[i] < 0 || c.mesh_material[i] >= nmat) return fail(ctx, AR_ERR_INVALID, "mesh material index out of range");
+
+    // primitives for the BVH
+    std::vector<arbvh::PrimInput> prims((size_t)nprim);
+    std::vector<int> prim_material((size_t)nprim), prim_light((size_t)nprim, -1);
+    for (long long i = 0; i < nprim; ++i)
+    {
+        arbvh::PrimInput& p = prims[i];
+        p.id = (uint32_t)i;
+        const float* tv = nullptr;
+        if (i < nobj)
+        {
+            prim_material[i] = c.object_material[i];
+            if (c.object_type[i] == AR_OBJECT_TRIANGLE) tv = &c.object_tri[9 * (size_t)i];
+            else
+            {
+                p.kind = c.object_type[i] == AR_OBJECT_CUBE ? AR_PRIM_KIND_BOX : AR_PRIM_KIND_SPHERE;
+                object_bounds(c.objects[i], p.lo, p.hi);
+            }
+        }
+        else
+        {
+            prim_material[i] = c.mesh_material[i - nobj];
+            tv = &c.mesh_v[9 * (size_t)(i - nobj)];
+        }
+        if (tv)
+        {
+            p.kind = AR_PRIM_KIND_TRI;
+            std::memcpy(p.v, tv, 9 * sizeof(float));
+            for (int k = 0; k < 3; ++k)
+            {
+                p.lo[k] = std::min(tv[k], std::min(tv[3 + k], tv[6 + k]));
+                p.hi[k] = std::max(tv[k], std::max(tv[3 + k], tv[6 + k]));
+            }
+        }
+    }
+    std::string err;
+    if (!arbvh::build_wide_bvh(prims, c.bvh, &err)) return fail(ctx, AR_ERR_INVALID, "BVH build: " + err);
+    if (c.bvh.depth >= AR_TRAV_STACK) return fail(ctx, AR_ERR_INVALID, "BVH deeper than the traversal stack");
+    std::vector<int> prim_slot((size_t)nprim, -1);
+    for (size_t s = 0; s < c.bvh.slots.size(); ++s)
+    {
+        uint32_t tag;
+        std::memcpy(&tag, &c.bvh.slots[s].a[3], 4);
+        prim_slot[tag & AR_PRIM_ID_MASK] = (int)s;
+    }
+
+    // light table (core/scene.cu:677-706): every primitive with a light material
+    c.lights.clear();
+    float total = 0.0f;
+    std::vector<float> weights;
+    for (long long i = 0; i < nprim; ++i)
+    {
+        const Material& m = c.materials[prim_material[i]];
+        if (m.shading != AR_MAT_LIGHT) continue;
+        Light L;
+        L.obj = (int)i;
+        L.type = (i < nobj) ? c.object_type[i] : AR_OBJ_TRIANGLE;
+        L.material = prim_material[i];
+        const float area = (i < nobj) ? object_area(c.objects[i]) : 0.0f;
+        const float w = fmaxf(area * luminance(m.emissive), 1.0e-20f);
+        total += w;
+        weights.push_back(w);
+        prim_light[i] = (int)c.lights.size();
+        c.lights.push_back(L);
+    }
+    float acc = 0.0f;
+    for (size_t k = 0; k < c.lights.size(); ++k)
+    {
+        c.lights[k].select_prob = weights[k] / total;
+        acc += c.lights[k].select_prob;
+        c.lights[k].cdf = acc;
+    }
+
+    // device upload
+    free_scene(c);
+    std::vector<Object> objs(c.objects);
+    if (objs.empty()) objs.resize(1);
+    AR_CUDA(ctx, alloc_dev(c.d_nodes, c.bvh.nodes.size() * sizeof(ar_wide_node)));
+    AR_CUDA(ctx, cudaMemcpy(c.d_nodes, c.bvh.nodes.data(), c.bvh.nodes.size() * sizeof(ar_wide_node), cudaMemcpyHostToDevice));
+    AR_CUDA(ctx, alloc_dev(c.d_slots, c.bvh.slots.size() * sizeof(ar_prim_slot)));
+    AR_CUDA(ctx, cudaMemcpy(c.d_slots, c.bvh.slots.data(), c.bvh.slots.size() * sizeof(ar_prim_slot), cudaMemcpyHostToDevice));
+    AR_CUDA(ctx, alloc_dev(c.d_objects, objs.size()));
+    AR_CUDA(ctx, cudaMemcpy(c.d_objects, objs.data(), objs.size() * sizeof(Object), cudaMemcpyHostToDevice));
+    AR_CUDA(ctx, alloc_dev(c.d_prim_material, (size_t)nprim));
+    AR_CUDA(ctx, cudaMemcpy(c.d_prim_material, prim_material.data(), nprim * sizeof(int), cudaMemcpyHostToDevice));
+    AR_CUDA(ctx, alloc_dev(c.d_prim_light, (size_t)nprim));
+    AR_CUDA(ctx, cudaMemcpy(c.d_prim_light, prim_light.data(), nprim * sizeof(int), cudaMemcpyHostToDevice));
+    AR_CUDA(ctx, alloc_dev(c.d_prim_slot, (size_t)nprim));
+    AR_CUDA(ctx, cudaMemcpy(c.d_prim_slot, prim_slot.data(), nprim * sizeof(int), cudaMemcpyHostToDevice));
+    AR_CUDA(ctx, alloc_dev(c.d_lights, c.lights.size()));
+    if (!c.lights.empty())
+        AR_CUDA(ctx, cudaMemcpy(c.d_lights, c.lights.data(), c.lights.size() * sizeof(Light), cudaMemcpyHostToDevice));
+
+    // spectral RGB LUT (2 GiB, built once per context on the GPU)
+    if (!c.d_lut_rgb)
+    {
+        const size_t bytes = (size_t)AR_LUT_RES * AR_LUT_RES * AR_LUT_RES * 4 * sizeof(float);
+        AR_CUDA(ctx, cudaMalloc((void**)&c.d_lut_rgb, bytes));
+        float* d_w = nullptr;
+        AR_CUDA(ctx, cudaMalloc((void**)&d_w, sizeof(AR_TAB_RGB_MLP)));
+        cudaError_t e = cudaMemcpy(d_w, AR_TAB_RGB_MLP, sizeof(AR_TAB_RGB_MLP), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_build_rgb_lut(c.d_lut_rgb, d_w, c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        cudaFree(d_w);
+        if (e != cudaSuccess)
+        {
+            free_dev(c.d_lut_rgb);
+            return cuda_fail(ctx, e, "spectral LUT build");
+        }
+    }
+    std::vector<Material> mats(c.materials);
+    AR_CUDA(ctx, alloc_dev(c.d_materials, std::max<size_t>(mats.size(), 1)));
+    if (!mats.empty())
+    {
+        AR_CUDA(ctx, cudaMemcpy(c.d_materials, mats.data(), mats.size() * sizeof(Material), cudaMemcpyHostToDevice));
+        AR_CUDA(ctx, launch_prepare_materials(c.d_materials, (int)mats.size(), c.d_lut_rgb, c.stream));
+        AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
+    }
+    c.built = true;
+    return AR_OK;
+}
+
+ar_status ar_scene_stats(ar_ctx* ctx, int64_t* n_nodes, int64_t* n_slots, int32_t* depth, int64_t* device_bytes)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    const Ctx& c = ctx->c;
+    if (n_nodes) *n_nodes = (int64_t)c.bvh.nodes.size();
+    if (n_slots) *n_slots = (int64_t)c.bvh.slots.size();
+    if (depth) *depth = c.bvh.depth;
+    if (device_bytes)
+        *device_bytes = (int64_t)(c.bvh.nodes.size() * sizeof(ar_wide_node) + c.bvh.slots.size() * sizeof(ar_prim_slot));
+    return AR_OK;
+}
+
+ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, int out_is_device, float* per_sample_xyz,
+                    void* stream)
+{
+    (void)stream;
+    if (!ctx || !prm || !out_xyz) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (!c.built) return fail(ctx, AR_ERR_STATE, "render before ar_scene_build");
+    if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth <= 0 || prm->max_depth > 0xffff)
+        return fail(ctx, AR_ERR_INVALID, "render: bad resolution, spp or depth");
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    RenderLaunch rl;
+    rl.width = prm->width;
+    rl.height = prm->height;
+    rl.spp = prm->spp;
+    rl.max_depth = prm->max_depth;
+    for (int k = 0; k < 3; ++k)
+    {
+        rl.cam_o[k] = prm->cam_origin[k];
+        rl.cam_d[k] = prm->cam_dir[k];
+    }
+    rl.fov_deg = prm->fov_deg;
+    rl.use_nee = prm->use_nee;
+    rl.seed = prm->seed;
+    rl.first_frame = prm->first_frame;
+    rl.profile = prm->profile;
+    c.profile = prm->profile != 0;
+    c.stage_events.clear();
+    for (int k = 0; k < ST_COUNT; ++k)
+    {
+        c.stage_ms[k] = 0.0f;
+        c.stage_launches[k] = 0;
+    }
+    if (c.profile)
+    {
+        if (!c.d_stats) AR_CUDA(ctx, cudaMalloc((void**)&c.d_stats, 8 * sizeof(unsigned long long)));
+        AR_CUDA(ctx, cudaMemsetAsync(c.d_stats, 0, 8 * sizeof(unsigned long long), c.stream));
+    }
+    // camera inside a medium (intersection::Overlap, core/render/intersection.cuh:312-327)
+    c.camera_inside = 0;
+    {
+        const V3 co = v3(rl.cam_o[0], rl.cam_o[1], rl.cam_o[2]);
+        for (size_t i = 0; i < c.objects.size(); ++i)
+            if (c.object_type[i] != AR_OBJECT_TRIANGLE && overlap_object(co, c.objects[i]))
+            {
+                c.camera_inside = 1;
+                break;
+            }
+    }
+    const long long npix = (long long)rl.width * rl.height;
+    const long long total = npix * rl.spp;
+    int cap = prm->wave_paths > 0 ? prm->wave_paths : (1 << 21);
+    if ((long long)cap > total) cap = (int)total;
+    ar_status st = ensure_waves(ctx, cap);
+    if (st != AR_OK) return st;
+    if (c.accum_pixels < (size_t)npix)
+    {
+        free_dev(c.d_accum);
+        AR_CUDA(ctx, cudaMalloc((void**)&c.d_accum, (size_t)npix * 3 * sizeof(double)));
+        c.accum_pixels = (size_t)npix;
+    }
+    AR_CUDA(ctx, cudaMemsetAsync(c.d_accum, 0, (size_t)npix * 3 * sizeof(double), c.stream));
+    float* d_samples = nullptr;
+    if (per_sample_xyz) AR_CUDA(ctx, cudaMalloc((void**)&d_samples, (size_t)cap * 3 * sizeof(float)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c.stream);
+    long long launches = 0;
+    cudaError_t e = cudaSuccess;
+    for (long long first = 0; first < total && e == cudaSuccess; first += cap)
+    {
+        const int n = (int)std::min<long long>(cap, total - first);
+        e = launch_render_wave(c, rl, first, n, d_samples, &launches);
+        if (e == cudaSuccess) e = launch_accumulate(c, rl, first, n, c.d_accum, &launches);
+        if (e == cudaSuccess && per_sample_xyz)
+            e = cudaMemcpyAsync(per_sample_xyz + 3 * first, d_samples, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, c.stream);
+    }
+    cudaEventRecord(e1, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) cudaEventElapsedTime(&c.last_render_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (d_samples) cudaFree(d_samples);
+    c.last_launches = launches;
+    for (const StageEvent& se : c.stage_events)
+    {
+        float ms = 0.0f;
+        if (e == cudaSuccess && cudaEventElapsedTime(&ms, se.a, se.b) == cudaSuccess) c.stage_ms[se.stage] += ms;
+        cudaEventDestroy(se.a);
+        cudaEventDestroy(se.b);
+    }
+    c.stage_events.clear();
+    if (c.profile && e == cudaSuccess)
+        e = cudaMemcpy(c.stats, c.d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    c.profile = false;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
+    // mean over samples
+    std::vector<double> sums((size_t)npix * 3);
+    AR_CUDA(ctx, cudaMemcpy(sums.data(), c.d_accum, sums.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    const double inv = 1.0 / (double)rl.spp;
+    for (auto& s : sums) s *= inv;
+    if (out_is_device) AR_CUDA(ctx, cudaMemcpy(out_xyz, sums.data(), sums.size() * sizeof(double), cudaMemcpyHostToDevice));
+    else std::memcpy(out_xyz, sums.data(), sums.size() * sizeof(double));
+    unsigned int word = 0;
+    AR_CUDA(ctx, cudaMemcpy(&word, c.d_err, sizeof(word), cudaMemcpyDeviceToHost));
+    if (word) return fail(ctx, AR_ERR_DEVICE, "device error word set: " + std::to_string(word));
+    return AR_OK;
+}
+
+ar_status ar_trace_closest(ar_ctx* ctx, const float* rays, int n, int32_t* prim_id, float* t, void* stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!rays || !prim_id))) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (!c.built) return fail(ctx, AR_ERR_STATE, "trace before ar_scene_build");
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    long long L = 0;
+    const cudaError_t e = launch_trace(dev_scene(c), rays, n, 0, prim_id, t, c.d_err, s, &L);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace_closest");
+    c.last_launches = L;
+    return AR_OK;
+}
+
+ar_status ar_trace_any(ar_ctx* ctx, const float* rays, int n, int32_t* hit, void* stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!rays || !hit))) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (!c.built) return fail(ctx, AR_ERR_STATE, "trace before ar_scene_build");
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    long long L = 0;
+    const cudaError_t e = launch_trace(dev_scene(c), rays, n, 1, hit, nullptr, c.d_err, s, &L);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace_any");
+    c.last_launches = L;
+    return AR_OK;
+}
+
+ar_status ar_last_render_stats(ar_ctx* ctx, float* ms, int64_t* launches)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    if (ms) *ms = ctx->c.last_render_ms;
+    if (launches) *launches = ctx->c.last_launches;
+    return AR_OK;
+}
+
+ar_status ar_last_render_profile(ar_ctx* ctx, ar_render_profile* out)
+{
+    if (!ctx || !out) return AR_ERR_INVALID;
+    const Ctx& c = ctx->c;
+    out->raygen_ms = c.stage_ms[ST_RAYGEN];
+    out->extend_ms = c.stage_ms[ST_EXTEND];
+    out->shade_ms = c.stage_ms[ST_SHADE];
+    out->shadow_ms = c.stage_ms[ST_SHADOW];
+    out->finalize_ms = c.stage_ms[ST_FINAL];
+    out->extend_node_visits = (int64_t)c.stats[0];
+    out->extend_prim_tests = (int64_t)c.stats[1];
+    out->shadow_node_visits = (int64_t)c.stats[2];
+    out->shadow_prim_tests = (int64_t)c.stats[3];
+    out->extend_rays = (int64_t)c.stats[4];
+    out->shadow_rays = (int64_t)c.stats[5];
+    out->extend_launches = c.stage_launches[ST_EXTEND];
+    out->shade_launches = c.stage_launches[ST_SHADE];
+    out->shadow_launches = c.stage_launches[ST_SHADOW];
+    return AR_OK;
+}
+
+ar_status ar_get_error_word(ar_ctx* ctx, uint32_t* word)
+{
+    if (!ctx || !word) return AR_ERR_INVALID;
+    unsigned int w = 0;
+    AR_CUDA(ctx, cudaMemcpy(&w, ctx->c.d_err, sizeof(w), cudaMemcpyDeviceToHost));
+    *word = w;
+    return AR_OK;
+}
+
+ar_status ar_clear_error_word(ar_ctx* ctx)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    AR_CUDA(ctx, cudaMemset(ctx->c.d_err, 0, sizeof(unsigned int)));
+    return AR_OK;
+}
+
+ar_status ar_host_rgb_encode(const float* rgb, int n, float* out)
+{
+    if (n < 0 || (n > 0 && (!rgb || !out))) return AR_ERR_INVALID;
+    for (int i = 0; i < n; ++i) rgb_encode(rgb + 3 * (size_t)i, out + 4 * (size_t)i, AR_TAB_RGB_MLP);
+    return AR_OK;
+}
+
+ar_status ar_host_lambda_encode(const float* lam, int n, float* out)
+{
+    if (n < 0 || (n > 0 && (!lam || !out))) return AR_ERR_INVALID;
+    for (int i = 0; i < n; ++i) lambda_encode(lam[i], out + 4 * (size_t)i, AR_TAB_LAM_MLP);
+    return AR_OK;
+}
+
+ar_status ar_host_sample_lambda(const float* u3, int n, float* lam, float* pdf)
+{
+    if (n < 0 || (n > 0 && (!u3 || !lam || !pdf))) return AR_ERR_INVALID;
+    for (int i = 0; i < n; ++i)
+    {
+        const LambdaSample s = sample_cie1931(u3[3 * i], u3[3 * i + 1], u3[3 * i + 2]);
+        lam[i] = s.lambda;
+        pdf[i] = s.pdf;
+    }
+    return AR_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,650 @@
+// Wavefront spectral path tracer (sm_103a) and the spectral LUT builder.
+//
+// The reference runs one megakernel thread per pixel sample through the whole
+// path (CalculateRadiance, core/render/render.cuh:460-999).  Here each bounce is
+// split into kernels over compacted queues of live paths:
+//   raygen  -> camera ray + hero wavelength           (core/scene.cu:146-164, render.cuh:466-473)
+//   extend  -> closest-hit traversal                  (render.cuh:77-108)
+//   shade   -> material sample/eval, hit offset, emitter MIS, NEE light sample,
+//              Russian roulette, next ray             (render.cuh:109-163, 541-907)
+//   shadow  -> any-hit traversal of the NEE segments  (render.cuh:254-263)
+//   finalize/accumulate -> XYZ per sample, FP64 per-pixel sums in sample order.
+// Per path, random numbers are drawn in exactly the reference's order, so the
+// GPU replays the reference's paths (see ar_rng.h for the stream layout).
+// Queues are compacted with warp ballots and one atomic per warp.
+#include <cuda_runtime.h>
+
+#include "ar_internal.h"
+#include "ar_rng.h"
+
+namespace ar
+{
+#define AR_BLOCK 256
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// warp-aggregated append: one atomic per warp, order within the warp by lane
+__device__ __forceinline__ int warp_append_slot(int* counter, bool pred)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    int base = 0;
+    if (lane_id() == 0 && m) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + __popc(m & ((1u << lane_id()) - 1u));
+}
+
+struct DevRand
+{
+    ar_pcg g;
+    __device__ float operator()() { return ar_rand1(&g); }
+};
+
+// ---------------------------------------------------------------- LUT build
+// RGB -> basis LUT, one lattice point per thread; MLP weights staged in shared
+// memory (34 KB, read as broadcast), the same arithmetic as rgb_encode.
+__global__ void __launch_bounds__(AR_BLOCK) k_build_rgb_lut(float4* __restrict__ lut, const float* __restrict__ w)
+{
+    __shared__ float sw[AR_RGB_MLP_FLOATS];
+    for (int i = threadIdx.x; i < AR_RGB_MLP_FLOATS; i += blockDim.x) sw[i] = w[i];
+    __syncthreads();
+    const long long total = (long long)AR_LUT_RES * AR_LUT_RES * AR_LUT_RES;
+    const float invRes = 1.0f / static_cast<float>(AR_LUT_RES);
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < total; v += (long long)gridDim.x * blockDim.x)
+    {
+        const int x = (int)(v % AR_LUT_RES);
+        const int y = (int)((v / AR_LUT_RES) % AR_LUT_RES);
+        const int z = (int)(v / ((long long)AR_LUT_RES * AR_LUT_RES));
+        const float in3[3] = {(x + 0.5f) * invRes, (y + 0.5f) * invRes, (z + 0.5f) * invRes};
+        float o[4];
+        rgb_encode(in3, o, sw);
+        lut[v] = make_float4(o[0], o[1], o[2], o[3]);
+    }
+}
+
+cudaError_t launch_build_rgb_lut(float* lut, const float* weights_dev, cudaStream_t s)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_build_rgb_lut<<<sms * 4, AR_BLOCK, 0, s>>>(reinterpret_cast<float4*>(lut), weights_dev);
+    return cudaGetLastError();
+}
+
+// Per-material spectral colours (albedo and emission bases), computed with
+// the same trilinear LUT query the reference performs per interaction.
+__global__ void k_prepare_materials(Material* mats, int n, const float* __restrict__ lut)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const PlainFetch f{lut};
+    mats[i].albedo_c = prepare_color(mats[i].albedo, f);
+    mats[i].emissive_c = prepare_color(mats[i].emissive, f);
+}
+
+cudaError_t launch_prepare_materials(Material* mats, int n, const float* lut, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    k_prepare_materials<<<(n + 127) / 128, 128, 0, s>>>(mats, n, lut);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- hit reconstruction
+// Full hit record for primitive slot `slot` at distance t (the traversal's t).
+__device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, V3 d, float t, Hit* h)
+{
+    const float4 a = __ldg(&sc.trav.slots[3 * (size_t)slot + 0]);
+    const uint32_t tag = __float_as_uint(a.w);
+    const uint32_t kind = tag >> AR_PRIM_KIND_SHIFT;
+    const int id = (int)(tag & AR_PRIM_ID_MASK);
+    h->hit = true;
+    h->obj = id;
+    h->light = sc.prim_light[id];
+    h->dist = t;
+    if (kind == AR_PRIM_KIND_TRI)
+    {
+        const float4 b = __ldg(&sc.trav.slots[3 * (size_t)slot + 1]);
+        const float4 c = __ldg(&sc.trav.slots[3 * (size_t)slot + 2]);
+        tri_frame(o, d, t, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &h->pos, &h->nrm);
+        h->local_pos = v3(0.0f, 0.0f, 0.0f);
+    }
+    else
+    {
+        const Object ob = sc.trav.objects[id];
+        if (kind == AR_PRIM_KIND_BOX) intersect_box(o, d, ob, h, true);
+        else intersect_sphere(o, d, ob, h, true);
+    }
+}
+
+// ---------------------------------------------------------------- raygen
+struct CamParams
+{
+    V3 o, d, right, up;
+    float tan_x, tan_y;
+};
+
+__global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, int* counter, long long first_path, int n,
+                                                   int width, int height, uint64_t seed, int first_frame, CamParams cam,
+                                                   int camera_inside)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) *counter = n;
+    if (k >= n) return;
+    const long long npix = (long long)width * height;
+    const long long g = first_path + k;
+    const uint32_t pixel = (uint32_t)(g % npix);
+    const uint32_t frame = (uint32_t)(g / npix) + (uint32_t)first_frame;
+    const int i = (int)(pixel % (uint32_t)width), j = (int)(pixel / (uint32_t)width);
+    DevRand R;
+    R.g = ar_pcg_init(seed, pixel, frame);
+    const float u = (i + R()) / static_cast<float>(width);
+    const float v = (j + R()) / static_cast<float>(height);
+    const float nx = u * 2.f - 1.f;
+    const float ny = (float)((1.0 - (double)v) * 2.f - 1.f);
+    const float sx = nx * cam.tan_x;
+    const float sy = ny * cam.tan_y;
+    V3 dir = normalize(cam.d + cam.right * sx + cam.up * sy);
+    dir = normalize(dir);  // CalculateRadiance normalizes its input again
+    const float r0 = R(), r1 = R(), r2 = R();
+    const LambdaSample ls = sample_cie1931(r0, r1, r2);
+    ps.rng[k] = R.g.state;
+    ps.pixel[k] = pixel;
+    ps.frame[k] = frame;
+    ps.ray_o[k] = make_float4(cam.o.x, cam.o.y, cam.o.z, ls.lambda);
+    ps.ray_d[k] = make_float4(dir.x, dir.y, dir.z, ls.pdf);
+    ps.radiance[k] = 0.0f;
+    ps.mask[k] = 1.0f;
+    ps.depths[k] = 0u;
+    ps.flags[k] = camera_inside ? 1u : 0u;
+    ps.media_v[k] = make_float4(cam.o.x, cam.o.y, cam.o.z, __int_as_float(-1));
+    ps.media_depth[k] = 0;
+    ps.prev[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    queue[k] = k;
+}
+
+// ---------------------------------------------------------------- extend
+__global__ void __launch_bounds__(AR_BLOCK) k_extend(DevScene sc, PathState ps, const int* __restrict__ queue,
+                                                   const int* __restrict__ counter, unsigned int* err)
+{
+    const int n = *counter;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    {
+        const int p = queue[q];
+        const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
+        const V3 o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
+        const uint32_t dep = ps.depths[p];
+        const int ndd = (int)(dep >> 16);
+        const float tmin = intersect_eps(ndd);
+        const uint32_t fl = ps.flags[p];
+        const int mobj = __float_as_int(ps.media_v[p].w);
+        float t = 0.0f;
+        int slot = -1;
+        if ((fl & 1u) && mobj >= 0)
+        {
+            // inside a medium: intersect only the enclosing object (render.cuh:89-92)
+            const int s = sc.prim_slot[mobj];
+            int id;
+            const float th = prim_hit(sc.trav, s, make_shear(d), o, d, &id);
+            if (th >= tmin)
+            {
+                t = th;
+                slot = s;
+            }
+        }
+        else
+        {
+            const TravResult r = traverse<false>(sc.trav, o, d, tmin, __int_as_float(0x7f800000), err,
+                                                 sc.stats ? sc.stats + 0 : nullptr);
+            t = r.t;
+            slot = r.slot;
+        }
+        if (sc.stats) atomicAdd(&sc.stats[4], 1ull);
+        ps.hit_t[p] = t;
+        ps.hit_slot[p] = slot;
+    }
+}
+
+// ---------------------------------------------------------------- shade
+struct ShadeParams
+{
+    int use_nee;
+    int max_depth;
+};
+
+__global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
+                                                  const int* __restrict__ counter, int* next_queue, int* next_counter,
+                                                  int* shadow_counter, ShadeParams prm)
+{
+    __shared__ float s_lam[AR_LAMBDA_LUT_RES * 4];
+    for (int i = threadIdx.x; i < AR_LAMBDA_LUT_RES * 4; i += blockDim.x) s_lam[i] = sc.lut_lambda[i];
+    __syncthreads();
+    const int n = *counter;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride)
+    {
+        const int q = base + lane_id();
+        const bool active = q < n;
+        bool keep = false;
+        bool shadow = false;
+        int p = 0;
+        V3 sh_o = v3(0, 0, 0), sh_d = v3(0, 0, 0);
+        float sh_tmax = 0.0f, sh_vun = 0.0f, sh_vocc = 0.0f;
+        bool sh_valid = false;
+        if (active)
+        {
+            p = queue[q];
+            const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
+            const V3 rayO = v3(ro.x, ro.y, ro.z), rayD = v3(rd.x, rd.y, rd.z);
+            const float lambda = ro.w;
+            const Basis lb = query_lambda(lambda, s_lam);
+            const float d65 = d65_norm(lambda, sc.d65);
+            const uint32_t dep = ps.depths[p];
+            int depth = (int)(dep & 0xffffu);
+            int ndd = (int)(dep >> 16);
+            uint32_t fl = ps.flags[p];
+            const float4 mv = ps.media_v[p];
+            Media media;
+            media.inside = (fl & 1u) != 0u;
+            media.vertex = v3(mv.x, mv.y, mv.z);
+            media.obj = __float_as_int(mv.w);
+            media.depth = ps.media_depth[p];
+            float radiance = ps.radiance[p];
+            float mask = ps.mask[p];
+            const float4 pv = ps.prev[p];
+            const bool prev_did_nee = (fl & 2u) != 0u;
+            DevRand R;
+            R.g.state = ps.rng[p];
+            R.g.inc = ar_pcg_increment(ps.pixel[p]);
+
+            const float eps = intersect_eps(ndd);
+            const int slot = ps.hit_slot[p];
+            Hit h;
+            h.hit = false;
+            h.obj = -1;
+            h.light = -1;
+            h.dist = 0.0f;
+            h.pos = v3(0, 0, 0);
+            h.nrm = v3(0, 0, 0);
+            h.local_pos = v3(0, 0, 0);
+            if (slot >= 0) hit_context(sc, slot, rayO, rayD, ps.hit_t[p], &h);
+
+            // ---- Trace (render.cuh:109-155)
+            BsdfSample S = bsdf_sample_default();
+            Material mat;
+            mat.shading = AR_MAT_DIFFUSE;
+            if (!h.hit && media.inside)
+            {
+                S.miss_thin = true;
+                S.brdf = 1.0f;
+                S.next_dir = rayD;
+                S.pdf = 1.0f;
+                h.local_pos = rayO;
+                h.obj = media.obj;
+                S.delta = true;
+                S.emissive = v3(0, 0, 0);
+                S.media.inside = false;
+                S.media.vertex = h.local_pos;
+            }
+            if (h.hit)
+            {
+                mat = sc.materials[sc.prim_material[h.obj]];
+                S = evaluate_material(lambda, lb, R, mat, rayD, h, media);
+            }
+            else
+            {
+                S.brdf = 1.0f;
+                S.delta = false;
+                S.next_dir = rayD;
+                S.pdf = 1.0f;
+                S.emissive = sky_lighting(rayD);
+                S.media.inside = false;
+            }
+            {
+                const float offsetEPS = eps * fmaxf(1.0f, length(h.pos));
+                h.pos = h.pos + signf(dot(h.nrm, S.next_dir)) * h.nrm * offsetEPS * (R() + 0.5f);
+            }
+            media = S.media;
+
+            // ---- emission (render.cuh:647-723)
+            if (!h.hit)
+            {
+                if (!S.miss_thin)
+                {
+                    const PlainFetch f{sc.lut_rgb};
+                    radiance = radiance + mask * interact_rgb(lb, S.emissive, f) * d65;
+                }
+            }
+            else if (h.light >= 0)
+            {
+                float misW = 1.0f;
+                if (prm.use_nee && depth > 0 && prev_did_nee)
+                {
+                    const float pB = fmaxf(pv.w, 0.0f);
+                    const Light L = sc.lights[h.light];
+                    float pL = 0.0f;
+                    const V3 lastPos = v3(pv.x, pv.y, pv.z);
+                    if (L.type == AR_OBJ_CUBE) pL = box_light_pdf_omega(sc.trav.objects[L.obj], L.select_prob, lastPos, h.pos, h.nrm);
+                    else if (L.type == AR_OBJ_SPHERE) pL = sphere_light_pdf_omega(sc.trav.objects[L.obj], L.select_prob, lastPos, h.pos, h.nrm);
+                    if (pL >= 0.0f && pB > 0.0f) misW = power_heuristic(pB, pL);
+                }
+                radiance = radiance + mask * interact(mat.emissive_c, lb) * d65 * misW;
+            }
+
+            const bool ended = (!h.hit && !S.miss_thin) || S.terminate;
+            if (!ended)
+            {
+                // ---- NEE (render.cuh:766-827, 206-343)
+                if (!S.miss_thin)
+                {
+                    const float useNEERate = sqrtf(saturate(mask));
+                    bool neeValid = false;
+                    if (prm.use_nee && ndd < AR_NEE_MAX_NON_DELTA_DEPTH && !S.delta && !media.inside && R() < useNEERate)
+                    {
+                        LightSample ls;
+                        ls.valid = false;
+                        if (sc.light_count > 0)
+                        {
+                            const float r = R();
+                            int pick = sc.light_count - 1;
+                            float pickProb = 0.0f;
+                            // first light whose running CDF exceeds r (same as the sequential scan)
+                            int lo = 0, hi = sc.light_count;
+                            while (lo < hi)
+                            {
+                                const int mid = (lo + hi) >> 1;
+                                if (r < sc.lights[mid].cdf) hi = mid;
+                                else lo = mid + 1;
+                            }
+                            if (lo < sc.light_count)
+                            {
+                                pick = lo;
+                                pickProb = sc.lights[lo].select_prob;
+                            }
+                            const Light L = sc.lights[pick];
+                            if (L.type == AR_OBJ_CUBE) ls = sample_box_light(R, sc.trav.objects[L.obj], h.pos);
+                            else if (L.type == AR_OBJ_SPHERE) ls = sample_sphere_light(R, sc.trav.objects[L.obj], h.pos);
+                            if (ls.valid)
+                            {
+                                ls.obj = L.obj;
+                                ls.material = L.material;
+                                ls.p_facet = ls.p_facet * pickProb;
+                            }
+                        }
+                        const float vZero = mask * 0.0f * d65;
+                        if (!ls.valid)
+                        {
+                            radiance = radiance + vZero;
+                        }
+                        else
+                        {
+                            const float pATotal = fmaxf(1e-20f, ls.p_a * ls.p_facet);
+                            const V3 lun = ls.point - h.pos;
+                            const float dist2 = fmaxf(dot(lun, lun), (float)1.0e-12);
+                            const V3 L = lun * arm_rsqrtf(dist2);
+                            const float cosX = fmaxf(0.0f, dot(h.nrm, L));
+                            const float cosY = fmaxf(0.0f, dot(ls.normal, -L));
+                            float vUn = vZero;
+                            bool validUn = false;
+                            if (!(cosX <= 0.0f || cosY <= 0.0f))
+                            {
+                                const float brdfCos = eval_bsdf_cos(lambda, lb, mat, rayD, L, h, media_default());
+                                const float G = (cosY / dist2);
+                                const float le = interact(sc.materials[ls.material].emissive_c, lb);
+                                const float contribution = brdfCos * le * (G / pATotal);
+                                const float pLight = area_to_solid_angle_pdf(h.pos, ls.point, ls.normal, ls.p_facet * ls.p_a);
+                                const float pBsdf = fmaxf(bsdf_pdf(lb, mat, h.nrm, rayD, L), 0.0f);
+                                const float misW = power_heuristic(pLight, pBsdf);
+                                vUn = mask * (contribution * misW) * d65;
+                                validUn = true;
+                            }
+                            // shadow segment (intersection.cuh:285-310)
+                            V3 dirS = ls.point - h.pos;
+                            const float distance = length(dirS);
+                            bool traced = false;
+                            if (distance > 0.0f)
+                            {
+                                dirS = dirS / distance;
+                                const float seps = intersect_eps(depth) * fmaxf(1.0f, fmaxf(length(h.pos), length(ls.point)));
+                                const float tmax = fmaxf(0.0f, distance - seps);
+                                if (tmax > 0.0f)
+                                {
+                                    traced = true;
+                                    shadow = true;
+                                    sh_o = h.pos;
+                                    sh_d = dirS;
+                                    sh_tmax = tmax;
+                                    sh_vun = vUn;
+                                    sh_vocc = vZero;
+                                    sh_valid = validUn;
+                                }
+                            }
+                            if (!traced)
+                            {
+                                radiance = radiance + vUn;
+                                neeValid = validUn;
+                            }
+                        }
+                    }
+                    fl = (fl & ~2u) | (neeValid ? 2u : 0u);
+                    ps.prev[p] = make_float4(h.pos.x, h.pos.y, h.pos.z, S.pdf);
+                }
+                // ---- Russian roulette (render.cuh:829-859)
+                const float contrib = S.brdf / fmaxf(S.pdf, 1e-12f);
+                float pSurvive = 1.0f;
+                bool survived = true;
+                if (ndd >= AR_MIN_TRACING_DEPTH)
+                {
+                    const float basic = clampf(mask * 0.5f + mask * 0.5f, 0.05f, 0.95f);
+                    pSurvive = lerpf(basic, 1.0f, media.inside ? AR_DELTA_RR_TERMINATE_REDUCE : 0.0f);
+                    if (R() > pSurvive) survived = false;
+                }
+                if (survived)
+                {
+                    mask = mask * contrib;
+                    mask = mask / pSurvive;
+                    if (!S.delta) ++ndd;
+                    ++depth;
+                    if (depth < prm.max_depth)
+                    {
+                        keep = true;
+                        ps.ray_o[p] = make_float4(h.pos.x, h.pos.y, h.pos.z, lambda);
+                        ps.ray_d[p] = make_float4(S.next_dir.x, S.next_dir.y, S.next_dir.z, rd.w);
+                        ps.mask[p] = mask;
+                        ps.depths[p] = (uint32_t)depth | ((uint32_t)ndd << 16);
+                        fl = (fl & ~1u) | (media.inside ? 1u : 0u);
+                        ps.media_v[p] = make_float4(media.vertex.x, media.vertex.y, media.vertex.z, __int_as_float(media.obj));
+                        ps.media_depth[p] = media.depth;
+                    }
+                }
+            }
+            ps.radiance[p] = radiance;
+            ps.flags[p] = fl;
+            ps.rng[p] = R.g.state;
+        }
+        const int nq = warp_append_slot(next_counter, keep);
+        if (keep) next_queue[nq] = p;
+        const int sqi = warp_append_slot(shadow_counter, shadow);
+        if (shadow)
+        {
+            sq.path[sqi] = p;
+            sq.o[sqi] = make_float4(sh_o.x, sh_o.y, sh_o.z, sh_tmax);
+            sq.d[sqi] = make_float4(sh_d.x, sh_d.y, sh_d.z, sh_vun);
+            sq.v_occ[sqi] = sh_vocc;
+            sq.valid_unocc[sqi] = sh_valid ? 1 : 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- shadow
+__global__ void __launch_bounds__(AR_BLOCK) k_shadow(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ counter,
+                                                   unsigned int* err)
+{
+    const int n = *counter;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const float4 o = sq.o[i], d = sq.d[i];
+        const int p = sq.path[i];
+        const TravResult r = traverse<true>(sc.trav, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, o.w, err,
+                                            sc.stats ? sc.stats + 2 : nullptr);
+        if (sc.stats) atomicAdd(&sc.stats[5], 1ull);
+        const bool occluded = r.slot >= 0;
+        ps.radiance[p] = ps.radiance[p] + (occluded ? sq.v_occ[i] : d.w);
+        const bool valid = occluded ? true : (sq.valid_unocc[i] != 0);
+        ps.flags[p] = (ps.flags[p] & ~2u) | (valid ? 2u : 0u);
+    }
+}
+
+// ---------------------------------------------------------------- finalize / accumulate
+__device__ __forceinline__ float nan_inf_to_zero(float x)
+{
+    if (x != x) return 0.0f;
+    if (fabsf(x) == __int_as_float(0x7f800000)) return x > 0.0f ? 0.0f : -0.0f;
+    return x;
+}
+
+__global__ void k_finalize(DevScene sc, PathState ps, int n, float* __restrict__ extra_out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float lambda = ps.ray_o[k].w;
+    const float pdf = ps.ray_d[k].w;
+    const V3 xyz = lambda_to_xyz(lambda, sc.cie_cmf);
+    const float r = nan_inf_to_zero(ps.radiance[k]);
+    const float x = fmaxf(0.0f, clampf(xyz.x * r / pdf, 0.0f, AR_RADIANCE_CLAMP));
+    const float y = fmaxf(0.0f, clampf(xyz.y * r / pdf, 0.0f, AR_RADIANCE_CLAMP));
+    const float z = fmaxf(0.0f, clampf(xyz.z * r / pdf, 0.0f, AR_RADIANCE_CLAMP));
+    ps.out_xyz[3 * k + 0] = x;
+    ps.out_xyz[3 * k + 1] = y;
+    ps.out_xyz[3 * k + 2] = z;
+    if (extra_out)
+    {
+        extra_out[3 * k + 0] = x;
+        extra_out[3 * k + 1] = y;
+        extra_out[3 * k + 2] = z;
+    }
+}
+
+// per pixel, adds the wave's samples in increasing sample order (deterministic)
+__global__ void k_accumulate(const float* __restrict__ out_xyz, long long first_path, int n, long long npix,
+                             double* __restrict__ accum)
+{
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    long long g = first_path - (first_path % npix) + p;
+    if (g < first_path) g += npix;
+    double sx = accum[3 * p], sy = accum[3 * p + 1], sz = accum[3 * p + 2];
+    bool any = false;
+    for (; g < first_path + n; g += npix)
+    {
+        const long long k = g - first_path;
+        sx += (double)out_xyz[3 * k];
+        sy += (double)out_xyz[3 * k + 1];
+        sz += (double)out_xyz[3 * k + 2];
+        any = true;
+    }
+    if (any)
+    {
+        accum[3 * p] = sx;
+        accum[3 * p + 1] = sy;
+        accum[3 * p + 2] = sz;
+    }
+}
+
+static CamParams make_camera(const RenderLaunch& rl)
+{
+    CamParams c;
+    c.o = v3(rl.cam_o[0], rl.cam_o[1], rl.cam_o[2]);
+    c.d = v3(rl.cam_d[0], rl.cam_d[1], rl.cam_d[2]);
+    const float FOV = rl.fov_deg * 3.1415926f / 180.0f;
+    const float aspect = static_cast<float>(rl.width) / fmaxf(1.0f, static_cast<float>(rl.height));
+    c.tan_y = arm_tanf(0.5f * FOV);
+    c.tan_x = c.tan_y * aspect;
+    c.right = normalize(cross(c.d, v3(0.0f, 1.0f, 0.0f)));
+    c.up = normalize(cross(c.d, c.right));
+    return c;
+}
+
+// records a stage interval when profiling
+struct StageScope
+{
+    Ctx& c;
+    int stage;
+    cudaEvent_t a = nullptr;
+    StageScope(Ctx& cc, int st) : c(cc), stage(st)
+    {
+        if (c.profile)
+        {
+            cudaEventCreate(&a);
+            cudaEventRecord(a, c.stream);
+        }
+    }
+    ~StageScope()
+    {
+        if (c.profile)
+        {
+            cudaEvent_t b;
+            cudaEventCreate(&b);
+            cudaEventRecord(b, c.stream);
+            c.stage_events.push_back(StageEvent{stage, a, b});
+            c.stage_launches[stage] += 1;
+        }
+    }
+};
+
+cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_path, int n, float* per_sample_out,
+                               long long* launches)
+{
+    const DevScene sc = dev_scene(c);
+    cudaStream_t s = c.stream;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
+    const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
+    const int grid_p = sms * 8;
+    int* cnt = c.d_counters;  // [0],[1]: extend queues, [2]: shadow
+    const CamParams cam = make_camera(rl);
+    {
+        StageScope st(c, ST_RAYGEN);
+        k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, c.d_queue[0], &cnt[0], first_path, n, rl.width, rl.height, rl.seed,
+                                             rl.first_frame, cam, c.camera_inside);
+    }
+    long long L = 1;
+    ShadeParams prm;
+    prm.use_nee = rl.use_nee;
+    prm.max_depth = rl.max_depth;
+    for (int b = 0; b < rl.max_depth; ++b)
+    {
+        const int cur = b & 1, nxt = cur ^ 1;
+        cudaMemsetAsync(&cnt[nxt], 0, sizeof(int), s);
+        cudaMemsetAsync(&cnt[2], 0, sizeof(int), s);
+        {
+            StageScope st(c, ST_EXTEND);
+            k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], &cnt[cur], c.d_err);
+        }
+        {
+            StageScope st(c, ST_SHADE);
+            k_shade<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur], c.d_queue[nxt], &cnt[nxt],
+                                                &cnt[2], prm);
+        }
+        {
+            StageScope st(c, ST_SHADOW);
+            k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[2], c.d_err);
+        }
+        L += 3;
+    }
+    {
+        StageScope st(c, ST_FINAL);
+        k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, c.ps, n, per_sample_out);
+    }
+    ++L;
+    if (launches) *launches += L;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate(Ctx& c, const RenderLaunch& rl, long long first_path, int n, double* accum, long long* launches)
+{
+    const long long npix = (long long)rl.width * rl.height;
+    const int grid = (int)((npix + AR_BLOCK - 1) / AR_BLOCK);
+    k_accumulate<<<grid, AR_BLOCK, 0, c.stream>>>(c.ps.out_xyz, first_path, n, npix, accum);
+    if (launches) *launches += 1;
+    return cudaGetLastError();
+}
+} // namespace ar

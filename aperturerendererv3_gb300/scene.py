@@ -1,0 +1,313 @@
+"""Host-side mirror of the reference's scene interface.
+
+Names, argument meaning and defaults follow the reference so calling code reads
+the same:
+  Material.Create*                core/render/object.cuh:119-206
+  SceneObject(center, extent, material, rotation, type)
+                                  core/render/object.cuh:227-316
+  SceneRenderer(objects).Render(size, origin, direction, sampleNum)
+                                  core/scene.hpp:94-114, core/scene.cu:210-238
+  Camera(renderer, name, resX, resY, position, direction).RenderToFile(...)
+                                  core/camera.hpp:56-99, core/camera.cu:64-89
+Differences, all additive: triangles and triangle meshes (the reference has
+none), a field of view argument (the reference fixes 60 degrees), a path-depth
+cap, and FP64 accumulation of the returned linear XYZ.  Everything runs through
+the C ABI (include/aperture/ar.h); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import (GLOBAL_SEED, OBJECT_CUBE, OBJECT_SPHERE, OBJECT_TRIANGLE, SHADING_DIFFUSE, SHADING_GGX,
+                   SHADING_GLASS, SHADING_LIGHT, ArMaterial, ArObject, ArRenderParams, check)
+
+Vec3 = Sequence[float]
+
+
+def _f3(v: Vec3) -> tuple[float, float, float]:
+    return (float(v[0]), float(v[1]), float(v[2]))
+
+
+@dataclass(frozen=True)
+class Material:
+    shading: int = SHADING_DIFFUSE
+    albedo: tuple = (1.0, 1.0, 1.0)
+    emissive: tuple = (0.0, 0.0, 0.0)
+    roughness: float = 0.0
+    metallic: float = 0.0
+    specular: float = 0.0
+    ior: float = 1.5
+    sigma_a: float = 100.0
+    abbe: float = 20.0
+    tilt: float = 0.0
+
+    @staticmethod
+    def CreateDiffusePureColor(color: Vec3, emissive: Vec3 = (0.0, 0.0, 0.0)) -> "Material":
+        return Material(SHADING_DIFFUSE, _f3(color), _f3(emissive))
+
+    @staticmethod
+    def CreateLight(emissive: Vec3) -> "Material":
+        return Material(SHADING_LIGHT, (0.0, 0.0, 0.0), _f3(emissive))
+
+    @staticmethod
+    def CreateGlassPureColor(color: Vec3, IOR: float, sigmaA: float, abbeNumber: float = 20.0,
+                             tiltNumber: float = 0.0) -> "Material":
+        return Material(SHADING_GLASS, _f3(color), (0.0, 0.0, 0.0), ior=float(IOR), sigma_a=float(sigmaA),
+                        abbe=float(abbeNumber), tilt=float(tiltNumber))
+
+    @staticmethod
+    def CreateGGXPureColor(baseColor: Vec3, roughness: float, metallic: float, specular: float,
+                           emissive: Vec3 = (0.0, 0.0, 0.0)) -> "Material":
+        return Material(SHADING_GGX, _f3(baseColor), _f3(emissive), roughness=float(roughness),
+                        metallic=float(metallic), specular=float(specular))
+
+    def to_c(self) -> ArMaterial:
+        m = ArMaterial()
+        m.shading = self.shading
+        m.albedo[:] = self.albedo
+        m.emissive[:] = self.emissive
+        m.roughness, m.metallic, m.specular = self.roughness, self.metallic, self.specular
+        m.ior, m.sigma_a, m.abbe, m.tilt = self.ior, self.sigma_a, self.abbe, self.tilt
+        return m
+
+
+@dataclass
+class SceneObject:
+    center: tuple = (0.0, 0.0, 0.0)
+    extent: tuple = (0.0, 0.0, 0.0)
+    material: Material = field(default_factory=Material)
+    rotation: tuple = (0.0, 0.0, 0.0)  # Euler angles in degrees
+    type: int = OBJECT_CUBE
+    v0: tuple = (0.0, 0.0, 0.0)
+    v1: tuple = (0.0, 0.0, 0.0)
+    v2: tuple = (0.0, 0.0, 0.0)
+
+    @staticmethod
+    def Triangle(v0: Vec3, v1: Vec3, v2: Vec3, material: Material) -> "SceneObject":
+        return SceneObject(material=material, type=OBJECT_TRIANGLE, v0=_f3(v0), v1=_f3(v1), v2=_f3(v2))
+
+
+@dataclass
+class TriangleMesh:
+    """Indexed triangles sharing a material table (large meshes)."""
+    vertices: np.ndarray          # (nv, 3) float32
+    indices: np.ndarray           # (nt, 3) uint32
+    material_ids: np.ndarray      # (nt,) int32 into `materials`
+    materials: list
+
+    def triangle_vertices(self) -> np.ndarray:
+        return np.asarray(self.vertices, np.float32)[np.asarray(self.indices, np.int64)].reshape(-1, 9)
+
+
+def flatten(objects: Iterable[SceneObject], mesh: TriangleMesh | None = None):
+    """Material table + C object array + mesh arrays for the C ABI."""
+    objects = list(objects)
+    table: dict[Material, int] = {}
+    mats: list[Material] = []
+
+    def mid(m: Material) -> int:
+        if m not in table:
+            table[m] = len(mats)
+            mats.append(m)
+        return table[m]
+
+    arr = (ArObject * max(1, len(objects)))()
+    for i, o in enumerate(objects):
+        a = arr[i]
+        a.type = o.type
+        a.material = mid(o.material)
+        a.center[:] = _f3(o.center)
+        a.extent[:] = _f3(o.extent)
+        a.rotation_deg[:] = _f3(o.rotation)
+        a.v0[:] = _f3(o.v0)
+        a.v1[:] = _f3(o.v1)
+        a.v2[:] = _f3(o.v2)
+    mesh_ids = None
+    if mesh is not None:
+        remap = np.array([mid(m) for m in mesh.materials], np.int32)
+        mesh_ids = remap[np.asarray(mesh.material_ids, np.int64)]
+    return mats, arr, len(objects), mesh_ids
+
+
+class SceneRenderer:
+    """GPU path tracer for one scene (drop-in for the reference's SceneRenderer)."""
+
+    def __init__(self, sceneObjects: Iterable[SceneObject], device: int = 0, mesh: TriangleMesh | None = None):
+        lib = _lib.load()
+        self._lib = lib
+        ctx = C.c_void_p()
+        code = lib.ar_create(C.byref(ctx), device)
+        if code != _lib.AR_OK:
+            raise _lib.ArError(code, f"ar_create(device={device}) failed (no usable CUDA device?)")
+        self._ctx = ctx
+        self.objects = list(sceneObjects)
+        self.mesh = mesh
+        self.bDirty = True
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            self._lib.ar_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def MarkAsDirty(self) -> None:
+        self.bDirty = True
+
+    def _build(self) -> None:
+        if not self.bDirty:
+            return
+        mats, arr, n, mesh_ids = flatten(self.objects, self.mesh)
+        carr = (ArMaterial * max(1, len(mats)))(*[m.to_c() for m in mats])
+        check(self._ctx, self._lib.ar_scene_set_materials(self._ctx, carr, len(mats)))
+        check(self._ctx, self._lib.ar_scene_set_objects(self._ctx, arr, n))
+        if self.mesh is not None:
+            v = np.ascontiguousarray(self.mesh.vertices, np.float32)
+            idx = np.ascontiguousarray(self.mesh.indices, np.uint32)
+            ids = np.ascontiguousarray(mesh_ids, np.int32)
+            check(self._ctx, self._lib.ar_scene_set_mesh(self._ctx, v.ctypes.data, len(v), idx.ctypes.data, len(idx),
+                                                         ids.ctypes.data))
+        else:
+            check(self._ctx, self._lib.ar_scene_set_mesh(self._ctx, None, 0, None, 0, None))
+        check(self._ctx, self._lib.ar_scene_build(self._ctx))
+        self.bDirty = False
+
+    def build(self) -> None:
+        self._build()
+
+    def stats(self) -> dict:
+        self._build()
+        n, s, d, b = C.c_int64(), C.c_int64(), C.c_int32(), C.c_int64()
+        check(self._ctx, self._lib.ar_scene_stats(self._ctx, C.byref(n), C.byref(s), C.byref(d), C.byref(b)))
+        return {"nodes": n.value, "slots": s.value, "depth": d.value, "bytes": b.value}
+
+    def params(self, size, cameraOrigin, cameraDirection, sampleNum, fov=60.0, max_depth=1000, use_nee=True,
+               seed=GLOBAL_SEED, first_frame=0, wave_paths=0, profile=False) -> ArRenderParams:
+        p = ArRenderParams()
+        p.width, p.height = int(size[0]), int(size[1])
+        p.spp = int(sampleNum)
+        p.max_depth = int(max_depth)
+        p.cam_origin[:] = _f3(cameraOrigin)
+        p.cam_dir[:] = _f3(cameraDirection)
+        p.fov_deg = float(fov)
+        p.use_nee = 1 if use_nee else 0
+        p.seed = int(seed)
+        p.first_frame = int(first_frame)
+        p.wave_paths = int(wave_paths)
+        p.profile = 1 if profile else 0
+        return p
+
+    def Render(self, size, cameraOrigin, cameraDirection, sampleNum: int = 1024, *, fov: float = 60.0,
+               max_depth: int = 1000, use_nee: bool = True, seed: int = GLOBAL_SEED, first_frame: int = 0,
+               per_sample: bool = False, wave_paths: int = 0, profile: bool = False):
+        """Mean linear XYZ per pixel, shape (height, width, 3), float64.
+
+        With per_sample=True also returns every sample's XYZ, shape
+        (sampleNum, height, width, 3), float32."""
+        self._build()
+        p = self.params(size, cameraOrigin, cameraDirection, sampleNum, fov, max_depth, use_nee, seed, first_frame,
+                        wave_paths, profile)
+        w, h = p.width, p.height
+        out = np.zeros((h, w, 3), np.float64)
+        ps = np.zeros((p.spp, h, w, 3), np.float32) if per_sample else None
+        code = self._lib.ar_render(self._ctx, C.byref(p), out.ctypes.data, 0,
+                                   ps.ctypes.data if ps is not None else None, None)
+        check(self._ctx, code)
+        return (out, ps) if per_sample else out
+
+    def last_render_stats(self) -> tuple[float, int]:
+        ms, n = C.c_float(), C.c_int64()
+        check(self._ctx, self._lib.ar_last_render_stats(self._ctx, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def render_profile(self) -> dict:
+        prof = _lib.ArRenderProfile()
+        check(self._ctx, self._lib.ar_last_render_profile(self._ctx, C.byref(prof)))
+        return prof.as_dict()
+
+    def error_word(self) -> int:
+        w = C.c_uint32()
+        check(self._ctx, self._lib.ar_get_error_word(self._ctx, C.byref(w)))
+        return w.value
+
+    # ---- raw ray queries (device tensors) --------------------------------
+    def trace_closest(self, rays, stream=None):
+        """rays: CUDA float32 tensor (n, 8) = (o, tmin, d, tmax).  Returns (prim_id int32, t float32)."""
+        import torch
+        self._build()
+        rays = rays.contiguous()
+        n = rays.shape[0]
+        ids = torch.empty(n, dtype=torch.int32, device=rays.device)
+        t = torch.empty(n, dtype=torch.float32, device=rays.device)
+        s = torch.cuda.current_stream(rays.device).cuda_stream if stream is None else stream
+        check(self._ctx, self._lib.ar_trace_closest(self._ctx, rays.data_ptr(), n, ids.data_ptr(), t.data_ptr(), s))
+        return ids, t
+
+    def trace_any(self, rays, stream=None):
+        import torch
+        self._build()
+        rays = rays.contiguous()
+        n = rays.shape[0]
+        hit = torch.empty(n, dtype=torch.int32, device=rays.device)
+        s = torch.cuda.current_stream(rays.device).cuda_stream if stream is None else stream
+        check(self._ctx, self._lib.ar_trace_any(self._ctx, rays.data_ptr(), n, hit.data_ptr(), s))
+        return hit
+
+
+class Camera:
+    """Headless camera (core/camera.hpp:14-99): renders to a file, no window."""
+
+    def __init__(self, renderer: SceneRenderer, name: str, resolutionX: int, resolutionY: int,
+                 position: Vec3, direction: Vec3, fov: float = 60.0):
+        self.renderer = renderer
+        self.name = name
+        self.resolution = (int(resolutionX), int(resolutionY))
+        self.position = _f3(position)
+        self.direction = _f3(direction)
+        self.fov = float(fov)
+
+    def Render(self, sampleNum: int = 1, **kw) -> np.ndarray:
+        return self.renderer.Render(self.resolution, self.position, self.direction, sampleNum, fov=self.fov, **kw)
+
+    def RenderToFile(self, path: str, sampleNum: int = 1024, **kw) -> np.ndarray:
+        """Writes the linear XYZ image as a PFM (Portable Float Map)."""
+        img = self.Render(sampleNum, **kw).astype(np.float32)
+        h, w, _ = img.shape
+        with open(path, "wb") as f:
+            f.write(f"PF\n{w} {h}\n-1.0\n".encode())
+            f.write(np.ascontiguousarray(img[::-1]).tobytes())
+        return img
+
+
+def host_rgb_encode(rgb: np.ndarray) -> np.ndarray:
+    lib = _lib.load()
+    rgb = np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+    out = np.zeros((len(rgb), 4), np.float32)
+    check(None, lib.ar_host_rgb_encode(rgb.ctypes.data, len(rgb), out.ctypes.data))
+    return out
+
+
+def host_lambda_encode(lam: np.ndarray) -> np.ndarray:
+    lib = _lib.load()
+    lam = np.ascontiguousarray(lam, np.float32).reshape(-1)
+    out = np.zeros((len(lam), 4), np.float32)
+    check(None, lib.ar_host_lambda_encode(lam.ctypes.data, len(lam), out.ctypes.data))
+    return out
+
+
+def host_sample_lambda(u3: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    lib = _lib.load()
+    u3 = np.ascontiguousarray(u3, np.float32).reshape(-1, 3)
+    lam = np.zeros(len(u3), np.float32)
+    pdf = np.zeros(len(u3), np.float32)
+    check(None, lib.ar_host_sample_lambda(u3.ctypes.data, len(u3), lam.ctypes.data, pdf.ctypes.data))
+    return lam, pdf

@@ -1,0 +1,274 @@
+"""Benchmark: Msamples/s of the spectral path tracer on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload cornell|terrain] [--impl ours|reference]
+
+A step renders the whole workload once (width x height x spp paths, each a full
+path up to max depth) with a fresh block of sample indices, so no work repeats.
+`value` is samples / device time (CUDA events on the renderer's stream, scene
+resident in HBM); `e2e` is the same metric through SceneRenderer.Render, the
+reference-facing call, with host output buffers and the result copied back
+inside the timed region.  Path state is ~170 B/path x 2M paths in flight, far
+above the 129 MB L2, so no L2 flush is needed between steps.
+
+--impl reference runs the reference's own integrator compiled for the CPU
+(oracle/_ref, built by __graft_entry__.build()) on every host core, on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    # 256x256, 16 spp, depth 8 Cornell box of triangles
+    "cornell": dict(size=(256, 256), spp=16, depth=8),
+    # 1920x1080, 64 spp, depth 16 terrain (8.4M triangles), 64 sphere lights + sun
+    "terrain": dict(size=(1920, 1080), spp=64, depth=16),
+}
+
+
+def build_workload(name: str):
+    from aperturerendererv3_gb300 import configs
+    if name == "cornell":
+        return configs.cornell_triangles(), None, configs.CORNELL_CAMERA
+    if name == "terrain":
+        objs, mesh = configs.terrain_scene()
+        return objs, mesh, configs.TERRAIN_CAMERA
+    raise KeyError(name)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic(workload: str):
+    """DRAM bytes per extend launch from the committed ncu summary (or None)."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get(workload)
+    return None
+
+
+def cpu_reference_run(workload: str, objs, mesh, cam, w: dict, sample_spp: int, sample_size, threads: int):
+    from oracle import ref_runner as rr
+    rr.ensure_built()
+    t0 = time.perf_counter()
+    _, _, st = rr.render(objs, sample_size, cam["origin"], cam["direction"], sample_spp, fov=cam["fov"],
+                         max_depth=w["depth"], mesh=mesh, threads=threads)
+    wall = time.perf_counter() - t0
+    return st, wall
+
+
+def run_reference(args, w) -> dict:
+    objs, mesh, cam = build_workload(args.workload)
+    threads = os.cpu_count() or 1
+    size = w["size"]
+    # bounded sample per step: a fraction of the frame at 1 spp
+    if args.workload == "cornell":
+        sample_size, sample_spp = size, 2
+    else:
+        sample_size, sample_spp = (96, 54), 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        st, wall = cpu_reference_run(args.workload, objs, mesh, cam, w, sample_spp, sample_size, threads)
+        if i >= args.warmup:
+            vals.append(st["msamples_per_s"])
+    value = float(np.mean(vals))
+    sample = f"{sample_size[0]}x{sample_size[1]}x{sample_spp} spp of the {args.workload} workload per step"
+    return {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.prod(sample_size) * sample_spp / value / 1e3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "width": size[0], "height": size[1], "spp": w["spp"],
+                       "max_depth": w["depth"], "parallelism": "cpu-openmp"},
+            "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "reference",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="cornell", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            try:
+                print(json.dumps(run_reference(args, w)))
+            except Exception as e:
+                print(json.dumps({"impl": "reference", "unavailable": f"reference CPU oracle failed: {e}"}))
+        return
+
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from aperturerendererv3_gb300 import SceneRenderer
+
+    objs, mesh, cam = build_workload(args.workload)
+    r = SceneRenderer(objs, device=local, mesh=mesh)
+    r.build()
+    size, spp, depth = w["size"], w["spp"], w["depth"]
+    samples = size[0] * size[1] * spp
+
+    def step(k: int):
+        return r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
+                        first_frame=(k * world + rank) * spp)
+
+    for k in range(args.warmup):
+        step(k)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    dev_ms, launches = 0.0, 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step(args.warmup + k)
+        ms, L = r.last_render_stats()
+        dev_ms += ms
+        launches += L
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    t = torch.tensor([dev_ms, wall], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev_ms, wall = float(t[0]), float(t[1])
+    total = samples * args.steps * world
+    value = total / (dev_ms / 1e3) / 1e6
+    e2e = total / wall / 1e6
+
+    # profiled render (outside the timed region): stage times + traversal counters
+    r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
+             first_frame=(args.warmup + args.steps) * world * spp, profile=True)
+    prof = r.render_profile()
+    node_b, slot_b, ray_io_b = 80, 48, 16 + 16 + 4 + 4 + 16 + 4 + 4  # node, primitive slot, per-ray state in/out
+    alg_bytes = prof["extend_node_visits"] * node_b + prof["extend_prim_tests"] * slot_b + prof["extend_rays"] * ray_io_b
+    launches_ext = max(1, prof["extend_launches"])
+    achieved = alg_bytes / (prof["extend_ms"] / 1e3) / 1e9
+    peaks = measured_peaks()
+    traffic = profile_traffic(args.workload)
+    out = {
+        "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": args.workload, "width": size[0], "height": size[1], "spp": spp, "max_depth": depth,
+                   "paths_per_step": samples, "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "l2": "inputs larger than L2 (path state ~170 B x 2M paths in flight)"},
+        "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 100,
+                "d2h_bytes_per_step": size[0] * size[1] * 3 * 8},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "roofline": {"kernel": "k_extend (closest-hit wide-BVH traversal)", "bound": "hbm",
+                     "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                     "traffic": traffic,
+                     "alg_bytes_per_launch": alg_bytes / launches_ext,
+                     "alg_bytes_def": "80 B x node visits + 48 B x primitive slots tested + 64 B ray state per ray"},
+        "stages_ms": {k: prof[k] for k in ("raygen_ms", "extend_ms", "shade_ms", "shadow_ms", "finalize_ms")},
+        "traversal": {k: prof[k] for k in ("extend_rays", "extend_node_visits", "extend_prim_tests", "shadow_rays",
+                                           "shadow_node_visits", "shadow_prim_tests")},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            threads = os.cpu_count() or 1
+            sample_size, sample_spp = ((size[0], size[1]), 2) if args.workload == "cornell" else ((96, 54), 1)
+            st, _ = cpu_reference_run(args.workload, objs, mesh, cam, w, sample_spp, sample_size, threads)
+            out["cpu_baseline"] = {"value": st["msamples_per_s"], "unit": "Msamples/s", "cores": st["threads"],
+                                   "kind": "reference",
+                                   "sample": f"{sample_size[0]}x{sample_size[1]}x{sample_spp} spp, same scene"}
+        except Exception as e:
+            out["cpu_baseline"] = {"value": None, "unit": "Msamples/s", "cores": 0, "kind": "reference",
+                                   "sample": f"unavailable: {e}"}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

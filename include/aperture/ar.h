@@ -1,0 +1,153 @@
+/*
+ * aperture-gb300 C ABI: GB300 (sm_103a) path tracing behind plain pointers.
+ *
+ * This is the drop-in boundary for the reference's host entry points:
+ *   SceneRenderer(const std::vector<SceneObject>&)        core/scene.hpp:94, core/scene.cu:734-743
+ *   std::vector<float3> SceneRenderer::Render(size, origin, dir, sampleNum)
+ *                                                          core/scene.hpp:107, core/scene.cu:210-238
+ *   SceneObject / Material::Create* / SceneSetting          core/render/object.cuh:10-27, 119-206, 227-316
+ *   BuildBVH + TraverseBVH (closest / any hit)             core/bvh/bvh.cuh:142-422, core/render/intersection.cuh:148-310
+ * A header-only C++ layer with the reference's class names sits on top of it
+ * (include/aperture/scene_renderer.hpp).
+ *
+ * Conventions: every call returns an ar_status (0 = ok, negative = error; the
+ * message is available from ar_last_error).  No call aborts or traps.  Device
+ * kernels report recoverable faults (traversal stack or queue overflow) in a
+ * sticky error word read with ar_get_error_word.  All state lives in the
+ * context; several contexts may coexist in one process.  `stream` arguments
+ * are cudaStream_t values (NULL = the context's own stream).
+ */
+#ifndef APERTURE_AR_H
+#define APERTURE_AR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ar_status;
+#define AR_OK 0
+#define AR_ERR_INVALID -1   /* bad argument */
+#define AR_ERR_CUDA -2      /* CUDA runtime error (no device, launch failure, ...) */
+#define AR_ERR_NOMEM -3     /* device or host allocation failed */
+#define AR_ERR_STATE -4     /* call out of order (e.g. render before build) */
+#define AR_ERR_DEVICE -5    /* a kernel raised its error word */
+
+/* object kinds (EObjectType, core/render/object.cuh:29-34, plus triangles) */
+#define AR_OBJECT_CUBE 0
+#define AR_OBJECT_SPHERE 1
+#define AR_OBJECT_TRIANGLE 3
+
+/* shading models (EShadingModel, core/render/object.cuh:44-51) */
+#define AR_SHADING_DIFFUSE 0
+#define AR_SHADING_LIGHT 1
+#define AR_SHADING_GLASS 2
+#define AR_SHADING_GGX 3
+
+/* device error word bits */
+#define AR_DEVERR_TRAVERSAL_STACK 1u
+#define AR_DEVERR_QUEUE 2u
+
+typedef struct ar_ctx ar_ctx;
+
+/* Material fields of GBuffer (core/render/object.cuh:59-71).  Values are
+ * clamped exactly as the Material::Create* factories do. */
+typedef struct ar_material
+{
+    int32_t shading;
+    float albedo[3];
+    float emissive[3];
+    float roughness, metallic, specular;
+    float ior, sigma_a, abbe, tilt;
+} ar_material;
+
+/* One SceneObject: an oriented box (centre, half extent, Euler rotation in
+ * degrees), a sphere (radius = max extent) or a triangle (v0, v1, v2). */
+typedef struct ar_object
+{
+    int32_t type;
+    int32_t material;        /* index into the material table */
+    float center[3];
+    float extent[3];
+    float rotation_deg[3];
+    float v0[3], v1[3], v2[3];
+} ar_object;
+
+/* Parameters of one render call (SceneRenderer::Render). */
+typedef struct ar_render_params
+{
+    int32_t width, height;
+    int32_t spp;             /* samples per pixel = frames */
+    int32_t max_depth;       /* path vertices; the reference's MAX_TRACING_DEPTH */
+    float cam_origin[3];
+    float cam_dir[3];
+    float fov_deg;           /* vertical field of view (the reference fixes 60) */
+    int32_t use_nee;         /* next-event estimation with MIS (SceneSetting::bUseNEE_) */
+    uint64_t seed;           /* global seed (GLOBAL_SEED = 0x9e3779b97f4a7c15) */
+    int32_t first_frame;     /* frame index of the first sample */
+    int32_t wave_paths;      /* paths in flight per wave, 0 = automatic */
+    int32_t profile;         /* 1 = record per-stage device times and traversal counters */
+} ar_render_params;
+
+/* Per-stage profile of the last ar_render with params->profile = 1. */
+typedef struct ar_render_profile
+{
+    float raygen_ms, extend_ms, shade_ms, shadow_ms, finalize_ms;
+    int64_t extend_rays, shadow_rays;
+    int64_t extend_node_visits, extend_prim_tests;
+    int64_t shadow_node_visits, shadow_prim_tests;
+    int64_t extend_launches, shadow_launches, shade_launches;
+} ar_render_profile;
+
+ar_status ar_create(ar_ctx** out, int device);
+ar_status ar_destroy(ar_ctx* ctx);
+
+/* Scene description.  Replaces the previous description; takes effect at
+ * ar_scene_build.  Primitive ids: objects first (0..n_objects-1), then mesh
+ * triangles (n_objects + i). */
+ar_status ar_scene_set_materials(ar_ctx* ctx, const ar_material* materials, int n);
+ar_status ar_scene_set_objects(ar_ctx* ctx, const ar_object* objects, int n);
+ar_status ar_scene_set_mesh(ar_ctx* ctx, const float* vertices, int n_vertices, const uint32_t* indices, int n_triangles,
+                            const int32_t* material_ids);
+/* Builds the BVH, the light table and the spectral LUTs; uploads the scene. */
+ar_status ar_scene_build(ar_ctx* ctx);
+/* BVH statistics: nodes, primitive slots, depth, bytes on the device. */
+ar_status ar_scene_stats(ar_ctx* ctx, int64_t* n_nodes, int64_t* n_slots, int32_t* depth, int64_t* device_bytes);
+
+/* Renders params->spp samples per pixel and writes the per-pixel mean linear
+ * CIE XYZ (3 doubles per pixel, row-major, FP64 accumulation in sample order).
+ * out_xyz is host memory when out_is_device == 0, device memory otherwise.
+ * per_sample_xyz (optional, host, 3 floats per pixel per sample in sample-major
+ * order) receives every sample's XYZ. */
+ar_status ar_render(ar_ctx* ctx, const ar_render_params* params, double* out_xyz, int out_is_device,
+                    float* per_sample_xyz, void* stream);
+
+/* Closest / any hit for n rays.  rays: device pointer, 8 floats per ray
+ * (ox, oy, oz, tmin, dx, dy, dz, tmax), direction normalised by the caller.
+ * prim_id: device int32[n] (-1 = miss).  t: device float[n] (closest only,
+ * may be NULL). */
+ar_status ar_trace_closest(ar_ctx* ctx, const float* rays, int n, int32_t* prim_id, float* t, void* stream);
+ar_status ar_trace_any(ar_ctx* ctx, const float* rays, int n, int32_t* hit, void* stream);
+
+/* Device time (ms) of the last ar_render and the number of kernels it launched. */
+ar_status ar_last_render_stats(ar_ctx* ctx, float* device_ms, int64_t* kernel_launches);
+/* Stage times and traversal counters of the last profiled ar_render. */
+ar_status ar_last_render_profile(ar_ctx* ctx, ar_render_profile* out);
+
+ar_status ar_get_error_word(ar_ctx* ctx, uint32_t* word);
+ar_status ar_clear_error_word(ar_ctx* ctx);
+const char* ar_last_error(ar_ctx* ctx);
+
+/* Host-side helpers (no GPU needed): the spectral encoders and the BVH builder
+ * as the kernels use them, for checks against the reference. */
+ar_status ar_host_rgb_encode(const float* rgb, int n, float* basis_out);
+ar_status ar_host_lambda_encode(const float* lambda_nm, int n, float* basis_out);
+ar_status ar_host_sample_lambda(const float* u3, int n, float* lambda_out, float* pdf_out);
+int ar_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* APERTURE_AR_H */

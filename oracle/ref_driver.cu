@@ -1,0 +1,450 @@
+// Host driver that runs the reference's own integrator and BVH on the CPU.
+//
+// TEST INFRASTRUCTURE ONLY (see oracle/prepare_ref.py).  Compiled against the
+// patched reference tree in oracle/_ref/src/core; every computation below is a
+// call into reference code:
+//   kat     spectrum::query::RGBEncode / LambdaEncode / SpectralInteract on the
+//           reference's golden vectors (core/spectrum/spectrum_basis.cuh:2472-2513)
+//   lut     the lambda LUT as PrecomputeLambdaLUTKernel builds it, and RGB LUT
+//           lattice values as PrecomputeRGBLUTKernel builds them
+//           (core/spectrum/spectrum_lut.cuh:12-60)
+//   trace   BuildBVH + intersection::TraverseBVH<false> over triangles
+//           (core/bvh/bvh.cuh:142-422, core/render/intersection.cuh:148-283),
+//           or brute force
+//   render  CalculateRadiance<true, NEE, false> per pixel sample
+//           (core/render/render.cuh:460-999) behind the camera model of
+//           RenderCamera (core/scene.cu:135-189), OpenMP over pixels.
+// The scene / light-table setup mirrors SceneRenderer::UpdateSceneToDeviceIfDirty
+// (core/scene.cu:656-732) on host memory.
+#include <cfloat>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cstdint>
+#include <vector>
+#include <string>
+#include <set>
+#include <chrono>
+#include <omp.h>
+
+#include "scene.hpp"
+#include "render/render.cuh"
+#include "spectrum/spectrum_lut.cuh"
+// explicit SDF instantiations the intersection dispatch links against
+#include "object/sdf/sdf_base.cu"
+
+#ifndef __CUDA_ARCH__
+
+static void die(const char* msg)
+{
+    fprintf(stderr, "ref_cpu: %s\n", msg);
+    exit(2);
+}
+
+static std::vector<char> read_file(const char* path)
+{
+    FILE* f = fopen(path, "rb");
+    if (!f) die("cannot open input");
+    fseek(f, 0, SEEK_END);
+    const long n = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    std::vector<char> buf(n);
+    if (n && fread(buf.data(), 1, n, f) != (size_t)n) die("short read");
+    fclose(f);
+    return buf;
+}
+
+static void write_file(const char* path, const void* data, size_t n, bool append = false)
+{
+    FILE* f = fopen(path, append ? "ab" : "wb");
+    if (!f) die("cannot open output");
+    if (n && fwrite(data, 1, n, f) != n) die("short write");
+    fclose(f);
+}
+
+// ---------------------------------------------------------------- kat
+static int cmd_kat()
+{
+    using namespace spectrum::query;
+    printf("{\"input\": [");
+    for (int i = 0; i < 100; ++i)
+    {
+        printf("%s[%.9g, %.9g, %.9g, %.9g]", i ? ", " : "", inputTest[0][i], inputTest[1][i], inputTest[2][i], inputTest[3][i]);
+    }
+    printf("], \"gt\": [");
+    for (int i = 0; i < 100; ++i) printf("%s%.9g", i ? ", " : "", gtTest[i]);
+    printf("], \"ref_pred\": [");
+    for (int i = 0; i < 100; ++i)
+    {
+        const float rgb3[3] = {inputTest[0][i], inputTest[1][i], inputTest[2][i]};
+        const float lam1[1] = {inputTest[3][i]};
+        float k1[KERNEL], k2[KERNEL];
+        RGBEncode(rgb3, k1);
+        LambdaEncode(lam1, k2);
+        printf("%s%.9g", i ? ", " : "", SpectralInteract(k1, k2));
+    }
+    printf("]}\n");
+    return 0;
+}
+
+// ---------------------------------------------------------------- lut
+// out: lambda LUT (840 x 4 f32), then RGBEncode at each requested lattice point
+static int cmd_lut(const char* lattice_path, const char* out_path)
+{
+    using namespace spectrum::query;
+    constexpr int LRES = SPECTRUM_LAMBDA_LUT_RES;
+    std::vector<float> lam((size_t)LRES * KERNEL);
+    const float step = (780.0f - 360.0f) / static_cast<float>(LRES);
+    for (int i = 0; i < LRES; ++i)
+    {
+        const float lambda = 360.0f + (i + 0.5f) * step;
+        const float in1[1] = {lambda};
+        LambdaEncode(in1, &lam[(size_t)i * KERNEL]);
+    }
+    write_file(out_path, lam.data(), lam.size() * 4);
+    std::vector<char> lat = read_file(lattice_path);
+    const int n = (int)(lat.size() / 12);
+    const int32_t* idx = reinterpret_cast<const int32_t*>(lat.data());
+    std::vector<float> vals((size_t)n * KERNEL);
+    constexpr int RES = SPECTRUM_RGB_LUT_RES;
+    constexpr float invRes = 1.0f / static_cast<float>(RES);
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i)
+    {
+        float in3[3] = {(idx[3 * i] + 0.5f) * invRes, (idx[3 * i + 1] + 0.5f) * invRes, (idx[3 * i + 2] + 0.5f) * invRes};
+        RGBEncode(in3, &vals[(size_t)i * KERNEL]);
+    }
+    write_file(out_path, vals.data(), vals.size() * 4, true);
+    return 0;
+}
+
+// ---------------------------------------------------------------- trace
+// Triangle intersector for TraverseBVH: same watertight test as the GPU, ties at
+// equal t resolved to the smallest primitive id.
+struct TriIntersector
+{
+    const float* tris;  // 9 floats per triangle
+    int sceneCount_;
+    __host__ __device__ bool operator()(const int, const int id, const float3 o, const float3 d,
+                                        const float tMin, const float tMax, IntersectionContext* out) const
+    {
+#ifndef __CUDA_ARCH__
+        ++ref_glue::g_prim_tests;
+#endif
+        const float* v = tris + (size_t)id * 9;
+        const ar::RayShear s = ar::make_shear(ref_glue::to_v(d));
+        float t, b0, b1, b2;
+        if (!ar::tri_intersect(s, ref_glue::to_v(o), ar::v3(v[0], v[1], v[2]), ar::v3(v[3], v[4], v[5]), ar::v3(v[6], v[7], v[8]), &t, &b0, &b1, &b2))
+            return false;
+        if (t < tMin) return false;
+        if (t > tMax) return false;
+        if (t == tMax && !(out && out->bHit_ && id < out->objectIndex_)) return false;
+        if (out)
+        {
+            out->bHit_ = true;
+            out->distance_ = t;
+            out->objectIndex_ = id;
+        }
+        return true;
+    }
+};
+
+static int cmd_trace(const char* tri_path, const char* ray_path, const char* out_path, bool brute)
+{
+    std::vector<char> tb = read_file(tri_path);
+    std::vector<char> rb = read_file(ray_path);
+    const int ntri = *reinterpret_cast<const int32_t*>(tb.data());
+    const float* tris = reinterpret_cast<const float*>(tb.data() + 4);
+    const int nray = *reinterpret_cast<const int32_t*>(rb.data());
+    const float* rays = reinterpret_cast<const float*>(rb.data() + 4);
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<PrimitiveProxy> proxy(ntri);
+    for (int i = 0; i < ntri; ++i)
+    {
+        const float* v = tris + (size_t)i * 9;
+        PrimitiveProxy p;
+        p.boundMin_ = float3{fminf(v[0], fminf(v[3], v[6])), fminf(v[1], fminf(v[4], v[7])), fminf(v[2], fminf(v[5], v[8]))};
+        p.boundMax_ = float3{fmaxf(v[0], fmaxf(v[3], v[6])), fmaxf(v[1], fmaxf(v[4], v[7])), fmaxf(v[2], fmaxf(v[5], v[8]))};
+        p.center_ = float3{(p.boundMin_.x + p.boundMax_.x) * 0.5f, (p.boundMin_.y + p.boundMax_.y) * 0.5f, (p.boundMin_.z + p.boundMax_.z) * 0.5f};
+        proxy[i] = p;
+    }
+    BVHHost bvh;
+    if (!brute) bvh = BuildBVH(proxy);
+    auto t1 = std::chrono::steady_clock::now();
+    std::vector<int32_t> ids(nray);
+    std::vector<float> ts(nray);
+    unsigned long long visits = 0, tests = 0;
+    const TriIntersector isect{tris, ntri};
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : visits, tests)
+    for (int r = 0; r < nray; ++r)
+    {
+        ref_glue::g_node_visits = 0;
+        ref_glue::g_prim_tests = 0;
+        const float* q = rays + (size_t)r * 8;
+        const float3 o{q[0], q[1], q[2]}, d{q[3], q[4], q[5]};
+        IntersectionContext res{};
+        if (brute)
+        {
+            res.distance_ = q[7];
+            for (int i = 0; i < ntri; ++i) isect(0, i, o, d, q[6], res.distance_, &res);
+        }
+        else
+        {
+            res = intersection::TraverseBVH<false>(0, o, d, isect, bvh.nodes_.data(), (int)bvh.nodes_.size(),
+                                                  bvh.objectIndices_.data(), q[6], q[7]);
+        }
+        ids[r] = res.bHit_ ? res.objectIndex_ : -1;
+        ts[r] = res.bHit_ ? res.distance_ : -1.0f;
+        visits += ref_glue::g_node_visits;
+        tests += ref_glue::g_prim_tests;
+    }
+    auto t2 = std::chrono::steady_clock::now();
+    write_file(out_path, ids.data(), ids.size() * 4);
+    write_file(out_path, ts.data(), ts.size() * 4, true);
+    printf("{\"build_s\": %.4f, \"trace_s\": %.4f, \"nodes\": %zu, \"node_visits\": %llu, \"prim_tests\": %llu, \"threads\": %d}\n",
+           std::chrono::duration<double>(t1 - t0).count(), std::chrono::duration<double>(t2 - t1).count(),
+           bvh.nodes_.size(), visits, tests, omp_get_max_threads());
+    return 0;
+}
+
+// ---------------------------------------------------------------- render
+#pragma pack(push, 1)
+struct FileObject
+{
+    int32_t type, shading;
+    float center[3], extent[3], rotation[3];
+    float v0[3], v1[3], v2[3];
+    float albedo[3], emissive[3];
+    float roughness, metallic, specular, ior, sigma_a, abbe, tilt;
+};
+struct RenderParams
+{
+    int32_t width, height, spp, max_depth;
+    float cam_origin[3], cam_dir[3];
+    float fov_deg;
+    int32_t use_nee;
+    uint64_t seed;
+    int32_t first_frame, per_sample_frames;
+};
+#pragma pack(pop)
+
+static float3 f3(const float* v) { return float3{v[0], v[1], v[2]}; }
+
+static Material make_material(const FileObject& o)
+{
+    switch (o.shading)
+    {
+        case 1: return Material::CreateLight(f3(o.emissive));
+        case 2: return Material::CreateGlassPureColor(f3(o.albedo), o.ior, o.sigma_a, o.abbe, o.tilt);
+        case 3: return Material::CreateGGXPureColor(f3(o.albedo), o.roughness, o.metallic, o.specular, f3(o.emissive));
+        default: return Material::CreateDiffusePureColor(f3(o.albedo), f3(o.emissive));
+    }
+}
+
+// RGB LUT lattice points a render can touch: material colours and the sky
+// gradient (SkyLighting depends on the ray's y only).  Only these are filled.
+static void collect_cells(float3 rgb, std::set<uint64_t>& pts)
+{
+    const float lum = max3(rgb);
+    if (lum > 1.0f) rgb = rgb / lum;
+    constexpr int RES = SPECTRUM_RGB_LUT_RES;
+    const float c[3] = {rgb.x, rgb.y, rgb.z};
+    int lo[3], hi[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        float g = c[k] * static_cast<float>(RES) - 0.5f;
+        g = fminf(fmaxf(g, 0.0f), static_cast<float>(RES) - 1.0f);
+        lo[k] = (int)floorf(g);
+        hi[k] = lo[k] + 1 >= RES ? RES - 1 : lo[k] + 1;
+    }
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            for (int e = 0; e < 2; ++e)
+            {
+                const uint64_t x = a ? hi[0] : lo[0], y = b ? hi[1] : lo[1], z = e ? hi[2] : lo[2];
+                pts.insert((z * RES + y) * RES + x);
+            }
+}
+
+static int cmd_render(const char* scene_path, const char* params_path, const char* out_path)
+{
+    std::vector<char> sb = read_file(scene_path);
+    std::vector<char> pb = read_file(params_path);
+    if (sb.size() < 8 || memcmp(sb.data(), "ARS1", 4) != 0) die("bad scene file");
+    const int nobj = *reinterpret_cast<const int32_t*>(sb.data() + 4);
+    const FileObject* fo = reinterpret_cast<const FileObject*>(sb.data() + 8);
+    RenderParams prm;
+    memcpy(&prm, pb.data(), sizeof(prm));
+
+    // scene objects through the reference's own constructors
+    std::vector<SceneObject> objs;
+    objs.reserve(nobj);
+    for (int i = 0; i < nobj; ++i)
+    {
+        const FileObject& o = fo[i];
+        if (o.type == 3)
+        {
+            SceneObject so;
+            so.type_ = EObjectType::OBJ_TRIANGLE;
+            so.material_ = make_material(o);
+            so.triV0_ = f3(o.v0);
+            so.triV1_ = f3(o.v1);
+            so.triV2_ = f3(o.v2);
+            so.proxy_.boundMin_ = float3{fminf(o.v0[0], fminf(o.v1[0], o.v2[0])), fminf(o.v0[1], fminf(o.v1[1], o.v2[1])), fminf(o.v0[2], fminf(o.v1[2], o.v2[2]))};
+            so.proxy_.boundMax_ = float3{fmaxf(o.v0[0], fmaxf(o.v1[0], o.v2[0])), fmaxf(o.v0[1], fmaxf(o.v1[1], o.v2[1])), fmaxf(o.v0[2], fmaxf(o.v1[2], o.v2[2]))};
+            so.proxy_.center_ = (so.proxy_.boundMin_ + so.proxy_.boundMax_) * 0.5f;
+            objs.push_back(so);
+        }
+        else
+        {
+            objs.emplace_back(f3(o.center), f3(o.extent), make_material(o), f3(o.rotation),
+                              o.type == 1 ? EObjectType::OBJ_SPHERE : EObjectType::OBJ_CUBE);
+        }
+    }
+    // BVH + light table (core/scene.cu:666-706)
+    std::vector<PrimitiveProxy> proxys;
+    for (auto& so : objs) proxys.push_back(so.proxy_);
+    BVHHost bvh = BuildBVH(proxys);
+    std::vector<AdditionalLightInfo> lights;
+    float total = 0.0f;
+    for (int i = 0; i < (int)objs.size(); ++i)
+    {
+        objs[i].objectIndex_ = i;
+        if (objs[i].material_.shadingModel_ == EShadingModel::MAT_LIGHT)
+        {
+            objs[i].lightIndex_ = (int)lights.size();
+            AdditionalLightInfo li;
+            li.objectIndex_ = i;
+            li.importanceWeight_ = fmaxf(objs[i].GetArea() * objs[i].GetEmissivePower(), 1.0e-20f);
+            total += li.importanceWeight_;
+            lights.push_back(li);
+        }
+        else
+        {
+            objs[i].lightIndex_ = -1;
+        }
+    }
+    for (auto& li : lights) li.selectProb_ = li.importanceWeight_ / total;
+
+    // spectral LUTs: full lambda LUT, RGB lattice points the scene can touch
+    using namespace spectrum::query;
+    constexpr int RES = SPECTRUM_RGB_LUT_RES;
+    constexpr int LRES = SPECTRUM_LAMBDA_LUT_RES;
+    std::vector<float> lam((size_t)LRES * KERNEL);
+    {
+        const float step = (780.0f - 360.0f) / static_cast<float>(LRES);
+        for (int i = 0; i < LRES; ++i)
+        {
+            const float in1[1] = {360.0f + (i + 0.5f) * step};
+            LambdaEncode(in1, &lam[(size_t)i * KERNEL]);
+        }
+    }
+    float* lut = static_cast<float*>(calloc((size_t)RES * RES * RES * KERNEL, sizeof(float)));
+    if (!lut) die("LUT allocation failed");
+    {
+        std::set<uint64_t> pts;
+        for (auto& so : objs)
+        {
+            collect_cells(so.material_.texture_.baseTexture_.albedo_, pts);
+            collect_cells(so.material_.texture_.baseTexture_.emissive_, pts);
+        }
+        const int NS = 1 << 22;
+        for (int i = 0; i <= NS; ++i)
+        {
+            const float y = -1.0f + 2.0f * (float)i / (float)NS;
+            collect_cells(SkyLighting(float3{0.0f, y, 0.0f}), pts);
+        }
+        std::vector<uint64_t> v(pts.begin(), pts.end());
+        constexpr float invRes = 1.0f / static_cast<float>(RES);
+#pragma omp parallel for
+        for (int i = 0; i < (int)v.size(); ++i)
+        {
+            const uint64_t p = v[i];
+            const int x = (int)(p % RES), y = (int)((p / RES) % RES), z = (int)(p / ((uint64_t)RES * RES));
+            float in3[3] = {(x + 0.5f) * invRes, (y + 0.5f) * invRes, (z + 0.5f) * invRes};
+            RGBEncode(in3, &lut[p * KERNEL]);
+        }
+    }
+
+    SCENE_OBJECTS = objs.data();
+    SCENE_OBJECT_COUNTS = (int)objs.size();
+    SCENE_LIGHTS_INFO = lights.data();
+    SCENE_LIGHTS_COUNTS = (int)lights.size();
+    BVH_NODES = bvh.nodes_.data();
+    BVH_NODES_COUNTS = (int)bvh.nodes_.size();
+    BVH_OBJECT_INDICES = bvh.objectIndices_.data();
+    SPECTRUM_LUT_RGB = lut;
+    SPECTRUM_LUT_LAMBDA = lam.data();
+    REF_MAX_TRACING_DEPTH = prm.max_depth;
+    SCENE_PROBES_COUNTS = 0;
+
+    const int W = prm.width, H = prm.height;
+    const size_t npix = (size_t)W * H;
+    std::vector<double> sums(npix * 3, 0.0);
+    std::vector<float> per_sample((size_t)prm.per_sample_frames * npix * 3, 0.0f);
+    const float3 camO = f3(prm.cam_origin), camD = f3(prm.cam_dir);
+    const float FOV = prm.fov_deg * 3.1415926f / 180.0f;
+    const float aspect = static_cast<float>(W) / fmaxf(1.0f, static_cast<float>(H));
+    const float tanHalfY = arm_tanf(0.5f * FOV);
+    const float tanHalfX = tanHalfY * aspect;
+    const float3 right = normalize(cross(camD, float3{0.0, 1.0, 0.0}));
+    const float3 up = normalize(cross(camD, right));
+
+    auto t0 = std::chrono::steady_clock::now();
+    for (int s = 0; s < prm.spp; ++s)
+    {
+        const int frame = prm.first_frame + s;
+        FRAME_INDEX = frame;
+        TOTAL_FRAME_INDEX = (uint64_t)frame;
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long long p = 0; p < (long long)npix; ++p)
+        {
+            const int i = (int)(p % W), j = (int)(p / W);
+            curandState seed = ar_pcg_init(prm.seed, (uint64_t)p, (uint64_t)frame);
+            const float u = (i + Rand1(&seed)) / static_cast<float>(W);
+            const float v = (j + Rand1(&seed)) / static_cast<float>(H);
+            const float2 ndc = make_float2(u * 2.f - 1.f, (1.0 - v) * 2.f - 1.f);
+            const float sx = ndc.x * tanHalfX;
+            const float sy = ndc.y * tanHalfY;
+            const float3 rayDirection = normalize(camD + right * sx + up * sy);
+            float4 r;
+            if (prm.use_nee) r = CalculateRadiance<true, true, false>(&seed, camO, rayDirection);
+            else r = CalculateRadiance<true, false, false>(&seed, camO, rayDirection);
+            float3 result = make_f3(r);
+            result = max(float3{0}, result);
+            sums[3 * p + 0] += (double)result.x;
+            sums[3 * p + 1] += (double)result.y;
+            sums[3 * p + 2] += (double)result.z;
+            if (s < prm.per_sample_frames)
+            {
+                float* q = &per_sample[((size_t)s * npix + p) * 3];
+                q[0] = result.x;
+                q[1] = result.y;
+                q[2] = result.z;
+            }
+        }
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    write_file(out_path, sums.data(), sums.size() * 8);
+    if (prm.per_sample_frames) write_file(out_path, per_sample.data(), per_sample.size() * 4, true);
+    free(lut);
+    const double secs = std::chrono::duration<double>(t1 - t0).count();
+    printf("{\"render_s\": %.6f, \"samples\": %llu, \"msamples_per_s\": %.6f, \"threads\": %d, \"bvh_nodes\": %zu}\n",
+           secs, (unsigned long long)npix * prm.spp, (double)npix * prm.spp / secs / 1e6, omp_get_max_threads(), bvh.nodes_.size());
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 2) die("usage: ref_cpu kat | lut <lattice> <out> | trace|brute <tris> <rays> <out> | render <scene> <params> <out>");
+    const std::string cmd = argv[1];
+    if (cmd == "kat") return cmd_kat();
+    if (cmd == "lut" && argc == 4) return cmd_lut(argv[2], argv[3]);
+    if ((cmd == "trace" || cmd == "brute") && argc == 5) return cmd_trace(argv[2], argv[3], argv[4], cmd == "brute");
+    if (cmd == "render" && argc == 5) return cmd_render(argv[2], argv[3], argv[4]);
+    die("bad arguments");
+    return 2;
+}
+#else
+int main() { return 0; }
+#endif

@@ -1,0 +1,138 @@
+"""Runs the reference CPU oracle (oracle/_ref/ref_cpu) on our scene descriptions.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline / reference arm, never by the product package.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+EXE = HERE / "_ref" / "ref_cpu"
+
+OBJ_DTYPE = np.dtype([("type", "<i4"), ("shading", "<i4"), ("center", "<f4", 3), ("extent", "<f4", 3),
+                      ("rotation", "<f4", 3), ("v0", "<f4", 3), ("v1", "<f4", 3), ("v2", "<f4", 3),
+                      ("albedo", "<f4", 3), ("emissive", "<f4", 3), ("roughness", "<f4"), ("metallic", "<f4"),
+                      ("specular", "<f4"), ("ior", "<f4"), ("sigma_a", "<f4"), ("abbe", "<f4"), ("tilt", "<f4")])
+PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("max_depth", "<i4"),
+                         ("cam_origin", "<f4", 3), ("cam_dir", "<f4", 3), ("fov", "<f4"), ("use_nee", "<i4"),
+                         ("seed", "<u8"), ("first_frame", "<i4"), ("per_sample", "<i4")])
+
+
+def available() -> bool:
+    return EXE.exists()
+
+
+def ensure_built() -> Path:
+    """Builds the oracle if its patched sources are present (see prepare_ref.py)."""
+    if EXE.exists():
+        return EXE
+    from . import prepare_ref  # noqa: F401  (package-relative when imported as oracle.ref_runner)
+    return prepare_ref.build_ref()
+
+
+def scene_bytes(objects, mesh=None) -> bytes:
+    """Objects (and mesh triangles, appended as triangle objects) in the oracle's file format."""
+    n_mesh = 0 if mesh is None else len(mesh.indices)
+    rec = np.zeros(len(objects) + n_mesh, OBJ_DTYPE)
+    for i, o in enumerate(objects):
+        m = o.material
+        rec[i] = (o.type, m.shading, o.center, o.extent, o.rotation, o.v0, o.v1, o.v2, m.albedo, m.emissive,
+                  m.roughness, m.metallic, m.specular, m.ior, m.sigma_a, m.abbe, m.tilt)
+    if n_mesh:
+        tv = mesh.triangle_vertices().reshape(-1, 3, 3)
+        base = len(objects)
+        r = rec[base:]
+        r["type"] = 3
+        r["v0"], r["v1"], r["v2"] = tv[:, 0], tv[:, 1], tv[:, 2]
+        mids = np.asarray(mesh.material_ids, np.int64)
+        for k, m in enumerate(mesh.materials):
+            sel = mids == k
+            r["shading"][sel] = m.shading
+            r["albedo"][sel] = m.albedo
+            r["emissive"][sel] = m.emissive
+            r["roughness"][sel] = m.roughness
+            r["metallic"][sel] = m.metallic
+            r["specular"][sel] = m.specular
+            r["ior"][sel] = m.ior
+            r["sigma_a"][sel] = m.sigma_a
+            r["abbe"][sel] = m.abbe
+            r["tilt"][sel] = m.tilt
+    return b"ARS1" + np.int32(len(rec)).tobytes() + rec.tobytes()
+
+
+def render(objects, size, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
+           seed=0x9E3779B97F4A7C15, first_frame=0, per_sample_frames=0, mesh=None, threads=None):
+    """Returns (mean XYZ (H, W, 3) float64, per-sample XYZ or None, stats dict)."""
+    exe = ensure_built()
+    w, h = int(size[0]), int(size[1])
+    prm = np.zeros(1, PARAMS_DTYPE)
+    prm[0] = (w, h, spp, max_depth, origin, direction, fov, 1 if use_nee else 0, seed, first_frame, per_sample_frames)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "scene.bin").write_bytes(scene_bytes(objects, mesh))
+        (td / "params.bin").write_bytes(prm.tobytes())
+        env = dict(os.environ)
+        if threads:
+            env["OMP_NUM_THREADS"] = str(threads)
+        env.setdefault("OMP_PROC_BIND", "close")
+        r = subprocess.run([str(exe), "render", str(td / "scene.bin"), str(td / "params.bin"), str(td / "out.bin")],
+                           capture_output=True, text=True, env=env)
+        if r.returncode != 0:
+            raise RuntimeError("reference oracle failed: " + r.stderr)
+        stats = json.loads(r.stdout.strip().splitlines()[-1])
+        raw = (td / "out.bin").read_bytes()
+    npix = w * h
+    sums = np.frombuffer(raw[: npix * 24], np.float64).reshape(h, w, 3)
+    per = None
+    if per_sample_frames:
+        per = np.frombuffer(raw[npix * 24:], np.float32).reshape(per_sample_frames, h, w, 3)
+    return sums / spp, per, stats
+
+
+def trace(tris: np.ndarray, rays: np.ndarray, brute: bool = False, threads=None):
+    """Closest hit through the reference BVH (or brute force): (prim_id int32, t float32, stats)."""
+    exe = ensure_built()
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "tris.bin").write_bytes(np.int32(len(tris)).tobytes() + tris.tobytes())
+        (td / "rays.bin").write_bytes(np.int32(len(rays)).tobytes() + rays.tobytes())
+        env = dict(os.environ)
+        if threads:
+            env["OMP_NUM_THREADS"] = str(threads)
+        r = subprocess.run([str(exe), "brute" if brute else "trace", str(td / "tris.bin"), str(td / "rays.bin"),
+                            str(td / "out.bin")], capture_output=True, text=True, env=env)
+        if r.returncode != 0:
+            raise RuntimeError("reference oracle failed: " + r.stderr)
+        stats = json.loads(r.stdout.strip().splitlines()[-1])
+        raw = (td / "out.bin").read_bytes()
+    n = len(rays)
+    return np.frombuffer(raw[: 4 * n], np.int32).copy(), np.frombuffer(raw[4 * n:], np.float32).copy(), stats
+
+
+def kat() -> dict:
+    exe = ensure_built()
+    r = subprocess.run([str(exe), "kat"], capture_output=True, text=True, check=True)
+    return json.loads(r.stdout)
+
+
+def luts(lattice: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """(lambda LUT (840, 4), RGBEncode at the given (n, 3) int lattice points)."""
+    exe = ensure_built()
+    lattice = np.ascontiguousarray(lattice, np.int32).reshape(-1, 3)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "lat.bin").write_bytes(lattice.tobytes())
+        subprocess.run([str(exe), "lut", str(td / "lat.bin"), str(td / "out.bin")], check=True, capture_output=True)
+        raw = (td / "out.bin").read_bytes()
+    lam = np.frombuffer(raw[: 840 * 16], np.float32).reshape(840, 4)
+    rgb = np.frombuffer(raw[840 * 16:], np.float32).reshape(-1, 4)
+    return lam, rgb

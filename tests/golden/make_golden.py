@@ -1,0 +1,79 @@
+"""Generates the committed golden fixtures from the reference oracle.
+
+Run in a checkout that has the reference tree (oracle/prepare_ref.py builds
+oracle/_ref/ref_cpu from it):
+
+    python tests/golden/make_golden.py
+
+Fixtures:
+  spectral_kat.json      the reference's 100 spectral known-answer vectors
+                         (inputTest / gtTest, core/spectrum/spectrum_basis.cuh:2472-2489)
+                         and the reference encoder's own predictions for them
+  spectral_luts.npz      the lambda LUT (840 x 4) and RGB-LUT lattice values at
+                         seeded lattice points, computed by the reference code
+  trace_small.npz        triangles, rays, and closest-hit ids / t from the
+                         reference BVH traversal (ties: smallest id)
+  render_*.npz           per-sample XYZ of small renders of the reference's own
+                         Cornell box and of the triangle Cornell box (first
+                         bounce and full depth) from the reference integrator
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from aperturerendererv3_gb300 import configs  # noqa: E402
+from oracle import ref_runner as rr  # noqa: E402
+
+RENDERS = {
+    "render_refcornell_depth1": ("reference_cornell", 24, 24, 2, 1),
+    "render_refcornell_full": ("reference_cornell", 24, 24, 2, 1000),
+    "render_cornell_depth1": ("cornell_triangles", 24, 24, 2, 1),
+    "render_cornell_depth8": ("cornell_triangles", 24, 24, 2, 8),
+}
+
+
+def scene_by_name(name):
+    if name == "reference_cornell":
+        return configs.reference_cornell(), configs.REFERENCE_CORNELL_CAMERA
+    if name == "cornell_triangles":
+        return configs.cornell_triangles(), configs.CORNELL_CAMERA
+    raise KeyError(name)
+
+
+def trace_case(seed: int = 3, ntri: int = 6000, nray: int = 4096):
+    tris = configs.random_triangles(ntri, seed=seed)
+    cam = configs.BVH_STRESS_CAMERA
+    rays = configs.pinhole_rays(64, 64, cam["origin"], cam["direction"], cam["fov"])[:nray]
+    return tris, rays
+
+
+def main() -> None:
+    k = rr.kat()
+    (HERE / "spectral_kat.json").write_text(json.dumps(k))
+    rng = np.random.default_rng(11)
+    lattice = rng.integers(0, 512, (256, 3)).astype(np.int32)
+    lattice[:4] = [[0, 0, 0], [511, 511, 511], [0, 511, 0], [255, 256, 257]]
+    lam, rgb = rr.luts(lattice)
+    np.savez(HERE / "spectral_luts.npz", lambda_lut=lam, lattice=lattice, rgb_values=rgb)
+    tris, rays = trace_case()
+    ids, t, _ = rr.trace(tris, rays)
+    bids, bt, _ = rr.trace(tris, rays, brute=True)
+    assert np.array_equal(ids, bids) and np.array_equal(t.view(np.uint32), bt.view(np.uint32))
+    np.savez(HERE / "trace_small.npz", tris=tris, rays=rays, ids=ids, t=t)
+    for name, (scene, w, h, spp, depth) in RENDERS.items():
+        objs, cam = scene_by_name(scene)
+        mean, per, _ = rr.render(objs, (w, h), cam["origin"], cam["direction"], spp, fov=cam["fov"],
+                                 max_depth=depth, per_sample_frames=spp)
+        np.savez(HERE / f"{name}.npz", per_sample=per, mean=mean, scene=scene, size=(w, h), spp=spp, depth=depth)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
