@@ -67,7 +67,7 @@ EXPORTED = [
     "ar_scene_build", "ar_scene_stats", "ar_render", "ar_trace_closest", "ar_trace_any", "ar_last_render_stats",
     "ar_last_render_profile",
     "ar_get_error_word", "ar_clear_error_word", "ar_last_error", "ar_host_rgb_encode", "ar_host_lambda_encode",
-    "ar_host_sample_lambda", "ar_abi_version",
+    "ar_host_sample_lambda", "ar_host_trace_closest", "ar_abi_version",
 ]
 
 _lib = None
@@ -109,6 +109,7 @@ def load() -> C.CDLL:
         "ar_host_rgb_encode": (C.c_int, [vp, C.c_int, vp]),
         "ar_host_lambda_encode": (C.c_int, [vp, C.c_int, vp]),
         "ar_host_sample_lambda": (C.c_int, [vp, C.c_int, vp, vp]),
+        "ar_host_trace_closest": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp, P(C.c_int64)]),
         "ar_abi_version": (C.c_int, []),
     }
     for name, (res, args) in sig.items():

@@ -135,7 +135,7 @@ struct Ctx
     float last_render_ms = 0.0f;
     long long last_launches = 0;
     // profiling
-    bool profile = false;
+    int profile = 0;  // bit0: stage events, bit1: traversal counters
     unsigned long long* d_stats = nullptr;  // 8 counters
     std::vector<StageEvent> stage_events;
     float stage_ms[ST_COUNT] = {0, 0, 0, 0, 0};

@@ -35,24 +35,44 @@ struct TravResult
     int id;    // primitive id, -1 on miss
 };
 
-__device__ __forceinline__ uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, int s)
+// The traversal is compiled for the device and, for the CPU test suite, for
+// the host; these shims are the only difference.
+#if defined(__CUDA_ARCH__)
+#define AR_LDG(p) __ldg(p)
+#define AR_FFS(x) __ffs(x)
+#define AR_POPC(x) __popc(x)
+#define AR_F2U(x) __float_as_uint(x)
+#define AR_U2F(x) __uint_as_float(x)
+#define AR_ATOMIC_OR(p, v) atomicOr((p), (v))
+#define AR_ATOMIC_ADD64(p, v) atomicAdd((p), (v))
+#else
+#define AR_ATOMIC_OR(p, v) (*(p) |= (v))
+#define AR_ATOMIC_ADD64(p, v) (*(p) += (v))
+#define AR_LDG(p) (*(p))
+#define AR_FFS(x) __builtin_ffs((int)(x))
+#define AR_POPC(x) __builtin_popcount(x)
+#define AR_F2U(x) arm_detail::float_to_bits(x)
+#define AR_U2F(x) arm_detail::bits_to_float(x)
+#endif
+
+AR_HD uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, int s)
 {
     const uint32_t w = (s < 4) ? lo_word : hi_word;
     return (w >> (8 * (s & 3))) & 0xffu;
 }
 
 // Intersects one primitive slot; returns t (or -1 on miss) and the id.
-__device__ __forceinline__ float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3 d, int* id_out)
+AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3 d, int* id_out)
 {
-    const float4 a = __ldg(&sc.slots[3 * (size_t)slot + 0]);
-    const uint32_t tag = __float_as_uint(a.w);
+    const float4 a = AR_LDG(&sc.slots[3 * (size_t)slot + 0]);
+    const uint32_t tag = AR_F2U(a.w);
     const uint32_t kind = tag >> AR_PRIM_KIND_SHIFT;
     const int id = (int)(tag & AR_PRIM_ID_MASK);
     *id_out = id;
     if (kind == AR_PRIM_KIND_TRI)
     {
-        const float4 b = __ldg(&sc.slots[3 * (size_t)slot + 1]);
-        const float4 c = __ldg(&sc.slots[3 * (size_t)slot + 2]);
+        const float4 b = AR_LDG(&sc.slots[3 * (size_t)slot + 1]);
+        const float4 c = AR_LDG(&sc.slots[3 * (size_t)slot + 2]);
         float t, b0, b1, b2;
         if (tri_intersect(sh, o, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &t, &b0, &b1, &b2)) return t;
         return -1.0f;
@@ -69,7 +89,7 @@ __device__ __forceinline__ float prim_hit(const TravScene& sc, int slot, const R
 #define AR_DEVERR_QUEUE 2u
 
 template <bool AnyHit>
-__device__ __forceinline__ TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,
+AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,
                                                     unsigned int* err, uint32_t& n_visits, uint32_t& n_tests)
 {
     TravResult res;
@@ -89,15 +109,15 @@ __device__ __forceinline__ TravResult traverse_impl(const TravScene& sc, V3 o, V
         {
             ++n_visits;
             const uint4* np = sc.nodes + 5 * (size_t)node;
-            const uint4 w0 = __ldg(np + 0);
-            const uint4 w1 = __ldg(np + 1);
-            const uint4 w2 = __ldg(np + 2);
-            const uint4 w3 = __ldg(np + 3);
-            const uint4 w4 = __ldg(np + 4);
-            const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
-            const float sx = __uint_as_float((w0.w & 0xffu) << 23);
-            const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
-            const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+            const uint4 w0 = AR_LDG(np + 0);
+            const uint4 w1 = AR_LDG(np + 1);
+            const uint4 w2 = AR_LDG(np + 2);
+            const uint4 w3 = AR_LDG(np + 3);
+            const uint4 w4 = AR_LDG(np + 4);
+            const float px = AR_U2F(w0.x), py = AR_U2F(w0.y), pz = AR_U2F(w0.z);
+            const float sx = AR_U2F((w0.w & 0xffu) << 23);
+            const float sy = AR_U2F(((w0.w >> 8) & 0xffu) << 23);
+            const float sz = AR_U2F(((w0.w >> 16) & 0xffu) << 23);
             const uint32_t imask = w0.w >> 24;
             const uint32_t child_base = w1.x;
             const uint32_t prim_base = w1.y;
@@ -127,7 +147,7 @@ __device__ __forceinline__ TravResult traverse_impl(const TravScene& sc, V3 o, V
             }
             while (hit_leaf)
             {
-                const uint32_t i = __ffs(hit_leaf) - 1;
+                const uint32_t i = AR_FFS(hit_leaf) - 1;
                 hit_leaf &= hit_leaf - 1;
                 const int s = (int)(i ^ oct);
                 const uint32_t meta = byte_of(w1.z, w1.w, s);
@@ -160,14 +180,14 @@ __device__ __forceinline__ TravResult traverse_impl(const TravScene& sc, V3 o, V
             node = -1;
             if (hit_int)
             {
-                const uint32_t i = __ffs(hit_int) - 1;
+                const uint32_t i = AR_FFS(hit_int) - 1;
                 hit_int &= hit_int - 1;
                 const uint32_t s = i ^ oct;
-                node = (int)(child_base + __popc(imask & ((1u << s) - 1u)));
+                node = (int)(child_base + AR_POPC(imask & ((1u << s) - 1u)));
                 if (hit_int)
                 {
                     if (sp < AR_TRAV_STACK) stack[sp++] = make_uint2(child_base, hit_int | (imask << 8));
-                    else if (err) atomicOr(err, AR_DEVERR_STACK);
+                    else if (err) AR_ATOMIC_OR(err, AR_DEVERR_STACK);
                 }
                 continue;
             }
@@ -176,10 +196,10 @@ __device__ __forceinline__ TravResult traverse_impl(const TravScene& sc, V3 o, V
         uint2 e = stack[--sp];
         uint32_t m = e.y & 0xffu;
         const uint32_t im = e.y >> 8;
-        const uint32_t i = __ffs(m) - 1;
+        const uint32_t i = AR_FFS(m) - 1;
         m &= m - 1;
         const uint32_t s = i ^ oct;
-        node = (int)(e.x + __popc(im & ((1u << s) - 1u)));
+        node = (int)(e.x + AR_POPC(im & ((1u << s) - 1u)));
         if (m) stack[sp++] = make_uint2(e.x, m | (im << 8));
     }
     if (res.slot < 0) res.t = tmax;
@@ -188,15 +208,15 @@ __device__ __forceinline__ TravResult traverse_impl(const TravScene& sc, V3 o, V
 
 // stats (optional): [0] += node visits, [1] += primitive tests
 template <bool AnyHit>
-__device__ __forceinline__ TravResult traverse(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,
+AR_HD TravResult traverse(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,
                                                unsigned int* err, unsigned long long* stats = nullptr)
 {
     uint32_t n_visits = 0, n_tests = 0;
     TravResult res = traverse_impl<AnyHit>(sc, o, d, tmin, tmax, err, n_visits, n_tests);
     if (stats)
     {
-        atomicAdd(&stats[0], (unsigned long long)n_visits);
-        atomicAdd(&stats[1], (unsigned long long)n_tests);
+        AR_ATOMIC_ADD64(&stats[0], (unsigned long long)n_visits);
+        AR_ATOMIC_ADD64(&stats[1], (unsigned long long)n_tests);
     }
     return res;
 }

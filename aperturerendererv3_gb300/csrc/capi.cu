@@ -43,7 +43,7 @@ DevScene dev_scene(const Ctx& c)
     s.cie_cmf = c.d_cie;
     s.d65 = c.d_d65;
     s.camera_inside = c.camera_inside;
-    s.stats = c.profile ? c.d_stats : nullptr;
+    s.stats = (c.profile & 2) ? c.d_stats : nullptr;
     return s;
 }
 } // namespace ar
@@ -552,7 +552,7 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     rl.seed = prm->seed;
     rl.first_frame = prm->first_frame;
     rl.profile = prm->profile;
-    c.profile = prm->profile != 0;
+    c.profile = prm->profile & 3;
     c.stage_events.clear();
     for (int k = 0; k < ST_COUNT; ++k)
     {
@@ -619,9 +619,9 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
         cudaEventDestroy(se.b);
     }
     c.stage_events.clear();
-    if (c.profile && e == cudaSuccess)
+    if ((c.profile & 2) && e == cudaSuccess)
         e = cudaMemcpy(c.stats, c.d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
-    c.profile = false;
+    c.profile = 0;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
     // mean over samples
     std::vector<double> sums((size_t)npix * 3);
@@ -705,6 +705,45 @@ ar_status ar_clear_error_word(ar_ctx* ctx)
     if (!ctx) return AR_ERR_INVALID;
     AR_CUDA(ctx, cudaMemset(ctx->c.d_err, 0, sizeof(unsigned int)));
     return AR_OK;
+}
+
+ar_status ar_host_trace_closest(const float* tris, int ntri, const float* rays, int nray, int32_t* ids, float* t,
+                                int64_t* node_visits)
+{
+    if (ntri < 0 || nray < 0 || (ntri > 0 && !tris) || (nray > 0 && (!rays || !ids))) return AR_ERR_INVALID;
+    std::vector<arbvh::PrimInput> prims((size_t)ntri);
+    for (int i = 0; i < ntri; ++i)
+    {
+        arbvh::PrimInput& p = prims[i];
+        const float* v = tris + 9 * (size_t)i;
+        std::memcpy(p.v, v, 9 * sizeof(float));
+        p.id = (uint32_t)i;
+        p.kind = AR_PRIM_KIND_TRI;
+        for (int k = 0; k < 3; ++k)
+        {
+            p.lo[k] = std::min(v[k], std::min(v[3 + k], v[6 + k]));
+            p.hi[k] = std::max(v[k], std::max(v[3 + k], v[6 + k]));
+        }
+    }
+    arbvh::WideBVH bvh;
+    std::string err;
+    if (!arbvh::build_wide_bvh(prims, bvh, &err)) return AR_ERR_INVALID;
+    TravScene sc;
+    sc.nodes = reinterpret_cast<const uint4*>(bvh.nodes.data());
+    sc.slots = reinterpret_cast<const float4*>(bvh.slots.data());
+    sc.objects = nullptr;
+    sc.node_count = (int)bvh.nodes.size();
+    unsigned int errw = 0;
+    unsigned long long stats[2] = {0, 0};
+    for (int r = 0; r < nray; ++r)
+    {
+        const float* q = rays + 8 * (size_t)r;
+        const TravResult res = traverse<false>(sc, v3(q[0], q[1], q[2]), v3(q[4], q[5], q[6]), q[3], q[7], &errw, stats);
+        ids[r] = res.id;
+        if (t) t[r] = res.slot >= 0 ? res.t : -1.0f;
+    }
+    if (node_visits) *node_visits = (int64_t)stats[0];
+    return errw ? AR_ERR_DEVICE : AR_OK;
 }
 
 ar_status ar_host_rgb_encode(const float* rgb, int n, float* out)

@@ -571,7 +571,7 @@ struct StageScope
     cudaEvent_t a = nullptr;
     StageScope(Ctx& cc, int st) : c(cc), stage(st)
     {
-        if (c.profile)
+        if (c.profile & 1)
         {
             cudaEventCreate(&a);
             cudaEventRecord(a, c.stream);
@@ -579,7 +579,7 @@ struct StageScope
     }
     ~StageScope()
     {
-        if (c.profile)
+        if (c.profile & 1)
         {
             cudaEvent_t b;
             cudaEventCreate(&b);

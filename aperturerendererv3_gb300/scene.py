@@ -203,7 +203,7 @@ class SceneRenderer:
         p.seed = int(seed)
         p.first_frame = int(first_frame)
         p.wave_paths = int(wave_paths)
-        p.profile = 1 if profile else 0
+        p.profile = int(profile)  # 1: stage times, 2: traversal counters, 3: both
         return p
 
     def Render(self, size, cameraOrigin, cameraDirection, sampleNum: int = 1024, *, fov: float = 60.0,

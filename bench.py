@@ -136,7 +136,7 @@ def run_reference(args, w) -> dict:
     if args.workload == "cornell":
         sample_size, sample_spp = size, 2
     else:
-        sample_size, sample_spp = (96, 54), 1
+        sample_size, sample_spp = (32, 18), 1
     vals = []
     for i in range(args.warmup + args.steps):
         st, wall = cpu_reference_run(args.workload, objs, mesh, cam, w, sample_spp, sample_size, threads)
@@ -222,10 +222,19 @@ def main() -> None:
     value = total / (dev_ms / 1e3) / 1e6
     e2e = total / wall / 1e6
 
-    # profiled render (outside the timed region): stage times + traversal counters
-    r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
-             first_frame=(args.warmup + args.steps) * world * spp, profile=True)
+    # profiled renders (outside the timed region) of the same step: stage times
+    # from events only, then traversal counters in a second pass (the counters'
+    # atomics would distort the times)
+    probe_frame = (args.warmup + args.steps) * world * spp
+    r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, first_frame=probe_frame,
+             profile=1)
     prof = r.render_profile()
+    r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, first_frame=probe_frame,
+             profile=2)
+    counters = r.render_profile()
+    for k in ("extend_rays", "extend_node_visits", "extend_prim_tests", "shadow_rays", "shadow_node_visits",
+              "shadow_prim_tests"):
+        prof[k] = counters[k]
     node_b, slot_b, ray_io_b = 80, 48, 16 + 16 + 4 + 4 + 16 + 4 + 4  # node, primitive slot, per-ray state in/out
     alg_bytes = prof["extend_node_visits"] * node_b + prof["extend_prim_tests"] * slot_b + prof["extend_rays"] * ray_io_b
     launches_ext = max(1, prof["extend_launches"])
@@ -256,7 +265,7 @@ def main() -> None:
     if rank == 0 and not args.no_cpu_baseline:
         try:
             threads = os.cpu_count() or 1
-            sample_size, sample_spp = ((size[0], size[1]), 2) if args.workload == "cornell" else ((96, 54), 1)
+            sample_size, sample_spp = ((size[0], size[1]), 2) if args.workload == "cornell" else ((32, 18), 1)
             st, _ = cpu_reference_run(args.workload, objs, mesh, cam, w, sample_spp, sample_size, threads)
             out["cpu_baseline"] = {"value": st["msamples_per_s"], "unit": "Msamples/s", "cores": st["threads"],
                                    "kind": "reference",

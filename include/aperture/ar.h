@@ -145,6 +145,10 @@ const char* ar_last_error(ar_ctx* ctx);
 ar_status ar_host_rgb_encode(const float* rgb, int n, float* basis_out);
 ar_status ar_host_lambda_encode(const float* lambda_nm, int n, float* basis_out);
 ar_status ar_host_sample_lambda(const float* u3, int n, float* lambda_out, float* pdf_out);
+/* Builds the wide BVH over n triangles (9 floats each) on the host and runs the
+ * kernels' closest-hit traversal on the CPU; same outputs as ar_trace_closest. */
+ar_status ar_host_trace_closest(const float* tris, int ntri, const float* rays, int nray, int32_t* prim_id, float* t,
+                                int64_t* node_visits);
 int ar_abi_version(void);
 
 #ifdef __cplusplus

@@ -180,18 +180,20 @@ static int cmd_trace(const char* tri_path, const char* ray_path, const char* out
     {
         ref_glue::g_node_visits = 0;
         ref_glue::g_prim_tests = 0;
+        // ray layout: origin, tmin, direction, tmax
         const float* q = rays + (size_t)r * 8;
-        const float3 o{q[0], q[1], q[2]}, d{q[3], q[4], q[5]};
+        const float3 o{q[0], q[1], q[2]}, d{q[4], q[5], q[6]};
+        const float tmin = q[3], tmax = q[7];
         IntersectionContext res{};
         if (brute)
         {
-            res.distance_ = q[7];
-            for (int i = 0; i < ntri; ++i) isect(0, i, o, d, q[6], res.distance_, &res);
+            res.distance_ = tmax;
+            for (int i = 0; i < ntri; ++i) isect(0, i, o, d, tmin, res.distance_, &res);
         }
         else
         {
             res = intersection::TraverseBVH<false>(0, o, d, isect, bvh.nodes_.data(), (int)bvh.nodes_.size(),
-                                                  bvh.objectIndices_.data(), q[6], q[7]);
+                                                  bvh.objectIndices_.data(), tmin, tmax);
         }
         ids[r] = res.bHit_ ? res.objectIndex_ : -1;
         ts[r] = res.bHit_ ? res.distance_ : -1.0f;

@@ -36,14 +36,19 @@ RENDERS = {
     "render_refcornell_full": ("reference_cornell", 24, 24, 2, 1000),
     "render_cornell_depth1": ("cornell_triangles", 24, 24, 2, 1),
     "render_cornell_depth8": ("cornell_triangles", 24, 24, 2, 8),
+    "render_terrain_small_depth16": ("terrain_small", 24, 24, 2, 16),
 }
 
 
 def scene_by_name(name):
+    """(objects, mesh, camera)"""
     if name == "reference_cornell":
-        return configs.reference_cornell(), configs.REFERENCE_CORNELL_CAMERA
+        return configs.reference_cornell(), None, configs.REFERENCE_CORNELL_CAMERA
     if name == "cornell_triangles":
-        return configs.cornell_triangles(), configs.CORNELL_CAMERA
+        return configs.cornell_triangles(), None, configs.CORNELL_CAMERA
+    if name == "terrain_small":
+        objs, mesh = configs.terrain_scene(res=48, n_spheres=8, seed=7)
+        return objs, mesh, configs.TERRAIN_CAMERA
     raise KeyError(name)
 
 
@@ -68,9 +73,9 @@ def main() -> None:
     assert np.array_equal(ids, bids) and np.array_equal(t.view(np.uint32), bt.view(np.uint32))
     np.savez(HERE / "trace_small.npz", tris=tris, rays=rays, ids=ids, t=t)
     for name, (scene, w, h, spp, depth) in RENDERS.items():
-        objs, cam = scene_by_name(scene)
+        objs, mesh, cam = scene_by_name(scene)
         mean, per, _ = rr.render(objs, (w, h), cam["origin"], cam["direction"], spp, fov=cam["fov"],
-                                 max_depth=depth, per_sample_frames=spp)
+                                 max_depth=depth, per_sample_frames=spp, mesh=mesh)
         np.savez(HERE / f"{name}.npz", per_sample=per, mean=mean, scene=scene, size=(w, h), spp=spp, depth=depth)
     print("golden fixtures written to", HERE)
 

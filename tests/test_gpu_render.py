@@ -15,9 +15,12 @@ ABS_FLOOR = 1e-6
 
 
 def scene(name):
-    if name == "reference_cornell":
-        return configs.reference_cornell(), configs.REFERENCE_CORNELL_CAMERA
-    return configs.cornell_triangles(), configs.CORNELL_CAMERA
+    """(objects, mesh, camera) as the golden fixtures were made."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.scene_by_name(name)
 
 
 def close(ours, ref):
@@ -26,13 +29,14 @@ def close(ours, ref):
 
 
 @pytest.mark.parametrize("name", ["render_refcornell_depth1", "render_cornell_depth1",
-                                  "render_refcornell_full", "render_cornell_depth8"])
+                                  "render_refcornell_full", "render_cornell_depth8",
+                                  "render_terrain_small_depth16"])
 def test_golden_per_sample_parity(cuda_device, name):
     g = np.load(GOLDEN / f"{name}.npz")
-    objs, cam = scene(str(g["scene"]))
+    objs, mesh, cam = scene(str(g["scene"]))
     w, h = (int(x) for x in g["size"])
     spp, depth = int(g["spp"]), int(g["depth"])
-    r = SceneRenderer(objs)
+    r = SceneRenderer(objs, mesh=mesh)
     mean, per = r.Render((w, h), cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
                          per_sample=True)
     ok = close(per, g["per_sample"])
@@ -42,23 +46,25 @@ def test_golden_per_sample_parity(cuda_device, name):
     assert r.error_word() == 0
 
 
-def test_larger_render_vs_live_oracle(cuda_device):
+@pytest.mark.parametrize("name,size,spp,depth", [("cornell_triangles", (96, 96), 4, 8),
+                                                   ("terrain_small", (80, 45), 3, 16)])
+def test_larger_render_vs_live_oracle(cuda_device, name, size, spp, depth):
     from oracle import ref_runner as rr
     if not rr.available():
         pytest.skip("reference oracle unavailable on this machine; golden tests cover parity")
-    objs, cam = scene("cornell_triangles")
-    r = SceneRenderer(objs)
-    mean, per = r.Render((96, 96), cam["origin"], cam["direction"], 4, fov=cam["fov"], max_depth=8,
+    objs, mesh, cam = scene(name)
+    r = SceneRenderer(objs, mesh=mesh)
+    mean, per = r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
                          per_sample=True)
-    rmean, rper, _ = rr.render(objs, (96, 96), cam["origin"], cam["direction"], 4, fov=cam["fov"], max_depth=8,
-                               per_sample_frames=4)
+    rmean, rper, _ = rr.render(objs, size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
+                               per_sample_frames=spp, mesh=mesh)
     ok = close(per, rper)
     assert ok.mean() == 1.0, f"{100 * (1 - ok.mean()):.4f}% of sample channels differ"
     np.testing.assert_allclose(mean, rmean, rtol=1e-5, atol=1e-6)
 
 
 def test_render_is_deterministic_and_wave_size_independent(cuda_device):
-    objs, cam = scene("cornell_triangles")
+    objs, _, cam = scene("cornell_triangles")
     r = SceneRenderer(objs)
     a = r.Render((64, 48), cam["origin"], cam["direction"], 3, fov=cam["fov"], max_depth=8)
     b = r.Render((64, 48), cam["origin"], cam["direction"], 3, fov=cam["fov"], max_depth=8, wave_paths=1000)
@@ -68,7 +74,7 @@ def test_render_is_deterministic_and_wave_size_independent(cuda_device):
 
 def test_errors_are_reported_not_raised_on_device(cuda_device):
     from aperturerendererv3_gb300 import ArError
-    objs, cam = scene("cornell_triangles")
+    objs, _, cam = scene("cornell_triangles")
     r = SceneRenderer(objs)
     with pytest.raises(ArError):
         r.Render((0, 16), cam["origin"], cam["direction"], 1)

@@ -116,5 +116,6 @@ def test_single_triangle_and_analytic_objects(cuda_device):
                      [9.0, 9.0, 5.0, 0.0, 0.0, 0.0, -1.0, np.inf]], np.float32)
     ids, t, hit = gpu_trace(r, rays)
     assert list(ids) == [0, 1, 2, -1]
-    assert t[0] == np.float32(5.0)
+    assert abs(t[0] - 5.0) < 1e-6
     assert abs(t[2] - 4.5) < 1e-6
+    assert list(hit) == [1, 1, 1, 0]
