@@ -163,9 +163,15 @@ def main() -> None:
     ap.add_argument("--workload", default="cornell", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", default=None, help="WxH override (small profiling cases)")
+    ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.size:
+        w["size"] = tuple(int(x) for x in args.size.lower().split("x"))
+    if args.spp:
+        w["spp"] = args.spp
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
