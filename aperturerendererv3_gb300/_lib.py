@@ -65,7 +65,7 @@ class ArRenderProfile(C.Structure):
 EXPORTED = [
     "ar_create", "ar_destroy", "ar_scene_set_materials", "ar_scene_set_objects", "ar_scene_set_mesh",
     "ar_scene_build", "ar_scene_stats", "ar_render", "ar_trace_closest", "ar_trace_any", "ar_last_render_stats",
-    "ar_last_render_profile",
+    "ar_last_render_profile", "ar_render_noalloc",
     "ar_get_error_word", "ar_clear_error_word", "ar_last_error", "ar_host_rgb_encode", "ar_host_lambda_encode",
     "ar_host_sample_lambda", "ar_host_trace_closest", "ar_abi_version",
 ]
@@ -99,6 +99,7 @@ def load() -> C.CDLL:
         "ar_scene_build": (C.c_int, [vp]),
         "ar_scene_stats": (C.c_int, [vp, P(C.c_int64), P(C.c_int64), P(C.c_int32), P(C.c_int64)]),
         "ar_render": (C.c_int, [vp, P(ArRenderParams), vp, C.c_int, vp, vp]),
+        "ar_render_noalloc": (C.c_int, [vp, P(ArRenderParams), vp, vp]),
         "ar_trace_closest": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
         "ar_trace_any": (C.c_int, [vp, vp, C.c_int, vp, vp]),
         "ar_last_render_stats": (C.c_int, [vp, P(C.c_float), P(C.c_int64)]),

@@ -145,6 +145,19 @@ struct Ctx
 
 DevScene dev_scene(const Ctx& c);
 
+// Wavefront working set supplied by the caller (allocation-free rendering).
+struct WaveBuffers
+{
+    PathState ps;
+    ShadowQueue sq;
+    int* queue[2];
+    int* counters;   // 3 ints
+    double* accum;   // 3 doubles per pixel
+    cudaStream_t stream;
+};
+cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb, int device, const RenderLaunch& rl,
+                                       int camera_inside, long long first_path, int n, unsigned int* err);
+
 // kernel launchers (render.cu / trace.cu)
 cudaError_t launch_build_rgb_lut(float* lut, const float* weights_dev, cudaStream_t s);
 cudaError_t launch_prepare_materials(Material* mats, int n, const float* lut, cudaStream_t s);

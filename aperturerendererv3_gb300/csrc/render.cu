@@ -639,6 +639,40 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     return cudaGetLastError();
 }
 
+// Wave launch over caller-provided buffers (used by the allocation-free entry
+// point); same kernel sequence as launch_render_wave.
+cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb, int device, const RenderLaunch& rl,
+                                       int camera_inside, long long first_path, int n, unsigned int* err)
+{
+    cudaStream_t s = wb.stream;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
+    const int grid_p = sms * 8;
+    int* cnt = wb.counters;
+    const CamParams cam = make_camera(rl);
+    k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(wb.ps, wb.queue[0], &cnt[0], first_path, n, rl.width, rl.height, rl.seed,
+                                         rl.first_frame, cam, camera_inside);
+    ShadeParams prm;
+    prm.use_nee = rl.use_nee;
+    prm.max_depth = rl.max_depth;
+    for (int b = 0; b < rl.max_depth; ++b)
+    {
+        const int cur = b & 1, nxt = cur ^ 1;
+        cudaMemsetAsync(&cnt[nxt], 0, sizeof(int), s);
+        cudaMemsetAsync(&cnt[2], 0, sizeof(int), s);
+        k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[cur], err);
+        k_shade<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[cur], wb.queue[nxt], &cnt[nxt], &cnt[2],
+                                            prm);
+        k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[2], err);
+    }
+    k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);
+    const long long npix = (long long)rl.width * rl.height;
+    k_accumulate<<<(int)((npix + AR_BLOCK - 1) / AR_BLOCK), AR_BLOCK, 0, s>>>(wb.ps.out_xyz, first_path, n, npix,
+                                                                             wb.accum);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_accumulate(Ctx& c, const RenderLaunch& rl, long long first_path, int n, double* accum, long long* launches)
 {
     const long long npix = (long long)rl.width * rl.height;

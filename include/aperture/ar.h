@@ -131,6 +131,24 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* params, double* out_xyz
 ar_status ar_trace_closest(ar_ctx* ctx, const float* rays, int n, int32_t* prim_id, float* t, void* stream);
 ar_status ar_trace_any(ar_ctx* ctx, const float* rays, int n, int32_t* hit, void* stream);
 
+/* Allocation-free rendering.  No counterpart in the reference: it exists for
+ * callers that must not allocate device memory (a frame loop that cannot
+ * afford the device-wide synchronisation of cudaFree, an application whose
+ * memory pool owns every allocation).  Same result as ar_render, written as
+ * per-pixel mean XYZ (3 doubles per pixel) into the caller's DEVICE buffer
+ * out_xyz_device, which also serves as the FP64 accumulator.  The wavefront
+ * working set comes from one fixed 8 MiB array in the library image
+ * (AR_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library until
+ * exit), so at most AR_NOALLOC_MAX_PATHS paths are in flight per wave;
+ * params->wave_paths above that is rejected with AR_ERR_INVALID (0 = the
+ * maximum).  The first call on a device looks the array up with
+ * cudaGetSymbolAddress and must happen before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race, so serialise them.  No
+ * cudaMalloc / cudaFree is made; profiling (params->profile) is rejected. */
+#define AR_NOALLOC_SCRATCH_BYTES (8u << 20)
+#define AR_NOALLOC_MAX_PATHS 49408
+ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* params, double* out_xyz_device, void* stream);
+
 /* Device time (ms) of the last ar_render and the number of kernels it launched. */
 ar_status ar_last_render_stats(ar_ctx* ctx, float* device_ms, int64_t* kernel_launches);
 /* Stage times and traversal counters of the last profiled ar_render. */
