@@ -47,7 +47,11 @@ class ArRenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("cam_origin", F3), ("cam_dir", F3), ("fov_deg", C.c_float), ("use_nee", C.c_int32),
                 ("seed", C.c_uint64), ("first_frame", C.c_int32), ("wave_paths", C.c_int32),
-                ("profile", C.c_int32)]
+                ("profile", C.c_int32), ("guide", C.c_int32), ("guide_unit", C.c_float)]
+
+
+GUIDE_NONE = 0
+GUIDE_VOXEL = 1
 
 
 class ArRenderProfile(C.Structure):
@@ -65,9 +69,9 @@ class ArRenderProfile(C.Structure):
 EXPORTED = [
     "ar_create", "ar_destroy", "ar_scene_set_materials", "ar_scene_set_objects", "ar_scene_set_mesh",
     "ar_scene_build", "ar_scene_stats", "ar_render", "ar_trace_closest", "ar_trace_any", "ar_last_render_stats",
-    "ar_last_render_profile", "ar_render_noalloc",
+    "ar_last_render_profile", "ar_render_noalloc", "ar_guide_reset", "ar_guide_stats",
     "ar_get_error_word", "ar_clear_error_word", "ar_last_error", "ar_host_rgb_encode", "ar_host_lambda_encode",
-    "ar_host_sample_lambda", "ar_host_trace_closest", "ar_abi_version",
+    "ar_host_sample_lambda", "ar_host_trace_closest", "ar_host_guide_eval", "ar_abi_version",
 ]
 
 _lib = None
@@ -104,6 +108,8 @@ def load() -> C.CDLL:
         "ar_trace_any": (C.c_int, [vp, vp, C.c_int, vp, vp]),
         "ar_last_render_stats": (C.c_int, [vp, P(C.c_float), P(C.c_int64)]),
         "ar_last_render_profile": (C.c_int, [vp, P(ArRenderProfile)]),
+        "ar_guide_reset": (C.c_int, [vp, P(C.c_int32)]),
+        "ar_guide_stats": (C.c_int, [vp, P(C.c_int32), P(C.c_int32)]),
         "ar_get_error_word": (C.c_int, [vp, P(C.c_uint32)]),
         "ar_clear_error_word": (C.c_int, [vp]),
         "ar_last_error": (C.c_char_p, [vp]),
@@ -111,6 +117,7 @@ def load() -> C.CDLL:
         "ar_host_lambda_encode": (C.c_int, [vp, C.c_int, vp]),
         "ar_host_sample_lambda": (C.c_int, [vp, C.c_int, vp, vp]),
         "ar_host_trace_closest": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp, P(C.c_int64)]),
+        "ar_host_guide_eval": (C.c_int, [vp, C.c_int, vp]),
         "ar_abi_version": (C.c_int, []),
     }
     for name, (res, args) in sig.items():

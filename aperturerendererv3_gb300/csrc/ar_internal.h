@@ -8,11 +8,78 @@
 #include <vector>
 
 #include "ar_bvh_build.h"
+#include "ar_guide.h"
 #include "ar_shade.h"
 #include "ar_traverse.cuh"
 
 namespace ar
 {
+// Voxel guide as the kernels see it: a sparse open-addressing hash from the
+// packed (voxel, face) key to a probe index, and the probe pool.  The
+// reference keeps the same sparse key set as a sorted unique array
+// (core/guiding/guiding.cuh:84-160); a hash gives O(1) lookups and inserts
+// without a sort, and any scene extent works.
+constexpr unsigned long long AR_PG_KEY_EMPTY = ~0ull;
+constexpr int AR_PG_HASH_PROBES = 64;  // linear-probe limit; a key that finds no slot stays unguided
+constexpr int AR_PG_KEY_BITS = 19;     // per axis, signed: +-262144 voxels
+
+struct DevGuide
+{
+    const unsigned long long* keys;
+    const int* vals;     // probe index; -3 = key known but the pool was full
+    const Probe* probes;
+    int probe_count;     // > 0 once any probe exists
+    unsigned mask;       // hash slots - 1 (power of two)
+    float inv_unit;
+};
+
+// packed key: face (5 bits) | z | y | x (19 bits each, biased); EMPTY if out of range
+AR_HD unsigned long long guide_pack(VoxelKey k)
+{
+    const int lim = 1 << (AR_PG_KEY_BITS - 1);
+    if (k.f < 0 || k.f >= AR_PG_FACES) return AR_PG_KEY_EMPTY;
+    if (k.x < -lim || k.x >= lim || k.y < -lim || k.y >= lim || k.z < -lim || k.z >= lim) return AR_PG_KEY_EMPTY;
+    const unsigned long long m = (1ull << AR_PG_KEY_BITS) - 1ull;
+    return ((unsigned long long)k.f << (3 * AR_PG_KEY_BITS)) |
+           ((unsigned long long)(unsigned)(k.z + lim) & m) << (2 * AR_PG_KEY_BITS) |
+           ((unsigned long long)(unsigned)(k.y + lim) & m) << AR_PG_KEY_BITS |
+           ((unsigned long long)(unsigned)(k.x + lim) & m);
+}
+
+AR_HD unsigned guide_hash(unsigned long long key)
+{
+    key ^= key >> 33;
+    key *= 0xff51afd7ed558ccdull;
+    key ^= key >> 33;
+    key *= 0xc4ceb9fe1a85ec53ull;
+    key ^= key >> 33;
+    return (unsigned)key;
+}
+
+// probe index for a packed key, -1 when it has none
+AR_HD int guide_lookup(const DevGuide& g, unsigned long long key)
+{
+    if (key == AR_PG_KEY_EMPTY || g.keys == nullptr) return -1;
+    unsigned s = guide_hash(key) & g.mask;
+    for (int i = 0; i < AR_PG_HASH_PROBES; ++i)
+    {
+        const unsigned long long k = AR_LDG(&g.keys[s]);
+        if (k == key) return AR_LDG(&g.vals[s]);
+        if (k == AR_PG_KEY_EMPTY) return -1;
+        s = (s + 1u) & g.mask;
+    }
+    return -1;
+}
+
+// Radiance records emitted at path end (core/guiding/guiding.cuh:22-32)
+struct GuideSamples
+{
+    float4* radiance;         // xyz
+    float4* dir;              // xyz
+    unsigned long long* key;  // packed voxel key, EMPTY = out of range
+    int* count;
+    int capacity;
+};
 // Device-side scene as the kernels see it (passed by value).
 struct DevScene
 {
@@ -31,6 +98,7 @@ struct DevScene
     // profiling counters (null unless profiling): extend visits, extend tests,
     // shadow visits, shadow tests, extend rays, shadow rays
     unsigned long long* stats;
+    DevGuide guide;
 };
 
 // stage ids for the per-stage profile
@@ -69,6 +137,12 @@ struct PathState
     int* hit_slot;
     float* out_xyz;     // 3 per path
     int capacity;
+    // guided rendering only: RGB probe query and the per-vertex radiance
+    // collection (AR_PG_COLLECT_DEPTH slots of capacity entries each)
+    float4* maskq;      // xyz query
+    float4* pg_dir;     // xyz sampled direction, w = collected radiance
+    float4* pg_loc;     // xyz vertex position, w = radiance mask
+    float4* pg_vdir;    // xyz reflected direction (voxel face key)
 };
 
 struct ShadowQueue
@@ -89,6 +163,7 @@ struct RenderLaunch
     uint64_t seed;
     int first_frame;
     int profile;
+    int guide;  // 0 none, 1 voxel probes
 };
 
 struct Ctx
@@ -141,7 +216,24 @@ struct Ctx
     float stage_ms[ST_COUNT] = {0, 0, 0, 0, 0};
     long long stage_launches[ST_COUNT] = {0, 0, 0, 0, 0};
     unsigned long long stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // voxel guide
+    DevGuide guide{};
+    unsigned long long* d_pg_keys = nullptr;  // hash slots: packed voxel key
+    int* d_pg_vals = nullptr;                 // hash slots: probe index
+    Probe* d_pg_probes = nullptr;
+    Probe* d_pg_temp = nullptr;
+    int* d_pg_meta = nullptr;     // [0] probe count, [1] sample count
+    int pg_capacity = 0;
+    int pg_hash_slots = 0;
+    float pg_unit = 0.0f;
+    GuideSamples gs{};
+    int gs_capacity = 0;
+    int pg_path_cap = 0;  // wavefront capacity the collection slots were sized for
 };
+
+// voxel guide (guide.cu)
+cudaError_t launch_guide_update(Ctx& c, long long* launches);
+int guide_probe_count(Ctx& c);
 
 DevScene dev_scene(const Ctx& c);
 

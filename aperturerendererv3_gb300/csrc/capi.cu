@@ -16,6 +16,7 @@
 
 #include "../../include/aperture/ar.h"
 #include "ar_internal.h"
+#include "ar_rng.h"
 #include "spectral_tables.inc"
 
 struct ar_ctx
@@ -44,6 +45,7 @@ DevScene dev_scene(const Ctx& c)
     s.d65 = c.d_d65;
     s.camera_inside = c.camera_inside;
     s.stats = (c.profile & 2) ? c.d_stats : nullptr;
+    s.guide = c.guide;
     return s;
 }
 } // namespace ar
@@ -140,6 +142,97 @@ ar_status ensure_waves(ar_ctx* ctx, int cap)
     AR_CUDA(ctx, alloc_dev(c.d_queue[1], n));
     p.capacity = cap;
     c.wave_capacity = cap;
+    return AR_OK;
+}
+
+void free_guide(Ctx& c)
+{
+    free_dev(c.d_pg_keys);
+    free_dev(c.d_pg_vals);
+    free_dev(c.d_pg_probes);
+    free_dev(c.d_pg_temp);
+    free_dev(c.d_pg_meta);
+    free_dev(c.gs.radiance);
+    free_dev(c.gs.dir);
+    free_dev(c.gs.key);
+    free_dev(c.gs.count);
+    free_dev(c.ps.maskq);
+    free_dev(c.ps.pg_dir);
+    free_dev(c.ps.pg_loc);
+    free_dev(c.ps.pg_vdir);
+    c.guide = DevGuide{};
+    c.pg_capacity = 0;
+    c.pg_hash_slots = 0;
+    c.pg_unit = 0.0f;
+    c.gs = GuideSamples{};
+    c.gs_capacity = 0;
+    c.pg_path_cap = 0;
+}
+
+// Voxel-guide storage: dense index table over the scene's voxel box (voxel =
+// floor(p / unit), as the reference keys its sparse volume) and a probe pool.
+ar_status ensure_guide(ar_ctx* ctx, float unit, long long npix)
+{
+    Ctx& c = ctx->c;
+    if (!(unit > 0.0f)) unit = 0.05f;
+    if (c.d_pg_keys && c.pg_unit == unit && c.ps.maskq && c.pg_path_cap == c.ps.capacity &&
+        (long long)c.gs_capacity >= AR_PG_COLLECT_DEPTH * npix)
+        return AR_OK;
+    const bool keep_probes = c.d_pg_keys && c.pg_unit == unit;
+    if (!keep_probes)
+    {
+        free_guide(c);
+        // probe pool of 131072 probes (182 MB) and a hash at load factor <= 1/4
+        const int capacity = 131072;
+        const int slots = 4 * capacity;
+        AR_CUDA(ctx, cudaMalloc((void**)&c.d_pg_keys, (size_t)slots * sizeof(unsigned long long)));
+        AR_CUDA(ctx, cudaMemset(c.d_pg_keys, 0xff, (size_t)slots * sizeof(unsigned long long)));
+        AR_CUDA(ctx, cudaMalloc((void**)&c.d_pg_vals, (size_t)slots * sizeof(int)));
+        AR_CUDA(ctx, cudaMemset(c.d_pg_vals, 0xff, (size_t)slots * sizeof(int)));
+        AR_CUDA(ctx, cudaMalloc((void**)&c.d_pg_probes, (size_t)capacity * sizeof(Probe)));
+        AR_CUDA(ctx, cudaMemset(c.d_pg_probes, 0, (size_t)capacity * sizeof(Probe)));
+        AR_CUDA(ctx, cudaMalloc((void**)&c.d_pg_temp, (size_t)capacity * sizeof(Probe)));
+        AR_CUDA(ctx, cudaMemset(c.d_pg_temp, 0, (size_t)capacity * sizeof(Probe)));
+        AR_CUDA(ctx, cudaMalloc((void**)&c.d_pg_meta, 4 * sizeof(int)));
+        AR_CUDA(ctx, cudaMemset(c.d_pg_meta, 0, 4 * sizeof(int)));
+        c.pg_capacity = capacity;
+        c.pg_hash_slots = slots;
+        c.pg_unit = unit;
+        c.guide.keys = c.d_pg_keys;
+        c.guide.vals = c.d_pg_vals;
+        c.guide.probes = c.d_pg_probes;
+        c.guide.probe_count = 0;
+        c.guide.mask = (unsigned)(slots - 1);
+        c.guide.inv_unit = 1.0f / unit;
+    }
+    // per-path collection slots use the wavefront buffers' stride; the record
+    // buffer holds a whole frame (up to AR_PG_COLLECT_DEPTH records per pixel)
+    const int wave_cap = c.ps.capacity;
+    const size_t ns = (size_t)AR_PG_COLLECT_DEPTH * wave_cap;
+    const size_t nrec = (size_t)AR_PG_COLLECT_DEPTH * (size_t)npix;
+    if (c.gs_capacity < (long long)nrec)
+    {
+        free_dev(c.gs.radiance);
+        free_dev(c.gs.dir);
+        free_dev(c.gs.key);
+        free_dev(c.gs.count);
+        AR_CUDA(ctx, alloc_dev(c.gs.radiance, nrec));
+        AR_CUDA(ctx, alloc_dev(c.gs.dir, nrec));
+        AR_CUDA(ctx, alloc_dev(c.gs.key, nrec));
+        AR_CUDA(ctx, alloc_dev(c.gs.count, 1));
+        AR_CUDA(ctx, cudaMemset(c.gs.count, 0, sizeof(int)));
+        c.gs.capacity = (int)nrec;
+        c.gs_capacity = (int)nrec;
+    }
+    free_dev(c.ps.maskq);
+    free_dev(c.ps.pg_dir);
+    free_dev(c.ps.pg_loc);
+    free_dev(c.ps.pg_vdir);
+    AR_CUDA(ctx, alloc_dev(c.ps.maskq, (size_t)wave_cap));
+    AR_CUDA(ctx, alloc_dev(c.ps.pg_dir, ns));
+    AR_CUDA(ctx, alloc_dev(c.ps.pg_loc, ns));
+    AR_CUDA(ctx, alloc_dev(c.ps.pg_vdir, ns));
+    c.pg_path_cap = wave_cap;
     return AR_OK;
 }
 
@@ -295,6 +388,7 @@ ar_status ar_destroy(ar_ctx* ctx)
     cudaSetDevice(c.device);
     if (c.stream) cudaStreamSynchronize(c.stream);
     free_scene(c);
+    free_guide(c);
     free_waves(c);
     free_dev(c.d_lut_rgb);
     free_dev(c.d_lut_lambda);
@@ -466,8 +560,9 @@ ar_status ar_scene_build(ar_ctx* ctx)
         c.lights[k].cdf = acc;
     }
 
-    // device upload
+    // device upload (a rebuilt scene starts with an empty guide)
     free_scene(c);
+    free_guide(c);
     std::vector<Object> objs(c.objects);
     if (objs.empty()) objs.resize(1);
     AR_CUDA(ctx, alloc_dev(c.d_nodes, c.bvh.nodes.size() * sizeof(ar_wide_node)));
@@ -577,10 +672,19 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     }
     const long long npix = (long long)rl.width * rl.height;
     const long long total = npix * rl.spp;
+    rl.guide = prm->guide;
+    if (rl.guide != 0 && rl.guide != 1) return fail(ctx, AR_ERR_INVALID, "render: unknown guide mode");
     int cap = prm->wave_paths > 0 ? prm->wave_paths : (1 << 21);
     if ((long long)cap > total) cap = (int)total;
+    // guided frames learn from the previous frame: waves never straddle frames
+    if (rl.guide && (long long)cap > npix) cap = (int)npix;
     ar_status st = ensure_waves(ctx, cap);
     if (st != AR_OK) return st;
+    if (rl.guide)
+    {
+        st = ensure_guide(ctx, prm->guide_unit, npix);
+        if (st != AR_OK) return st;
+    }
     if (c.accum_pixels < (size_t)npix)
     {
         free_dev(c.d_accum);
@@ -596,13 +700,23 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     cudaEventRecord(e0, c.stream);
     long long launches = 0;
     cudaError_t e = cudaSuccess;
-    for (long long first = 0; first < total && e == cudaSuccess; first += cap)
+    for (long long first = 0; first < total && e == cudaSuccess;)
     {
-        const int n = (int)std::min<long long>(cap, total - first);
+        // a wave never crosses a frame boundary in guided mode
+        long long n_ll = std::min<long long>(cap, total - first);
+        if (rl.guide) n_ll = std::min<long long>(n_ll, npix - first % npix);
+        const int n = (int)n_ll;
         e = launch_render_wave(c, rl, first, n, d_samples, &launches);
         if (e == cudaSuccess) e = launch_accumulate(c, rl, first, n, c.d_accum, &launches);
         if (e == cudaSuccess && per_sample_xyz)
             e = cudaMemcpyAsync(per_sample_xyz + 3 * first, d_samples, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, c.stream);
+        first += n;
+        if (rl.guide && e == cudaSuccess && first % npix == 0)
+        {
+            // end of a frame: learn from its radiance records (core/scene.cu:258-273)
+            e = launch_guide_update(c, &launches);
+            c.guide.probe_count = 1;
+        }
     }
     cudaEventRecord(e1, c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
@@ -667,6 +781,28 @@ ar_status ar_last_render_stats(ar_ctx* ctx, float* ms, int64_t* launches)
     if (!ctx) return AR_ERR_INVALID;
     if (ms) *ms = ctx->c.last_render_ms;
     if (launches) *launches = ctx->c.last_launches;
+    return AR_OK;
+}
+
+ar_status ar_guide_stats(ar_ctx* ctx, int32_t* n_probes, int32_t* capacity)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
+    if (n_probes) *n_probes = guide_probe_count(c);
+    if (capacity) *capacity = c.pg_capacity;
+    return AR_OK;
+}
+
+ar_status ar_guide_reset(ar_ctx* ctx, int32_t* n_probes)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
+    if (n_probes) *n_probes = guide_probe_count(c);
+    free_guide(c);
     return AR_OK;
 }
 
@@ -744,6 +880,59 @@ ar_status ar_host_trace_closest(const float* tris, int ntri, const float* rays, 
     }
     if (node_visits) *node_visits = (int64_t)stats[0];
     return errw ? AR_ERR_DEVICE : AR_OK;
+}
+
+ar_status ar_host_guide_eval(const float* in, int n, float* out)
+{
+    // same record layout as the oracle's guide mode: leaf (AR_PG_RES2 x float4), then
+    // n x {dir 3, normal 3, query 3, pos 3, uv 2, seed as 2 floats}
+    if (n < 0 || !in || !out) return AR_ERR_INVALID;
+    Probe* pr = new (std::nothrow) Probe();
+    if (!pr) return AR_ERR_NOMEM;
+    std::memset(pr, 0, sizeof(Probe));
+    for (int i = 0; i < AR_PG_RES2; ++i) pr->data[i] = make_float4(in[4 * i], in[4 * i + 1], in[4 * i + 2], in[4 * i + 3]);
+    generate_mipmaps(*pr);
+    for (int i = 0; i < AR_PG_TEXELS_PAD; ++i)
+    {
+        out[4 * i] = pr->data[i].x;
+        out[4 * i + 1] = pr->data[i].y;
+        out[4 * i + 2] = pr->data[i].z;
+        out[4 * i + 3] = pr->data[i].w;
+    }
+    const float* rec = in + AR_PG_RES2 * 4;
+    for (int i = 0; i < n; ++i)
+    {
+        const float* r = rec + (size_t)i * 16;
+        const V3 dir = v3(r[0], r[1], r[2]), nrm = v3(r[3], r[4], r[5]), q = v3(r[6], r[7], r[8]);
+        const V3 pos = v3(r[9], r[10], r[11]);
+        uint64_t seed;
+        std::memcpy(&seed, r + 14, 8);
+        float* o = out + AR_PG_TEXELS_PAD * 4 + (size_t)i * 14;
+        const VoxelKey k = voxel_key(pos, dir, 1.0f / 0.05);
+        o[0] = (float)k.f;
+        o[1] = (float)k.x;
+        o[2] = (float)k.y;
+        o[3] = (float)k.z;
+        sphere_to_uv(dir, &o[4], &o[5]);
+        const V3 s = uv_to_sphere(r[12], r[13]);
+        o[6] = s.x;
+        o[7] = s.y;
+        o[8] = s.z;
+        o[9] = octahedron_hemisphere_pdf(*pr, dir, nrm, q);
+        struct HostRand
+        {
+            ar_pcg g;
+            float operator()() { return ar_rand1(&g); }
+        } R;
+        R.g = ar_pcg_init(seed, (uint64_t)i, 0);
+        const GuideSample gsmp = sample_octahedron_hemisphere(*pr, R, nrm, q);
+        o[10] = gsmp.dir.x;
+        o[11] = gsmp.dir.y;
+        o[12] = gsmp.dir.z;
+        o[13] = gsmp.pdf;
+    }
+    delete pr;
+    return AR_OK;
 }
 
 ar_status ar_host_rgb_encode(const float* rgb, int n, float* out)

@@ -208,8 +208,60 @@ struct ShadeParams
 {
     int use_nee;
     int max_depth;
+    int frame;  // frame index of the wave (guided rendering: mixture probability)
 };
 
+// CollectRadiance (core/render/render.cuh:353-432) on the path's collection
+// slots; valid bits live in flags bits 8..12.
+__device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uint32_t& fl, float endpointLe, V3 nextDir,
+                                                 float segContrib, float rrProb, int ndd, bool allowStart, bool advance,
+                                                 V3 rayDir, V3 hitLoc, V3 hitNrm)
+{
+    const int cap = ps.capacity;
+    if (endpointLe != 0.0f)
+    {
+        const int hi = min(ndd, AR_PG_COLLECT_DEPTH);
+        for (int i = 0; i < hi; ++i)
+        {
+            const float m = ps.pg_loc[i * cap + p].w;
+            if (m != 0.0f)
+            {
+                float4 d = ps.pg_dir[i * cap + p];
+                d.w = d.w + m * endpointLe;
+                ps.pg_dir[i * cap + p] = d;
+                fl |= 1u << (8 + i);
+            }
+        }
+    }
+    if (allowStart && ndd < AR_PG_COLLECT_DEPTH)
+    {
+        const float4 l = ps.pg_loc[ndd * cap + p];
+        if (l.w == 0.0f)
+        {
+            const float w = ps.pg_dir[ndd * cap + p].w;
+            ps.pg_dir[ndd * cap + p] = make_float4(nextDir.x, nextDir.y, nextDir.z, w);
+            ps.pg_loc[ndd * cap + p] = make_float4(hitLoc.x, hitLoc.y, hitLoc.z, 1.0f);
+            const V3 vd = reflect(rayDir, hitNrm);
+            ps.pg_vdir[ndd * cap + p] = make_float4(vd.x, vd.y, vd.z, 0.0f);
+        }
+    }
+    if (advance)
+    {
+        const float invQ = (float)(1.0 / (double)rrProb);
+        const int hi = min(ndd + (allowStart ? 1 : 0), AR_PG_COLLECT_DEPTH);
+        for (int i = 0; i < hi; ++i)
+        {
+            float4 l = ps.pg_loc[i * cap + p];
+            if (l.w != 0.0f)
+            {
+                l.w = l.w * (segContrib * invQ);
+                ps.pg_loc[i * cap + p] = l;
+            }
+        }
+    }
+}
+
+template <bool GUIDE>
 __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
                                                   const int* __restrict__ counter, int* next_queue, int* next_counter,
                                                   int* shadow_counter, ShadeParams prm)
@@ -304,11 +356,61 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
             }
             media = S.media;
 
+            // ---- guided mixture sampling (render.cuh:553-638)
+            const Probe* probe = nullptr;
+            V3 maskq = v3(1.0f, 1.0f, 1.0f);
+            float pgProb = 0.0f;
+            if constexpr (GUIDE)
+            {
+                const float4 mq = ps.maskq[p];
+                maskq = v3(mq.x, mq.y, mq.z);
+                pgProb = guide_probability(prm.frame);
+                if (h.hit && !S.delta && !S.pure_light && !media.inside && sc.guide.probe_count > 0)
+                {
+                    const VoxelKey key = voxel_key(h.pos, reflect(rayD, h.nrm), sc.guide.inv_unit);
+                    const int idx = guide_lookup(sc.guide, guide_pack(key));
+                    if (idx >= 0)
+                    {
+                        probe = &sc.guide.probes[idx];
+                        const float pB = S.pdf;
+                        const float pP = octahedron_hemisphere_pdf(*probe, S.next_dir, h.nrm, maskq);
+                        if (pB > 1.0e-12f && pP > 1.0e-12f)
+                        {
+                            if (R() < pgProb)
+                            {
+                                const GuideSample g = sample_octahedron_hemisphere(*probe, R, h.nrm, maskq);
+                                if (dot(g.dir, h.nrm) > 1.0e-12f)
+                                {
+                                    const float pBs = bsdf_pdf(lb, mat, h.nrm, rayD, g.dir);
+                                    S.next_dir = g.dir;
+                                    S.brdf = eval_bsdf_cos(lambda, lb, mat, rayD, g.dir, h, media);
+                                    S.pdf = (1.0f - pgProb) * fmaxf(pBs, 1.0e-12f) + pgProb * g.pdf;
+                                }
+                                else
+                                {
+                                    probe = nullptr;
+                                }
+                            }
+                            else
+                            {
+                                S.pdf = (1.0f - pgProb) * pB + pgProb * pP;
+                            }
+                        }
+                        else
+                        {
+                            probe = nullptr;
+                        }
+                    }
+                }
+            }
+
             // ---- emission (render.cuh:647-723)
+            V3 endpointLe = v3(0.0f, 0.0f, 0.0f);
             if (!h.hit)
             {
                 if (!S.miss_thin)
                 {
+                    endpointLe = S.emissive;
                     const PlainFetch f{sc.lut_rgb};
                     radiance = radiance + mask * interact_rgb(lb, S.emissive, f) * d65;
                 }
@@ -326,7 +428,18 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                     else if (L.type == AR_OBJ_SPHERE) pL = sphere_light_pdf_omega(sc.trav.objects[L.obj], L.select_prob, lastPos, h.pos, h.nrm);
                     if (pL >= 0.0f && pB > 0.0f) misW = power_heuristic(pB, pL);
                 }
+                endpointLe = S.emissive * misW;
                 radiance = radiance + mask * interact(mat.emissive_c, lb) * d65 * misW;
+            }
+            else if (!all_zero(S.emissive))
+            {
+                endpointLe = S.emissive;
+            }
+            if constexpr (GUIDE)
+            {
+                const PlainFetch f{sc.lut_rgb};
+                collect_radiance(ps, p, fl, interact_rgb(lb, endpointLe, f) * d65, S.next_dir, 0.0f, 1.0f, ndd, false,
+                                 false, rayD, h.pos, h.nrm);
             }
 
             const bool ended = (!h.hit && !S.miss_thin) || S.terminate;
@@ -391,7 +504,13 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                                 const float le = interact(sc.materials[ls.material].emissive_c, lb);
                                 const float contribution = brdfCos * le * (G / pATotal);
                                 const float pLight = area_to_solid_angle_pdf(h.pos, ls.point, ls.normal, ls.p_facet * ls.p_a);
-                                const float pBsdf = fmaxf(bsdf_pdf(lb, mat, h.nrm, rayD, L), 0.0f);
+                                float pBsdf = fmaxf(bsdf_pdf(lb, mat, h.nrm, rayD, L), 0.0f);
+                                if constexpr (GUIDE)
+                                {
+                                    if (probe)
+                                        pBsdf = (1.0f - pgProb) * pBsdf +
+                                                pgProb * octahedron_hemisphere_pdf(*probe, L, h.nrm, maskq);
+                                }
                                 const float misW = power_heuristic(pLight, pBsdf);
                                 vUn = mask * (contribution * misW) * d65;
                                 validUn = true;
@@ -439,8 +558,22 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                 }
                 if (survived)
                 {
+                    if constexpr (GUIDE)
+                    {
+                        const bool allowStart = h.hit && !S.delta && !S.pure_light && !media.inside;
+                        collect_radiance(ps, p, fl, 0.0f, S.next_dir, contrib, pSurvive, ndd, allowStart, true, rayD, h.pos,
+                                         h.nrm);
+                    }
                     mask = mask * contrib;
                     mask = mask / pSurvive;
+                    if constexpr (GUIDE)
+                    {
+                        const V3 xyz = lambda_to_xyz(lambda, sc.cie_cmf);
+                        V3 q = vmax(mask * xyz, (float)AR_PG_QUERY_EPS);
+                        const float div = (float)((double)sum3(q) + AR_PG_QUERY_EPS);
+                        q = q / div;
+                        ps.maskq[p] = make_float4(q.x, q.y, q.z, 0.0f);
+                    }
                     if (!S.delta) ++ndd;
                     ++depth;
                     if (depth < prm.max_depth)
@@ -520,6 +653,50 @@ __global__ void k_finalize(DevScene sc, PathState ps, int n, float* __restrict__
         extra_out[3 * k + 0] = x;
         extra_out[3 * k + 1] = y;
         extra_out[3 * k + 2] = z;
+    }
+}
+
+// guided rendering: clear the collection slots and set the probe query
+__global__ void k_guide_init(PathState ps, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    ps.maskq[k] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    for (int i = 0; i < AR_PG_COLLECT_DEPTH; ++i)
+    {
+        ps.pg_dir[i * ps.capacity + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        ps.pg_loc[i * ps.capacity + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        ps.pg_vdir[i * ps.capacity + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+// radiance records of finished paths (core/render/render.cuh:909-963)
+__global__ void k_guide_emit(DevScene sc, PathState ps, int n, GuideSamples gs)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t fl = ps.flags[k];
+    if (((fl >> 8) & 31u) == 0u) return;
+    const float lambda = ps.ray_o[k].w;
+    const float pdf = ps.ray_d[k].w;
+    const V3 lxyz = lambda_to_xyz(lambda, sc.cie_cmf);
+    for (int i = 0; i < AR_PG_COLLECT_DEPTH; ++i)
+    {
+        if (!((fl >> (8 + i)) & 1u)) continue;
+        const float4 d = ps.pg_dir[i * ps.capacity + k];
+        const V3 xyz = lxyz * d.w / pdf;
+        const float strength = fminf(max3(xyz), AR_PG_COLLECT_MAX);
+        if (strength < AR_PG_COLLECT_MIN) continue;
+        const float4 l = ps.pg_loc[i * ps.capacity + k];
+        const float4 vd = ps.pg_vdir[i * ps.capacity + k];
+        const VoxelKey key = voxel_key(v3(l.x, l.y, l.z), v3(vd.x, vd.y, vd.z), sc.guide.inv_unit);
+        const unsigned long long packed = guide_pack(key);
+        const int slot = atomicAdd(gs.count, 1);
+        if (slot >= gs.capacity) continue;
+        const V3 rad = vmax(xyz, 0.0f);
+        gs.radiance[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        gs.dir[slot] = make_float4(d.x, d.y, d.z, 0.0f);
+        gs.key[slot] = packed;
     }
 }
 
@@ -605,11 +782,13 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         StageScope st(c, ST_RAYGEN);
         k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, c.d_queue[0], &cnt[0], first_path, n, rl.width, rl.height, rl.seed,
                                              rl.first_frame, cam, c.camera_inside);
+        if (rl.guide) k_guide_init<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, n);
     }
-    long long L = 1;
+    long long L = rl.guide ? 2 : 1;
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
+    prm.frame = rl.first_frame + (int)(first_path / ((long long)rl.width * rl.height));
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
@@ -621,8 +800,12 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         }
         {
             StageScope st(c, ST_SHADE);
-            k_shade<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur], c.d_queue[nxt], &cnt[nxt],
-                                                &cnt[2], prm);
+            if (rl.guide)
+                k_shade<true><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur], c.d_queue[nxt],
+                                                          &cnt[nxt], &cnt[2], prm);
+            else
+                k_shade<false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur], c.d_queue[nxt],
+                                                           &cnt[nxt], &cnt[2], prm);
         }
         {
             StageScope st(c, ST_SHADOW);
@@ -633,6 +816,11 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     {
         StageScope st(c, ST_FINAL);
         k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, c.ps, n, per_sample_out);
+        if (rl.guide)
+        {
+            k_guide_emit<<<grid_n, AR_BLOCK, 0, s>>>(sc, c.ps, n, c.gs);
+            ++L;
+        }
     }
     ++L;
     if (launches) *launches += L;
@@ -656,14 +844,15 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
+    prm.frame = rl.first_frame;
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
         cudaMemsetAsync(&cnt[nxt], 0, sizeof(int), s);
         cudaMemsetAsync(&cnt[2], 0, sizeof(int), s);
         k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[cur], err);
-        k_shade<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[cur], wb.queue[nxt], &cnt[nxt], &cnt[2],
-                                            prm);
+        k_shade<false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[cur], wb.queue[nxt], &cnt[nxt],
+                                                   &cnt[2], prm);
         k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[2], err);
     }
     k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);

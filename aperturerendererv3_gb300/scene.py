@@ -191,7 +191,8 @@ class SceneRenderer:
         return {"nodes": n.value, "slots": s.value, "depth": d.value, "bytes": b.value}
 
     def params(self, size, cameraOrigin, cameraDirection, sampleNum, fov=60.0, max_depth=1000, use_nee=True,
-               seed=GLOBAL_SEED, first_frame=0, wave_paths=0, profile=False) -> ArRenderParams:
+               seed=GLOBAL_SEED, first_frame=0, wave_paths=0, profile=False, guide=0,
+               guide_unit=0.0) -> ArRenderParams:
         p = ArRenderParams()
         p.width, p.height = int(size[0]), int(size[1])
         p.spp = int(sampleNum)
@@ -204,18 +205,23 @@ class SceneRenderer:
         p.first_frame = int(first_frame)
         p.wave_paths = int(wave_paths)
         p.profile = int(profile)  # 1: stage times, 2: traversal counters, 3: both
+        p.guide = int(guide)
+        p.guide_unit = float(guide_unit)
         return p
 
     def Render(self, size, cameraOrigin, cameraDirection, sampleNum: int = 1024, *, fov: float = 60.0,
                max_depth: int = 1000, use_nee: bool = True, seed: int = GLOBAL_SEED, first_frame: int = 0,
-               per_sample: bool = False, wave_paths: int = 0, profile: bool = False):
+               per_sample: bool = False, wave_paths: int = 0, profile: bool = False, guide: int = 0,
+               guide_unit: float = 0.0):
         """Mean linear XYZ per pixel, shape (height, width, 3), float64.
 
         With per_sample=True also returns every sample's XYZ, shape
-        (sampleNum, height, width, 3), float32."""
+        (sampleNum, height, width, 3), float32.  guide=1 turns on the voxel
+        path guide: frames render one sample per pixel each and the probes learn
+        after every frame (and persist across calls until ResetGuiding)."""
         self._build()
         p = self.params(size, cameraOrigin, cameraDirection, sampleNum, fov, max_depth, use_nee, seed, first_frame,
-                        wave_paths, profile)
+                        wave_paths, profile, guide, guide_unit)
         w, h = p.width, p.height
         out = np.zeros((h, w, 3), np.float64)
         ps = np.zeros((p.spp, h, w, 3), np.float32) if per_sample else None
@@ -228,6 +234,17 @@ class SceneRenderer:
         ms, n = C.c_float(), C.c_int64()
         check(self._ctx, self._lib.ar_last_render_stats(self._ctx, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def MarkNeedResetGuiding(self) -> int:
+        """Forgets the voxel guide's probes; returns how many there were."""
+        n = C.c_int32()
+        check(self._ctx, self._lib.ar_guide_reset(self._ctx, C.byref(n)))
+        return n.value
+
+    def guide_stats(self) -> tuple[int, int]:
+        n, cap = C.c_int32(), C.c_int32()
+        check(self._ctx, self._lib.ar_guide_stats(self._ctx, C.byref(n), C.byref(cap)))
+        return n.value, cap.value
 
     def render_profile(self) -> dict:
         prof = _lib.ArRenderProfile()

@@ -165,6 +165,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None, help="WxH override (small profiling cases)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
+    ap.add_argument("--guide", type=int, default=0, choices=[0, 1], help="1: voxel path guide on")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = dict(WORKLOADS[args.workload])
@@ -199,7 +200,7 @@ def main() -> None:
 
     def step(k: int):
         return r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
-                        first_frame=(k * world + rank) * spp)
+                        first_frame=(k * world + rank) * spp, guide=args.guide)
 
     for k in range(args.warmup):
         step(k)
@@ -233,10 +234,10 @@ def main() -> None:
     # atomics would distort the times)
     probe_frame = (args.warmup + args.steps) * world * spp
     r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, first_frame=probe_frame,
-             profile=1)
+             profile=1, guide=args.guide)
     prof = r.render_profile()
     r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, first_frame=probe_frame,
-             profile=2)
+             profile=2, guide=args.guide)
     counters = r.render_profile()
     for k in ("extend_rays", "extend_node_visits", "extend_prim_tests", "shadow_rays", "shadow_node_visits",
               "shadow_prim_tests"):
@@ -252,7 +253,7 @@ def main() -> None:
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": args.workload, "width": size[0], "height": size[1], "spp": spp, "max_depth": depth,
-                   "paths_per_step": samples, "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "guide": "voxel" if args.guide else "none", "paths_per_step": samples, "parallelism": "replicas" if world > 1 else "single-gpu",
                    "l2": "inputs larger than L2 (path state ~170 B x 2M paths in flight)"},
         "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 100,
                 "d2h_bytes_per_step": size[0] * size[1] * 3 * 8},

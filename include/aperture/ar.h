@@ -88,8 +88,17 @@ typedef struct ar_render_params
     uint64_t seed;           /* global seed (GLOBAL_SEED = 0x9e3779b97f4a7c15) */
     int32_t first_frame;     /* frame index of the first sample */
     int32_t wave_paths;      /* paths in flight per wave, 0 = automatic */
-    int32_t profile;         /* 1 = record per-stage device times and traversal counters */
+    int32_t profile;         /* 1 = per-stage device times, 2 = traversal counters, 3 = both */
+    int32_t guide;           /* AR_GUIDE_NONE or AR_GUIDE_VOXEL (SceneSetting::bUsePathGuiding_) */
+    float guide_unit;        /* voxel size of the guide (0 = 0.05, PATH_GUIDING_RESOLUTION_UNIT) */
 } ar_render_params;
+
+/* Path guiding modes.  With AR_GUIDE_VOXEL, ar_render renders one frame (one
+ * sample per pixel) at a time and, after each frame, folds its radiance records
+ * into the context's voxel probes (core/scene.cu:240-273, 409-570); the probes
+ * persist across ar_render calls until ar_guide_reset or a scene rebuild. */
+#define AR_GUIDE_NONE 0
+#define AR_GUIDE_VOXEL 1
 
 /* Per-stage profile of the last ar_render with params->profile = 1. */
 typedef struct ar_render_profile
@@ -154,6 +163,12 @@ ar_status ar_last_render_stats(ar_ctx* ctx, float* device_ms, int64_t* kernel_la
 /* Stage times and traversal counters of the last profiled ar_render. */
 ar_status ar_last_render_profile(ar_ctx* ctx, ar_render_profile* out);
 
+/* Forgets the learned voxel probes (SceneRenderer::MarkNeedResetGuiding,
+ * core/scene.hpp:102-105).  n_probes (optional) receives the probe count first. */
+ar_status ar_guide_reset(ar_ctx* ctx, int32_t* n_probes);
+/* Number of probes the voxel guide holds. */
+ar_status ar_guide_stats(ar_ctx* ctx, int32_t* n_probes, int32_t* capacity);
+
 ar_status ar_get_error_word(ar_ctx* ctx, uint32_t* word);
 ar_status ar_clear_error_word(ar_ctx* ctx);
 const char* ar_last_error(ar_ctx* ctx);
@@ -167,6 +182,9 @@ ar_status ar_host_sample_lambda(const float* u3, int n, float* lambda_out, float
  * kernels' closest-hit traversal on the CPU; same outputs as ar_trace_closest. */
 ar_status ar_host_trace_closest(const float* tris, int ntri, const float* rays, int nray, int32_t* prim_id, float* t,
                                 int64_t* node_visits);
+/* Voxel-guide probe math on the host (mips, voxel keys, equal-area map, pdf,
+ * sampling) for one probe: the functions the guided kernels run. */
+ar_status ar_host_guide_eval(const float* in, int n, float* out);
 int ar_abi_version(void);
 
 #ifdef __cplusplus

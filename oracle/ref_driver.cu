@@ -436,6 +436,65 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
     return 0;
 }
 
+// ---------------------------------------------------------------- guide
+// Probe math of the reference's voxel guide on one probe: in = header
+// {int32 n} + leaf (Octahedron::resolution2_ x float4) + n x {dir 3, normal 3,
+// query 3, pos 3, uv 2, seed u64 as 2 floats}; out = all texels
+// (Octahedron::totalPixelCountWithPad_ x float4) + n x 14 floats:
+// face, voxel xyz, uv(dir) 2, sphere(uv) 3, hemisphere pdf, sampled dir 3 + pdf.
+static int cmd_guide(const char* in_path, const char* out_path)
+{
+    std::vector<char> buf = read_file(in_path);
+    const int n = *reinterpret_cast<const int32_t*>(buf.data());
+    const float* leaf = reinterpret_cast<const float*>(buf.data() + 4);
+    constexpr int LEAF = Octahedron::resolution2_;
+    constexpr int ALL = Octahedron::totalPixelCountWithPad_;
+    const float* rec = leaf + LEAF * 4;
+    Octahedron* probe = new Octahedron();
+    for (int i = 0; i < LEAF; ++i)
+        probe->data_[i] = float4{leaf[4 * i], leaf[4 * i + 1], leaf[4 * i + 2], leaf[4 * i + 3]};
+    probe->GenerateMipmaps();
+    std::vector<float> out(ALL * 4 + (size_t)n * 14);
+    for (int i = 0; i < ALL; ++i)
+    {
+        out[4 * i] = probe->data_[i].x;
+        out[4 * i + 1] = probe->data_[i].y;
+        out[4 * i + 2] = probe->data_[i].z;
+        out[4 * i + 3] = probe->data_[i].w;
+    }
+    for (int i = 0; i < n; ++i)
+    {
+        const float* r = rec + (size_t)i * 16;
+        const float3 dir{r[0], r[1], r[2]}, nrm{r[3], r[4], r[5]}, q{r[6], r[7], r[8]}, pos{r[9], r[10], r[11]};
+        const float2 uv{r[12], r[13]};
+        uint64_t seed;
+        memcpy(&seed, r + 14, 8);
+        float* o = &out[ALL * 4 + (size_t)i * 14];
+        const int4 key = pg::GetVoxelGrid(pos, dir);
+        o[0] = (float)key.w;
+        o[1] = (float)key.x;
+        o[2] = (float)key.y;
+        o[3] = (float)key.z;
+        const float2 uvd = pg::SphereToUV(dir);
+        o[4] = uvd.x;
+        o[5] = uvd.y;
+        const float3 s = pg::UVtoSphere(uv);
+        o[6] = s.x;
+        o[7] = s.y;
+        o[8] = s.z;
+        o[9] = probe->OctahedronHemispherePDF(dir, nrm, q);
+        curandState st = ar_pcg_init(seed, (uint64_t)i, 0);
+        const Sample smp = probe->SampleOctahedronHemisphere(&st, nrm, q);
+        o[10] = smp.direction_.x;
+        o[11] = smp.direction_.y;
+        o[12] = smp.direction_.z;
+        o[13] = smp.pdf_;
+    }
+    delete probe;
+    write_file(out_path, out.data(), out.size() * 4);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 2) die("usage: ref_cpu kat | lut <lattice> <out> | trace|brute <tris> <rays> <out> | render <scene> <params> <out>");
@@ -444,6 +503,7 @@ int main(int argc, char** argv)
     if (cmd == "lut" && argc == 4) return cmd_lut(argv[2], argv[3]);
     if ((cmd == "trace" || cmd == "brute") && argc == 5) return cmd_trace(argv[2], argv[3], argv[4], cmd == "brute");
     if (cmd == "render" && argc == 5) return cmd_render(argv[2], argv[3], argv[4]);
+    if (cmd == "guide" && argc == 4) return cmd_guide(argv[2], argv[3]);
     die("bad arguments");
     return 2;
 }

@@ -118,6 +118,16 @@ def trace(tris: np.ndarray, rays: np.ndarray, brute: bool = False, threads=None)
     return np.frombuffer(raw[: 4 * n], np.int32).copy(), np.frombuffer(raw[4 * n:], np.float32).copy(), stats
 
 
+def guide_eval(payload: bytes, n: int) -> np.ndarray:
+    """The reference's probe math on one probe (see ref_driver.cu cmd_guide)."""
+    exe = ensure_built()
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "in.bin").write_bytes(np.int32(n).tobytes() + payload)
+        subprocess.run([str(exe), "guide", str(td / "in.bin"), str(td / "out.bin")], check=True, capture_output=True)
+        return np.frombuffer((td / "out.bin").read_bytes(), np.float32).copy()
+
+
 def kat() -> dict:
     exe = ensure_built()
     r = subprocess.run([str(exe), "kat"], capture_output=True, text=True, check=True)

@@ -72,6 +72,15 @@ def main() -> None:
     bids, bt, _ = rr.trace(tris, rays, brute=True)
     assert np.array_equal(ids, bids) and np.array_equal(t.view(np.uint32), bt.view(np.uint32))
     np.savez(HERE / "trace_small.npz", tris=tris, rays=rays, ids=ids, t=t)
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("tgh", HERE.parent / "test_guide_host.py")
+    tgh = importlib.util.module_from_spec(spec)
+    sys.path.insert(0, str(HERE.parent))
+    spec.loader.exec_module(tgh)
+    n = 512
+    payload = tgh.make_payload(n, seed=4)
+    np.savez(HERE / "guide_probe.npz", n=n, payload=np.frombuffer(payload, np.uint8),
+             ref_out=rr.guide_eval(payload, n))
     for name, (scene, w, h, spp, depth) in RENDERS.items():
         objs, mesh, cam = scene_by_name(scene)
         mean, per, _ = rr.render(objs, (w, h), cam["origin"], cam["direction"], spp, fov=cam["fov"],
