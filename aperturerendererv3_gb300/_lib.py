@@ -35,7 +35,8 @@ F3 = C.c_float * 3
 class ArMaterial(C.Structure):
     _fields_ = [("shading", C.c_int32), ("albedo", F3), ("emissive", F3),
                 ("roughness", C.c_float), ("metallic", C.c_float), ("specular", C.c_float),
-                ("ior", C.c_float), ("sigma_a", C.c_float), ("abbe", C.c_float), ("tilt", C.c_float)]
+                ("ior", C.c_float), ("sigma_a", C.c_float), ("abbe", C.c_float), ("tilt", C.c_float),
+                ("albedo_texture", C.c_int32)]
 
 
 class ArObject(C.Structure):
@@ -72,6 +73,7 @@ EXPORTED = [
     "ar_last_render_profile", "ar_render_noalloc", "ar_guide_reset", "ar_guide_stats",
     "ar_get_error_word", "ar_clear_error_word", "ar_last_error", "ar_host_rgb_encode", "ar_host_lambda_encode",
     "ar_host_sample_lambda", "ar_host_trace_closest", "ar_host_guide_eval", "ar_abi_version",
+    "ar_scene_set_textures", "ar_scene_set_mesh_uv", "ar_scene_update_texels", "ar_scene_texel_count", "ar_adjoint",
 ]
 
 _lib = None
@@ -119,6 +121,11 @@ def load() -> C.CDLL:
         "ar_host_trace_closest": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, vp, P(C.c_int64)]),
         "ar_host_guide_eval": (C.c_int, [vp, C.c_int, vp]),
         "ar_abi_version": (C.c_int, []),
+        "ar_scene_set_textures": (C.c_int, [vp, vp, vp, C.c_int]),
+        "ar_scene_set_mesh_uv": (C.c_int, [vp, vp, C.c_int]),
+        "ar_scene_update_texels": (C.c_int, [vp, vp, C.c_int64, C.c_int, vp]),
+        "ar_scene_texel_count": (C.c_int, [vp, P(C.c_int64)]),
+        "ar_adjoint": (C.c_int, [vp, P(ArRenderParams), vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -12,6 +12,9 @@
                         GGX floor and metal back wall.
   random_triangles()    n triangles, centroids U[0,1]^3, vertices offset by
                         N(0, 0.005^2) per axis: the 1M-triangle BVH stress scene.
+  textured_cornell()    the triangle Cornell box with a 512^2 albedo texture on
+                        every wall and box (U[0.2, 0.8] from a seed): the
+                        differentiable-rendering workload.
   terrain_scene()       2048^2 fBm heightfield (8 octaves, amplitude 0.2), 64
                         emissive spheres, a distant sun sphere, GGX materials
                         with roughness U[0.05, 0.6].
@@ -77,6 +80,70 @@ def cornell_triangles() -> list[SceneObject]:
     objs.append(SceneObject((0.0, 0.5 - 0.005, 0.0), (0.125, 0.005, 0.125), Material.CreateLight((17.0, 12.0, 4.0)),
                             (0.0, 0.0, 0.0), OBJECT_CUBE))
     return objs
+
+
+def _quad_uv(a, b, c, d):
+    """Two triangles (a, b, c), (a, c, d) and their corner uvs (a, b, c, d) -> (0,0) (1,0) (1,1) (0,1)."""
+    tris = [a + b + c, a + c + d]
+    uvs = [(0.0, 0.0, 1.0, 0.0, 1.0, 1.0), (0.0, 0.0, 1.0, 1.0, 0.0, 1.0)]
+    return tris, uvs
+
+
+def _box_quads(center, half, rot_y_deg):
+    cy, sy = math.cos(math.radians(rot_y_deg)), math.sin(math.radians(rot_y_deg))
+
+    def p(x, y, z):
+        x, y, z = x * half[0], y * half[1], z * half[2]
+        return (float(np.float32(center[0] + cy * x + sy * z)), float(np.float32(center[1] + y)),
+                float(np.float32(center[2] - sy * x + cy * z)))
+
+    c = {(i, j, k): p(i, j, k) for i in (-1, 1) for j in (-1, 1) for k in (-1, 1)}
+    faces = [((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1)),
+             ((-1, -1, 1), (-1, 1, 1), (1, 1, 1), (1, -1, 1)),
+             ((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1)),
+             ((1, -1, -1), (1, -1, 1), (1, 1, 1), (1, 1, -1)),
+             ((-1, -1, -1), (-1, -1, 1), (1, -1, 1), (1, -1, -1)),
+             ((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1))]
+    return [(c[f[0]], c[f[1]], c[f[2]], c[f[3]]) for f in faces]
+
+
+def cornell_textures(res: int = 512, seed: int = 11, n: int = 8) -> np.ndarray:
+    """n albedo textures of res x res RGB texels, U[0.2, 0.8] from `seed`: (n, res, res, 3) float32."""
+    rng = np.random.default_rng(seed)
+    return rng.uniform(0.2, 0.8, (n, res, res, 3)).astype(np.float32)
+
+
+def textured_cornell(textures: np.ndarray):
+    """The triangle Cornell box with every wall and both boxes carrying an albedo
+    texture (the differentiable-rendering workload): 6 walls + 2 boxes = 8
+    textures, one per surface group; each wall quad and each box face spans its
+    texture's full [0,1]^2.  Returns (objects, mesh, textures): the ceiling light
+    (a thin box) is the only object, everything textured is the mesh."""
+    h = 0.5
+    walls = [((-h, -h, -h), (h, -h, -h), (h, -h, h), (-h, -h, h)),      # floor
+             ((-h, h, -h), (-h, h, h), (h, h, h), (h, h, -h)),          # ceiling
+             ((-h, -h, -h), (-h, h, -h), (h, h, -h), (h, -h, -h)),      # back
+             ((-h, -h, h), (h, -h, h), (h, h, h), (-h, h, h)),          # front
+             ((-h, -h, -h), (-h, -h, h), (-h, h, h), (-h, h, -h)),      # left
+             ((h, -h, -h), (h, h, -h), (h, h, h), (h, -h, h))]          # right
+    groups = [[w] for w in walls]
+    groups.append(_box_quads((0.18, -0.35, 0.12), (0.15, 0.15, 0.15), -18.0))
+    groups.append(_box_quads((-0.17, -0.2, -0.15), (0.15, 0.3, 0.15), 18.0))
+    assert len(textures) == len(groups)
+    tris, uvs, mids = [], [], []
+    for g, quads in enumerate(groups):
+        for q in quads:
+            t, u = _quad_uv(*q)
+            tris += t
+            uvs += u
+            mids += [g, g]
+    mats = [Material.CreateDiffuseTextured(g) for g in range(len(groups))]
+    v = np.asarray(tris, np.float32).reshape(-1, 3)
+    mesh = TriangleMesh(v, np.arange(len(v), dtype=np.uint32).reshape(-1, 3), np.asarray(mids, np.int32), mats,
+                        uv=np.asarray(uvs, np.float32))
+    light = SceneObject((0.0, 0.5 - 0.005, 0.0), (0.125, 0.005, 0.125), Material.CreateLight((17.0, 12.0, 4.0)),
+                        (0.0, 0.0, 0.0), OBJECT_CUBE)
+    return [light], mesh, [t for t in textures]
 
 
 REFERENCE_CORNELL_CAMERA = dict(origin=(0.0, 0.0, 1.1), direction=(0.0, 0.0, -1.0), fov=60.0)

@@ -99,6 +99,12 @@ struct DevScene
     // shadow visits, shadow tests, extend rays, shadow rays
     unsigned long long* stats;
     DevGuide guide;
+    // albedo textures: RGB float32 texels, per texture {texel offset, width,
+    // height, 0}, per primitive id 6 uv floats (null when no texture is set)
+    const float* texels;
+    const int4* tex_info;
+    const float* prim_uv;
+    int tex_count;
 };
 
 // stage ids for the per-stage profile
@@ -143,6 +149,10 @@ struct PathState
     float4* pg_dir;     // xyz sampled direction, w = collected radiance
     float4* pg_loc;     // xyz vertex position, w = radiance mask
     float4* pg_vdir;    // xyz reflected direction (voxel face key)
+    // replay adjoint only: the path's total radiance (first pass) and
+    // d(loss)/d(radiance)
+    float* adj_total;
+    float* adj_delta;
 };
 
 struct ShadowQueue
@@ -163,7 +173,9 @@ struct RenderLaunch
     uint64_t seed;
     int first_frame;
     int profile;
-    int guide;  // 0 none, 1 voxel probes
+    int guide;    // 0 none, 1 voxel probes
+    int adjoint;  // 1: replay pass of ar_adjoint (gradient scatter, no output)
+    float* grad;  // replay pass: float32 texel gradients
 };
 
 struct Ctx
@@ -199,6 +211,20 @@ struct Ctx
     float* d_d65 = nullptr;
     unsigned int* d_err = nullptr;
     int* d_counters = nullptr;
+    // albedo textures
+    std::vector<float> tex_texels;
+    std::vector<int> tex_sizes;          // width, height per texture
+    std::vector<float> mesh_uv;          // 6 per mesh triangle
+    float* d_texels = nullptr;
+    int4* d_tex_info = nullptr;
+    float* d_prim_uv = nullptr;
+    long long texel_floats = 0;          // of the built scene
+    int tex_count = 0;
+    // replay adjoint
+    float* d_grad32 = nullptr;
+    long long grad32_n = 0;
+    float* d_adj = nullptr;              // 2 floats per wave path
+    int adj_capacity = 0;
     // wavefront buffers
     PathState ps{};
     ShadowQueue sq{};
@@ -259,4 +285,9 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
                                float* per_sample_out, long long* launches);
 cudaError_t launch_accumulate(Ctx& c, const RenderLaunch& rl, long long first_path, int n_paths, double* accum,
                               long long* launches);
+// replay adjoint (adjoint.cu): per-path seed between the two passes, and the
+// float32 -> float64 gradient fold after each wave
+cudaError_t launch_adjoint_seed(Ctx& c, const RenderLaunch& rl, int n_paths, const float* dl_dxyz,
+                                long long* launches);
+cudaError_t launch_grad_fold(Ctx& c, double* grad64, long long n, long long* launches);
 } // namespace ar

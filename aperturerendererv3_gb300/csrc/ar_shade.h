@@ -45,6 +45,7 @@ struct Material
     V3 albedo, emissive;
     float specular, metallic, roughness, ior, sigma_a, abbe, tilt;
     SpecColor albedo_c, emissive_c;  // prepared RGB->basis colours
+    int albedo_tex;                  // albedo texture index, -1 = none
 };
 
 struct Hit

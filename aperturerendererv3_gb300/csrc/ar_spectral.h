@@ -223,6 +223,57 @@ AR_HD float interact_rgb(const Basis& lam, V3 rgb, const Fetch& fetch)
     return interact(prepare_color(rgb, fetch), lam);
 }
 
+// Gradient of interact_rgb(lam, rgb) with respect to rgb: the trilinear
+// interpolation differentiated inside its cell, zero where a clamp is active
+// (the lattice edges, the [0, 1] clamp of the interaction).  When max(rgb) > 1
+// the colour is interacted as max(rgb) * q(rgb / max(rgb)), and the chain rule
+// runs through both factors.
+template <typename Fetch>
+AR_HD V3 interact_rgb_grad(const Basis& lam, V3 rgb, const Fetch& fetch)
+{
+    const float lum = max3(rgb);
+    const bool scaled = lum > 1.0f;
+    const V3 u = scaled ? rgb / lum : rgb;
+    const float RES = static_cast<float>(AR_LUT_RES);
+    const float maxC = RES - 1.0f;
+    const float g[3] = {u.x * RES - 0.5f, u.y * RES - 0.5f, u.z * RES - 0.5f};
+    int lo[3], hi[3];
+    float t[3], dg[3];
+    for (int a = 0; a < 3; ++a)
+    {
+        const float gc = fminf(fmaxf(g[a], 0.0f), maxC);
+        linear_coord(gc, AR_LUT_RES, lo[a], hi[a], t[a]);
+        dg[a] = (g[a] > 0.0f && g[a] < maxC && lo[a] != hi[a]) ? RES : 0.0f;
+    }
+    float q = 0.0f, dq[3] = {0.0f, 0.0f, 0.0f};
+    for (int c = 0; c < 8; ++c)
+    {
+        const int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
+        float v[4];
+        fetch(lut_voxel(bx ? hi[0] : lo[0], by ? hi[1] : lo[1], bz ? hi[2] : lo[2]), v);
+        float sc = 0.0f;
+        for (int i = 0; i < AR_BASIS; ++i) sc += v[i] * lam.k[i];
+        const float wx = bx ? t[0] : 1.0f - t[0];
+        const float wy = by ? t[1] : 1.0f - t[1];
+        const float wz = bz ? t[2] : 1.0f - t[2];
+        q += wx * wy * wz * sc;
+        dq[0] += (bx ? 1.0f : -1.0f) * wy * wz * sc;
+        dq[1] += (by ? 1.0f : -1.0f) * wx * wz * sc;
+        dq[2] += (bz ? 1.0f : -1.0f) * wx * wy * sc;
+    }
+    const float on = (q > 0.0f && q < 1.0f) ? 1.0f : 0.0f;
+    V3 gq = v3(dq[0] * dg[0] * on, dq[1] * dg[1] * on, dq[2] * dg[2] * on);
+    if (!scaled) return gq;
+    // f = lum * clamp(q(rgb / lum)), lum = rgb[m]
+    const float qc = fminf(fmaxf(q, 0.0f), 1.0f);
+    const float extra = qc - (gq.x * u.x + gq.y * u.y + gq.z * u.z);
+    const int m = (rgb.x >= rgb.y && rgb.x >= rgb.z) ? 0 : (rgb.y >= rgb.z ? 1 : 2);
+    if (m == 0) gq.x += extra;
+    else if (m == 1) gq.y += extra;
+    else gq.z += extra;
+    return gq;
+}
+
 // ---------------------------------------------------------------- sampling
 AR_HD float ndtrif(float u, float (*erfc_fn)(float) = nullptr)
 {

@@ -46,6 +46,10 @@ DevScene dev_scene(const Ctx& c)
     s.camera_inside = c.camera_inside;
     s.stats = (c.profile & 2) ? c.d_stats : nullptr;
     s.guide = c.guide;
+    s.texels = c.d_texels;
+    s.tex_info = c.d_tex_info;
+    s.prim_uv = c.d_prim_uv;
+    s.tex_count = c.tex_count;
     return s;
 }
 } // namespace ar
@@ -89,6 +93,11 @@ void free_scene(Ctx& c)
     free_dev(c.d_prim_light);
     free_dev(c.d_prim_slot);
     free_dev(c.d_lights);
+    free_dev(c.d_texels);
+    free_dev(c.d_tex_info);
+    free_dev(c.d_prim_uv);
+    c.tex_count = 0;
+    c.texel_floats = 0;
     c.built = false;
 }
 
@@ -279,6 +288,7 @@ Material make_material(const ar_material& m)
             r.emissive = emi;
             break;
     }
+    r.albedo_tex = (m.albedo_texture > 0 && m.shading != AR_SHADING_LIGHT) ? m.albedo_texture - 1 : -1;
     return r;
 }
 
@@ -338,11 +348,62 @@ bool cuda_device_ok(int device, std::string* why)
     }
     return true;
 }
+// Validates the render parameters and fills the launch description; resets
+// the per-render profile state and decides whether the camera starts inside
+// an object (intersection::Overlap, core/render/intersection.cuh:312-327).
+ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch& rl)
+{
+    Ctx& c = ctx->c;
+    if (!c.built) return fail(ctx, AR_ERR_STATE, "render before ar_scene_build");
+    if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth <= 0 || prm->max_depth > 0xffff)
+        return fail(ctx, AR_ERR_INVALID, "render: bad resolution, spp or depth");
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    rl = RenderLaunch{};
+    rl.width = prm->width;
+    rl.height = prm->height;
+    rl.spp = prm->spp;
+    rl.max_depth = prm->max_depth;
+    for (int k = 0; k < 3; ++k)
+    {
+        rl.cam_o[k] = prm->cam_origin[k];
+        rl.cam_d[k] = prm->cam_dir[k];
+    }
+    rl.fov_deg = prm->fov_deg;
+    rl.use_nee = prm->use_nee;
+    rl.seed = prm->seed;
+    rl.first_frame = prm->first_frame;
+    rl.profile = prm->profile;
+    c.profile = prm->profile & 3;
+    c.stage_events.clear();
+    for (int k = 0; k < ST_COUNT; ++k)
+    {
+        c.stage_ms[k] = 0.0f;
+        c.stage_launches[k] = 0;
+    }
+    if (c.profile)
+    {
+        if (!c.d_stats) AR_CUDA(ctx, cudaMalloc((void**)&c.d_stats, 8 * sizeof(unsigned long long)));
+        AR_CUDA(ctx, cudaMemsetAsync(c.d_stats, 0, 8 * sizeof(unsigned long long), c.stream));
+    }
+    // camera inside a medium (intersection::Overlap, core/render/intersection.cuh:312-327)
+    c.camera_inside = 0;
+    {
+        const V3 co = v3(rl.cam_o[0], rl.cam_o[1], rl.cam_o[2]);
+        for (size_t i = 0; i < c.objects.size(); ++i)
+            if (c.object_type[i] != AR_OBJECT_TRIANGLE && overlap_object(co, c.objects[i]))
+            {
+                c.camera_inside = 1;
+                break;
+            }
+    }
+    return AR_OK;
+}
+
 } // namespace
 
 extern "C" {
 
-int ar_abi_version(void) { return 1; }
+int ar_abi_version(void) { return 2; }
 
 ar_status ar_create(ar_ctx** out, int device)
 {
@@ -398,6 +459,8 @@ ar_status ar_destroy(ar_ctx* ctx)
     free_dev(c.d_counters);
     free_dev(c.d_accum);
     free_dev(c.d_stats);
+    free_dev(c.d_grad32);
+    free_dev(c.d_adj);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete ctx;
     return AR_OK;
@@ -473,6 +536,59 @@ ar_status ar_scene_set_mesh(ar_ctx* ctx, const float* v, int nv, const uint32_t*
     return AR_OK;
 }
 
+ar_status ar_scene_set_textures(ar_ctx* ctx, const float* texels, const int32_t* sizes, int n)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    if (n < 0 || (n > 0 && (!texels || !sizes))) return fail(ctx, AR_ERR_INVALID, "textures: bad pointer or count");
+    Ctx& c = ctx->c;
+    long long total = 0;
+    for (int i = 0; i < n; ++i)
+    {
+        const int w = sizes[2 * i], h = sizes[2 * i + 1];
+        if (w <= 0 || h <= 0 || (long long)w * h > (1ll << 28)) return fail(ctx, AR_ERR_INVALID, "textures: bad size");
+        total += (long long)w * h;
+    }
+    if (total > (1ll << 30)) return fail(ctx, AR_ERR_INVALID, "textures: more than 2^30 texels");
+    c.tex_sizes.assign(sizes, sizes + 2 * (size_t)n);
+    c.tex_texels.assign(texels, texels + 3 * (size_t)total);
+    c.built = false;
+    return AR_OK;
+}
+
+ar_status ar_scene_set_mesh_uv(ar_ctx* ctx, const float* uv, int nt)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    if (nt < 0 || (nt > 0 && !uv)) return fail(ctx, AR_ERR_INVALID, "mesh uv: bad pointer or count");
+    Ctx& c = ctx->c;
+    c.mesh_uv.assign(uv, uv + 6 * (size_t)nt);
+    c.built = false;
+    return AR_OK;
+}
+
+ar_status ar_scene_texel_count(ar_ctx* ctx, int64_t* n_floats)
+{
+    if (!ctx || !n_floats) return AR_ERR_INVALID;
+    if (!ctx->c.built) return fail(ctx, AR_ERR_STATE, "texel count before ar_scene_build");
+    *n_floats = ctx->c.texel_floats;
+    return AR_OK;
+}
+
+ar_status ar_scene_update_texels(ar_ctx* ctx, const float* texels, int64_t n_floats, int is_device, void* stream)
+{
+    if (!ctx || (n_floats > 0 && !texels)) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (!c.built) return fail(ctx, AR_ERR_STATE, "texel update before ar_scene_build");
+    if (n_floats != c.texel_floats) return fail(ctx, AR_ERR_INVALID, "texel update: count differs from the scene's");
+    if (n_floats == 0) return AR_OK;
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    AR_CUDA(ctx, cudaMemcpyAsync(c.d_texels, texels, (size_t)n_floats * sizeof(float),
+                                 is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    // later work on the context's stream sees the new texels
+    if (s != c.stream) AR_CUDA(ctx, cudaStreamSynchronize(s));
+    return AR_OK;
+}
+
 ar_status ar_scene_build(ar_ctx* ctx)
 {
     if (!ctx) return AR_ERR_INVALID;
@@ -487,6 +603,11 @@ ar_status ar_scene_build(ar_ctx* ctx)
         if (c.object_material[i] < 0 || c.object_material[i] >= nmat) return fail(ctx, AR_ERR_INVALID, "object material index out of range");
     for (int i = 0; i < nmesh; ++i)
         if (c.mesh_material[i] < 0 || c.mesh_material[i] >= nmat) return fail(ctx, AR_ERR_INVALID, "mesh material index out of range");
+    const int ntex = (int)(c.tex_sizes.size() / 2);
+    for (int i = 0; i < nmat; ++i)
+        if (c.materials[i].albedo_tex >= ntex) return fail(ctx, AR_ERR_INVALID, "material texture index out of range");
+    if (!c.mesh_uv.empty() && c.mesh_uv.size() != 6 * (size_t)nmesh)
+        return fail(ctx, AR_ERR_INVALID, "mesh uv count differs from the mesh's triangle count");
 
     // primitives for the BVH
     std::vector<arbvh::PrimInput> prims((size_t)nprim);
@@ -598,6 +719,27 @@ ar_status ar_scene_build(ar_ctx* ctx)
             return cuda_fail(ctx, e, "spectral LUT build");
         }
     }
+    // albedo textures: texels, per-texture {offset, width, height}, per-primitive uv
+    if (ntex > 0)
+    {
+        std::vector<int4> info((size_t)ntex);
+        long long off = 0;
+        for (int i = 0; i < ntex; ++i)
+        {
+            info[i] = make_int4((int)off, c.tex_sizes[2 * i], c.tex_sizes[2 * i + 1], 0);
+            off += (long long)c.tex_sizes[2 * i] * c.tex_sizes[2 * i + 1];
+        }
+        AR_CUDA(ctx, alloc_dev(c.d_texels, c.tex_texels.size()));
+        AR_CUDA(ctx, cudaMemcpy(c.d_texels, c.tex_texels.data(), c.tex_texels.size() * sizeof(float), cudaMemcpyHostToDevice));
+        AR_CUDA(ctx, alloc_dev(c.d_tex_info, info.size()));
+        AR_CUDA(ctx, cudaMemcpy(c.d_tex_info, info.data(), info.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        std::vector<float> uv((size_t)nprim * 6, 0.0f);
+        if (!c.mesh_uv.empty()) std::memcpy(&uv[(size_t)nobj * 6], c.mesh_uv.data(), c.mesh_uv.size() * sizeof(float));
+        AR_CUDA(ctx, alloc_dev(c.d_prim_uv, uv.size()));
+        AR_CUDA(ctx, cudaMemcpy(c.d_prim_uv, uv.data(), uv.size() * sizeof(float), cudaMemcpyHostToDevice));
+        c.tex_count = ntex;
+        c.texel_floats = (long long)c.tex_texels.size();
+    }
     std::vector<Material> mats(c.materials);
     AR_CUDA(ctx, alloc_dev(c.d_materials, std::max<size_t>(mats.size(), 1)));
     if (!mats.empty())
@@ -628,48 +770,9 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     (void)stream;
     if (!ctx || !prm || !out_xyz) return AR_ERR_INVALID;
     Ctx& c = ctx->c;
-    if (!c.built) return fail(ctx, AR_ERR_STATE, "render before ar_scene_build");
-    if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth <= 0 || prm->max_depth > 0xffff)
-        return fail(ctx, AR_ERR_INVALID, "render: bad resolution, spp or depth");
-    AR_CUDA(ctx, cudaSetDevice(c.device));
     RenderLaunch rl;
-    rl.width = prm->width;
-    rl.height = prm->height;
-    rl.spp = prm->spp;
-    rl.max_depth = prm->max_depth;
-    for (int k = 0; k < 3; ++k)
-    {
-        rl.cam_o[k] = prm->cam_origin[k];
-        rl.cam_d[k] = prm->cam_dir[k];
-    }
-    rl.fov_deg = prm->fov_deg;
-    rl.use_nee = prm->use_nee;
-    rl.seed = prm->seed;
-    rl.first_frame = prm->first_frame;
-    rl.profile = prm->profile;
-    c.profile = prm->profile & 3;
-    c.stage_events.clear();
-    for (int k = 0; k < ST_COUNT; ++k)
-    {
-        c.stage_ms[k] = 0.0f;
-        c.stage_launches[k] = 0;
-    }
-    if (c.profile)
-    {
-        if (!c.d_stats) AR_CUDA(ctx, cudaMalloc((void**)&c.d_stats, 8 * sizeof(unsigned long long)));
-        AR_CUDA(ctx, cudaMemsetAsync(c.d_stats, 0, 8 * sizeof(unsigned long long), c.stream));
-    }
-    // camera inside a medium (intersection::Overlap, core/render/intersection.cuh:312-327)
-    c.camera_inside = 0;
-    {
-        const V3 co = v3(rl.cam_o[0], rl.cam_o[1], rl.cam_o[2]);
-        for (size_t i = 0; i < c.objects.size(); ++i)
-            if (c.object_type[i] != AR_OBJECT_TRIANGLE && overlap_object(co, c.objects[i]))
-            {
-                c.camera_inside = 1;
-                break;
-            }
-    }
+    ar_status st = prepare_launch(ctx, prm, rl);
+    if (st != AR_OK) return st;
     const long long npix = (long long)rl.width * rl.height;
     const long long total = npix * rl.spp;
     rl.guide = prm->guide;
@@ -678,7 +781,7 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     if ((long long)cap > total) cap = (int)total;
     // guided frames learn from the previous frame: waves never straddle frames
     if (rl.guide && (long long)cap > npix) cap = (int)npix;
-    ar_status st = ensure_waves(ctx, cap);
+    st = ensure_waves(ctx, cap);
     if (st != AR_OK) return st;
     if (rl.guide)
     {
@@ -744,6 +847,74 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     for (auto& s : sums) s *= inv;
     if (out_is_device) AR_CUDA(ctx, cudaMemcpy(out_xyz, sums.data(), sums.size() * sizeof(double), cudaMemcpyHostToDevice));
     else std::memcpy(out_xyz, sums.data(), sums.size() * sizeof(double));
+    unsigned int word = 0;
+    AR_CUDA(ctx, cudaMemcpy(&word, c.d_err, sizeof(word), cudaMemcpyDeviceToHost));
+    if (word) return fail(ctx, AR_ERR_DEVICE, "device error word set: " + std::to_string(word));
+    return AR_OK;
+}
+
+ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* prm, const float* dl_dxyz, double* grad_texels, void* stream)
+{
+    if (!ctx || !prm || !dl_dxyz || !grad_texels) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (prm->guide != AR_GUIDE_NONE) return fail(ctx, AR_ERR_INVALID, "adjoint: guided rendering is not differentiated");
+    if (prm->profile) return fail(ctx, AR_ERR_INVALID, "adjoint: profiling is not supported");
+    RenderLaunch rl;
+    ar_status st = prepare_launch(ctx, prm, rl);
+    if (st != AR_OK) return st;
+    if (c.texel_floats == 0) return fail(ctx, AR_ERR_STATE, "adjoint: the scene has no textures");
+    // the caller's buffers are ordered on its stream: finish that work first
+    if (stream) AR_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    const long long npix = (long long)rl.width * rl.height;
+    const long long total = npix * rl.spp;
+    int cap = prm->wave_paths > 0 ? prm->wave_paths : (1 << 21);
+    if ((long long)cap > total) cap = (int)total;
+    st = ensure_waves(ctx, cap);
+    if (st != AR_OK) return st;
+    if (c.adj_capacity < c.ps.capacity)
+    {
+        free_dev(c.d_adj);
+        AR_CUDA(ctx, alloc_dev(c.d_adj, 2 * (size_t)c.ps.capacity));
+        c.adj_capacity = c.ps.capacity;
+    }
+    c.ps.adj_total = c.d_adj;
+    c.ps.adj_delta = c.d_adj + c.ps.capacity;
+    if (c.grad32_n < c.texel_floats)
+    {
+        free_dev(c.d_grad32);
+        AR_CUDA(ctx, alloc_dev(c.d_grad32, (size_t)c.texel_floats));
+        AR_CUDA(ctx, cudaMemset(c.d_grad32, 0, (size_t)c.texel_floats * sizeof(float)));
+        c.grad32_n = c.texel_floats;
+    }
+    AR_CUDA(ctx, cudaMemsetAsync(grad_texels, 0, (size_t)c.texel_floats * sizeof(double), c.stream));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c.stream);
+    long long launches = 0;
+    cudaError_t e = cudaSuccess;
+    RenderLaunch replay = rl;
+    replay.adjoint = 1;
+    replay.grad = c.d_grad32;
+    for (long long first = 0; first < total && e == cudaSuccess;)
+    {
+        const int n = (int)std::min<long long>(cap, total - first);
+        e = launch_render_wave(c, rl, first, n, nullptr, &launches);                           // radiance of each path
+        if (e == cudaSuccess) e = launch_adjoint_seed(c, rl, n, dl_dxyz, &launches);           // its adjoint
+        if (e == cudaSuccess) e = launch_render_wave(c, replay, first, n, nullptr, &launches);  // replay + scatter
+        if (e == cudaSuccess) e = launch_grad_fold(c, grad_texels, c.texel_floats, &launches);
+        first += n;
+    }
+    cudaEventRecord(e1, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) cudaEventElapsedTime(&c.last_render_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c.last_launches = launches;
+    c.ps.adj_total = nullptr;
+    c.ps.adj_delta = nullptr;
+    c.profile = 0;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "adjoint");
     unsigned int word = 0;
     AR_CUDA(ctx, cudaMemcpy(&word, c.d_err, sizeof(word), cudaMemcpyDeviceToHost));
     if (word) return fail(ctx, AR_ERR_DEVICE, "device error word set: " + std::to_string(word));

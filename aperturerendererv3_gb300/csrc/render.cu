@@ -115,6 +115,38 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
     }
 }
 
+// Albedo texel at a triangle hit: the mesh uv interpolated with the
+// barycentric weights of pos, nearest texel, clamped to the edge.  Returns the
+// texel index (in RGB units) or -1 when the primitive is not a triangle.
+__device__ __forceinline__ int albedo_texel(const DevScene& sc, int tex, int slot, int prim, V3 pos)
+{
+    const float4 a = __ldg(&sc.trav.slots[3 * (size_t)slot + 0]);
+    if ((__float_as_uint(a.w) >> AR_PRIM_KIND_SHIFT) != AR_PRIM_KIND_TRI) return -1;
+    const float4 b = __ldg(&sc.trav.slots[3 * (size_t)slot + 1]);
+    const float4 c = __ldg(&sc.trav.slots[3 * (size_t)slot + 2]);
+    const V3 v0 = v3(a.x, a.y, a.z);
+    const V3 e1 = v3(b.x, b.y, b.z) - v0, e2 = v3(c.x, c.y, c.z) - v0, d = pos - v0;
+    const float d00 = dot(e1, e1), d01 = dot(e1, e2), d11 = dot(e2, e2);
+    const float d20 = dot(d, e1), d21 = dot(d, e2);
+    const float den = d00 * d11 - d01 * d01;
+    float b1 = 0.0f, b2 = 0.0f;
+    if (den > 0.0f)
+    {
+        b1 = (d11 * d20 - d01 * d21) / den;
+        b2 = (d00 * d21 - d01 * d20) / den;
+    }
+    const float b0 = 1.0f - b1 - b2;
+    const float* uv = sc.prim_uv + 6 * (size_t)prim;
+    float u = b0 * __ldg(uv + 0) + b1 * __ldg(uv + 2) + b2 * __ldg(uv + 4);
+    float v = b0 * __ldg(uv + 1) + b1 * __ldg(uv + 3) + b2 * __ldg(uv + 5);
+    if (!(u == u)) u = 0.0f;
+    if (!(v == v)) v = 0.0f;
+    const int4 ti = __ldg(&sc.tex_info[tex]);
+    const int x = min(max((int)floorf(fminf(fmaxf(u, 0.0f), 1.0f) * (float)ti.y), 0), ti.y - 1);
+    const int y = min(max((int)floorf(fminf(fmaxf(v, 0.0f), 1.0f) * (float)ti.z), 0), ti.z - 1);
+    return ti.x + y * ti.y + x;
+}
+
 // ---------------------------------------------------------------- raygen
 struct CamParams
 {
@@ -208,7 +240,8 @@ struct ShadeParams
 {
     int use_nee;
     int max_depth;
-    int frame;  // frame index of the wave (guided rendering: mixture probability)
+    int frame;    // frame index of the wave (guided rendering: mixture probability)
+    float* grad;  // replay adjoint: float32 texel gradients (3 per texel)
 };
 
 // CollectRadiance (core/render/render.cuh:353-432) on the path's collection
@@ -261,7 +294,7 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
     }
 }
 
-template <bool GUIDE>
+template <bool GUIDE, bool ADJ>
 __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
                                                   const int* __restrict__ counter, int* next_queue, int* next_counter,
                                                   int* shadow_counter, ShadeParams prm)
@@ -336,9 +369,20 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                 S.media.inside = false;
                 S.media.vertex = h.local_pos;
             }
+            int texel = -1;
             if (h.hit)
             {
                 mat = sc.materials[sc.prim_material[h.obj]];
+                if (mat.albedo_tex >= 0 && sc.tex_count > 0)
+                {
+                    texel = albedo_texel(sc, mat.albedo_tex, slot, h.obj, h.pos);
+                    if (texel >= 0)
+                    {
+                        const float* tx = sc.texels + 3 * (size_t)texel;
+                        mat.albedo = v3(__ldg(tx), __ldg(tx + 1), __ldg(tx + 2));
+                        mat.albedo_c = prepare_color(mat.albedo, PlainFetch{sc.lut_rgb});
+                    }
+                }
                 S = evaluate_material(lambda, lb, R, mat, rayD, h, media);
             }
             else
@@ -434,6 +478,26 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
             else if (!all_zero(S.emissive))
             {
                 endpointLe = S.emissive;
+            }
+            if constexpr (ADJ)
+            {
+                // replay adjoint: every contribution still to come on this path
+                // (NEE here, emission and NEE further on) carries this vertex's
+                // albedo once; radiance holds the contributions that do not
+                if (texel >= 0 && mat.shading == AR_MAT_DIFFUSE)
+                {
+                    const float rest = ps.adj_total[p] - radiance;
+                    const float dlt = ps.adj_delta[p];
+                    const float alb = interact(mat.albedo_c, lb);
+                    if (rest != 0.0f && dlt != 0.0f && alb > 1.0e-8f)
+                    {
+                        const V3 g = interact_rgb_grad(lb, mat.albedo, PlainFetch{sc.lut_rgb}) * (dlt * rest / alb);
+                        float* gp = prm.grad + 3 * (size_t)texel;
+                        if (g.x != 0.0f) atomicAdd(gp + 0, g.x);
+                        if (g.y != 0.0f) atomicAdd(gp + 1, g.y);
+                        if (g.z != 0.0f) atomicAdd(gp + 2, g.z);
+                    }
+                }
             }
             if constexpr (GUIDE)
             {
@@ -789,6 +853,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
     prm.frame = rl.first_frame + (int)(first_path / ((long long)rl.width * rl.height));
+    prm.grad = rl.grad;
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
@@ -801,17 +866,25 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         {
             StageScope st(c, ST_SHADE);
             if (rl.guide)
-                k_shade<true><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur], c.d_queue[nxt],
-                                                          &cnt[nxt], &cnt[2], prm);
+                k_shade<true, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
+                                                                 c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
+            else if (rl.adjoint)
+                k_shade<false, true><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
+                                                                 c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
             else
-                k_shade<false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur], c.d_queue[nxt],
-                                                           &cnt[nxt], &cnt[2], prm);
+                k_shade<false, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
+                                                                  c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
         }
         {
             StageScope st(c, ST_SHADOW);
             k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[2], c.d_err);
         }
         L += 3;
+    }
+    if (rl.adjoint)
+    {
+        if (launches) *launches += L;
+        return cudaGetLastError();
     }
     {
         StageScope st(c, ST_FINAL);
@@ -845,13 +918,14 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
     prm.frame = rl.first_frame;
+    prm.grad = nullptr;
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
         cudaMemsetAsync(&cnt[nxt], 0, sizeof(int), s);
         cudaMemsetAsync(&cnt[2], 0, sizeof(int), s);
         k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[cur], err);
-        k_shade<false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[cur], wb.queue[nxt], &cnt[nxt],
+        k_shade<false, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[cur], wb.queue[nxt], &cnt[nxt],
                                                    &cnt[2], prm);
         k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[2], err);
     }

@@ -45,6 +45,7 @@ class Material:
     sigma_a: float = 100.0
     abbe: float = 20.0
     tilt: float = 0.0
+    texture: int | None = None   # albedo texture index (SceneRenderer textures); None = albedo
 
     @staticmethod
     def CreateDiffusePureColor(color: Vec3, emissive: Vec3 = (0.0, 0.0, 0.0)) -> "Material":
@@ -73,7 +74,13 @@ class Material:
         m.emissive[:] = self.emissive
         m.roughness, m.metallic, m.specular = self.roughness, self.metallic, self.specular
         m.ior, m.sigma_a, m.abbe, m.tilt = self.ior, self.sigma_a, self.abbe, self.tilt
+        m.albedo_texture = 0 if self.texture is None else int(self.texture) + 1
         return m
+
+    @staticmethod
+    def CreateDiffuseTextured(texture: int, emissive: Vec3 = (0.0, 0.0, 0.0)) -> "Material":
+        """Lambertian surface whose albedo is texture `texture` at the hit's uv."""
+        return Material(SHADING_DIFFUSE, (1.0, 1.0, 1.0), _f3(emissive), texture=int(texture))
 
 
 @dataclass
@@ -99,6 +106,7 @@ class TriangleMesh:
     indices: np.ndarray           # (nt, 3) uint32
     material_ids: np.ndarray      # (nt,) int32 into `materials`
     materials: list
+    uv: np.ndarray | None = None  # (nt, 6) float32: u, v at each corner (textured materials)
 
     def triangle_vertices(self) -> np.ndarray:
         return np.asarray(self.vertices, np.float32)[np.asarray(self.indices, np.int64)].reshape(-1, 9)
@@ -137,7 +145,8 @@ def flatten(objects: Iterable[SceneObject], mesh: TriangleMesh | None = None):
 class SceneRenderer:
     """GPU path tracer for one scene (drop-in for the reference's SceneRenderer)."""
 
-    def __init__(self, sceneObjects: Iterable[SceneObject], device: int = 0, mesh: TriangleMesh | None = None):
+    def __init__(self, sceneObjects: Iterable[SceneObject], device: int = 0, mesh: TriangleMesh | None = None,
+                 textures: Sequence[np.ndarray] | None = None):
         lib = _lib.load()
         self._lib = lib
         ctx = C.c_void_p()
@@ -147,6 +156,8 @@ class SceneRenderer:
         self._ctx = ctx
         self.objects = list(sceneObjects)
         self.mesh = mesh
+        self.textures = list(textures) if textures is not None else []
+        self.device = device
         self.bDirty = True
 
     def close(self) -> None:
@@ -178,6 +189,18 @@ class SceneRenderer:
                                                          ids.ctypes.data))
         else:
             check(self._ctx, self._lib.ar_scene_set_mesh(self._ctx, None, 0, None, 0, None))
+        if self.mesh is not None and self.mesh.uv is not None:
+            uv = np.ascontiguousarray(self.mesh.uv, np.float32).reshape(-1, 6)
+            check(self._ctx, self._lib.ar_scene_set_mesh_uv(self._ctx, uv.ctypes.data, len(uv)))
+        else:
+            check(self._ctx, self._lib.ar_scene_set_mesh_uv(self._ctx, None, 0))
+        if self.textures:
+            flat = np.concatenate([np.ascontiguousarray(t, np.float32).reshape(-1) for t in self.textures])
+            sizes = np.array([[t.shape[1], t.shape[0]] for t in self.textures], np.int32).reshape(-1)
+            check(self._ctx, self._lib.ar_scene_set_textures(self._ctx, flat.ctypes.data, sizes.ctypes.data,
+                                                             len(self.textures)))
+        else:
+            check(self._ctx, self._lib.ar_scene_set_textures(self._ctx, None, None, 0))
         check(self._ctx, self._lib.ar_scene_build(self._ctx))
         self.bDirty = False
 
@@ -229,6 +252,51 @@ class SceneRenderer:
                                    ps.ctypes.data if ps is not None else None, None)
         check(self._ctx, code)
         return (out, ps) if per_sample else out
+
+    # ---- device-side rendering and the replay adjoint (torch tensors) -----
+    def texel_count(self) -> int:
+        """Texel floats of the built scene (3 per texel, all textures)."""
+        self._build()
+        n = C.c_int64()
+        check(self._ctx, self._lib.ar_scene_texel_count(self._ctx, C.byref(n)))
+        return n.value
+
+    def update_texels(self, texels) -> None:
+        """Replaces every texel value (CUDA float32 tensor or host array of texel_count() floats)."""
+        self._build()
+        if hasattr(texels, "data_ptr"):
+            import torch
+            t = texels.detach().to(torch.float32).contiguous()
+            s = torch.cuda.current_stream(t.device).cuda_stream
+            check(self._ctx, self._lib.ar_scene_update_texels(self._ctx, t.data_ptr(), t.numel(), 1, s))
+        else:
+            a = np.ascontiguousarray(texels, np.float32).reshape(-1)
+            check(self._ctx, self._lib.ar_scene_update_texels(self._ctx, a.ctypes.data, a.size, 0, None))
+
+    def render_into(self, out, size, cameraOrigin, cameraDirection, sampleNum: int, **kw) -> None:
+        """Renders into a CUDA float64 tensor out of shape (height, width, 3)."""
+        import torch
+        self._build()
+        p = self.params(size, cameraOrigin, cameraDirection, sampleNum, **kw)
+        assert out.dtype == torch.float64 and out.is_contiguous() and out.numel() == 3 * p.width * p.height
+        s = torch.cuda.current_stream(out.device).cuda_stream
+        check(self._ctx, self._lib.ar_render(self._ctx, C.byref(p), out.data_ptr(), 1, None, s))
+
+    def adjoint(self, dl_dxyz, grad_out, size, cameraOrigin, cameraDirection, sampleNum: int, **kw) -> None:
+        """d(loss)/d(texels) into grad_out (CUDA float64, texel_count() elements), given
+        dl_dxyz = d(loss)/d(image) (CUDA float32, (height, width, 3)) for the image that
+        render_into / Render returns with the same arguments."""
+        import torch
+        self._build()
+        p = self.params(size, cameraOrigin, cameraDirection, sampleNum, **kw)
+        g = dl_dxyz.detach().to(torch.float32).contiguous()
+        if g.numel() != 3 * p.width * p.height:
+            raise ValueError("dl_dxyz must hold 3 floats per pixel")
+        n = self.texel_count()
+        if n and (grad_out.dtype != torch.float64 or not grad_out.is_contiguous() or grad_out.numel() != n):
+            raise ValueError(f"grad_out must be a contiguous float64 tensor of {n} elements")
+        s = torch.cuda.current_stream(g.device).cuda_stream
+        check(self._ctx, self._lib.ar_adjoint(self._ctx, C.byref(p), g.data_ptr(), grad_out.data_ptr(), s))
 
     def last_render_stats(self) -> tuple[float, int]:
         ms, n = C.c_float(), C.c_int64()

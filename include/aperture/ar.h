@@ -61,6 +61,10 @@ typedef struct ar_material
     float emissive[3];
     float roughness, metallic, specular;
     float ior, sigma_a, abbe, tilt;
+    /* Albedo texture (no counterpart in the reference): 0 = none (use albedo),
+     * k > 0 = texture k-1 of ar_scene_set_textures, sampled at the mesh
+     * triangle's interpolated uv (nearest texel, clamped to the edge). */
+    int32_t albedo_texture;
 } ar_material;
 
 /* One SceneObject: an oriented box (centre, half extent, Euler rotation in
@@ -120,6 +124,19 @@ ar_status ar_scene_set_materials(ar_ctx* ctx, const ar_material* materials, int 
 ar_status ar_scene_set_objects(ar_ctx* ctx, const ar_object* objects, int n);
 ar_status ar_scene_set_mesh(ar_ctx* ctx, const float* vertices, int n_vertices, const uint32_t* indices, int n_triangles,
                             const int32_t* material_ids);
+/* Albedo textures (no counterpart in the reference; the differentiable
+ * rendering workload's parameters).  texels: host, n_textures textures of
+ * sizes[2k] x sizes[2k+1] (width x height) RGB float32 texels, row-major,
+ * concatenated.  uv: host, 6 floats per mesh triangle (u, v at each vertex);
+ * texture row 0 is v = 0.  Both take effect at ar_scene_build. */
+ar_status ar_scene_set_textures(ar_ctx* ctx, const float* texels, const int32_t* sizes, int n_textures);
+ar_status ar_scene_set_mesh_uv(ar_ctx* ctx, const float* uv, int n_triangles);
+/* Replaces the texel values of a built scene without rebuilding it (same
+ * count as given to ar_scene_set_textures).  texels is device memory when
+ * is_device != 0, host memory otherwise; ordered on `stream`. */
+ar_status ar_scene_update_texels(ar_ctx* ctx, const float* texels, int64_t n_floats, int is_device, void* stream);
+/* Texel floats of the built scene (3 per texel, all textures). */
+ar_status ar_scene_texel_count(ar_ctx* ctx, int64_t* n_floats);
 /* Builds the BVH, the light table and the spectral LUTs; uploads the scene. */
 ar_status ar_scene_build(ar_ctx* ctx);
 /* BVH statistics: nodes, primitive slots, depth, bytes on the device. */
@@ -157,6 +174,21 @@ ar_status ar_trace_any(ar_ctx* ctx, const float* rays, int n, int32_t* hit, void
 #define AR_NOALLOC_SCRATCH_BYTES (8u << 20)
 #define AR_NOALLOC_MAX_PATHS 49408
 ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* params, double* out_xyz_device, void* stream);
+
+/* Replay adjoint (no counterpart in the reference).  Gradient of a scalar loss
+ * with respect to every albedo texel, given dl_dxyz = d(loss)/d(image), where
+ * image is what ar_render returns for the same params (per-pixel mean XYZ):
+ * device float32, 3 per pixel.  grad_texels: device float64, one per texel
+ * float (ar_scene_texel_count), overwritten.  The paths of the render are
+ * replayed from their random streams (nothing is stored per vertex): each wave
+ * is traced once for its radiance and once more to scatter
+ * d(loss)/d(radiance) x (radiance still to come) x d(albedo)/d(texel) / albedo
+ * at every textured diffuse vertex.  Russian-roulette and NEE decisions are
+ * held fixed (their probabilities are not differentiated).  Gradients gather
+ * in float32 per wave and fold into grad_texels in float64.  Guided rendering
+ * is rejected. */
+ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* params, const float* dl_dxyz, double* grad_texels,
+                     void* stream);
 
 /* Device time (ms) of the last ar_render and the number of kernels it launched. */
 ar_status ar_last_render_stats(ar_ctx* ctx, float* device_ms, int64_t* kernel_launches);

@@ -1,0 +1,74 @@
+"""The FP64 CPU oracle (oracle/pt64.cpp) pinned against the reference's own
+integrator (oracle/_ref, float), and its adjoint against its own central
+differences.  CPU only."""
+import numpy as np
+import pytest
+
+from aperturerendererv3_gb300 import configs
+from oracle import pt64
+from oracle import ref_runner as rr
+
+
+def per_sample_rel(objs, mesh, cam, size, spp, depth):
+    S = pt64.Scene64(objs, mesh)
+    m64, p64 = S.render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, per_sample=True)
+    mr, pr, _ = rr.render(objs, size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
+                          per_sample_frames=spp, mesh=mesh)
+    pr = pr.astype(np.float64)
+    rel = (np.abs(p64 - pr) / np.maximum(np.abs(pr), 1e-6)).max(-1)
+    return rel, m64, mr
+
+
+@pytest.fixture(scope="module")
+def ref_available():
+    if not rr.available():
+        pytest.skip("reference oracle not built in this checkout")
+
+
+def test_fp64_matches_reference_per_sample_on_the_triangle_cornell_box(ref_available):
+    rel, m64, mr = per_sample_rel(configs.cornell_triangles(), None, configs.CORNELL_CAMERA, (24, 24), 4, 8)
+    assert (rel < 1e-4).mean() > 0.999, (rel < 1e-4).mean()
+    assert abs(m64.mean() - mr.mean()) < 1e-5 * mr.mean()
+
+
+def test_fp64_matches_reference_per_sample_with_ggx_and_box_lights(ref_available):
+    rel, m64, mr = per_sample_rel(configs.reference_cornell(), None, configs.REFERENCE_CORNELL_CAMERA, (24, 24), 4, 16)
+    # glossy paths may part ways between float and double
+    assert (rel < 1e-3).mean() > 0.95, (rel < 1e-3).mean()
+
+
+def test_fp64_matches_reference_on_a_small_terrain(ref_available):
+    objs, mesh = configs.terrain_scene(res=48, n_spheres=8, seed=7)
+    rel, m64, mr = per_sample_rel(objs, mesh, configs.TERRAIN_CAMERA, (16, 12), 2, 16)
+    assert (rel < 1e-3).mean() > 0.9, (rel < 1e-3).mean()
+
+
+def test_fp64_adjoint_is_the_derivative_of_the_fp64_estimator():
+    """Central differences inside one LUT cell, NEE off, depth 3 (no roulette)."""
+    tex = configs.cornell_textures(4, seed=5)
+    objs, mesh, tx = configs.textured_cornell(tex)
+    cam = configs.CORNELL_CAMERA
+    size, spp, kw = (12, 12), 4, dict(fov=cam["fov"], max_depth=3, use_nee=False)
+    S = pt64.Scene64(objs, mesh, tx)
+    img = S.render(size, cam["origin"], cam["direction"], spp, **kw)
+    target = np.full_like(img, img.mean())
+    g = S.adjoint(2.0 * (img - target), size, cam["origin"], cam["direction"], spp, **kw)
+    flat = tex.reshape(-1).astype(np.float64)
+    gl = flat * 512 - 0.5
+    dist = np.abs(gl - np.round(gl)) / 512
+    cand = np.flatnonzero((np.abs(g) > 1e-6 * np.abs(g).max()) & (dist > 4e-4))
+    rng = np.random.default_rng(0)
+    probe = rng.choice(cand, size=min(12, len(cand)), replace=False)
+    for i in probe:
+        h = 0.45 * dist[i]
+        vals = []
+        for s in (1.0, -1.0):
+            t2 = flat.copy()
+            t2[i] += s * h
+            S2 = pt64.Scene64(objs, mesh, [t.astype(np.float32) for t in t2.reshape(tex.shape)])
+            im = S2.render(size, cam["origin"], cam["direction"], spp, **kw)
+            vals.append(((im - target) ** 2).sum())
+        # texels travel as float32: difference quotient over the float32 step
+        step = float(np.float32(flat[i] + h)) - float(np.float32(flat[i] - h))
+        fd = (vals[0] - vals[1]) / step
+        assert abs(fd - g[i]) <= 1e-3 * abs(fd) + 1e-12, (i, fd, g[i])
