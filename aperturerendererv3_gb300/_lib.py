@@ -74,6 +74,7 @@ EXPORTED = [
     "ar_get_error_word", "ar_clear_error_word", "ar_last_error", "ar_host_rgb_encode", "ar_host_lambda_encode",
     "ar_host_sample_lambda", "ar_host_trace_closest", "ar_host_guide_eval", "ar_abi_version",
     "ar_scene_set_textures", "ar_scene_set_mesh_uv", "ar_scene_update_texels", "ar_scene_texel_count", "ar_adjoint",
+    "ar_diag_umma_gemm", "ar_diag_mlp",
 ]
 
 _lib = None
@@ -126,6 +127,8 @@ def load() -> C.CDLL:
         "ar_scene_update_texels": (C.c_int, [vp, vp, C.c_int64, C.c_int, vp]),
         "ar_scene_texel_count": (C.c_int, [vp, P(C.c_int64)]),
         "ar_adjoint": (C.c_int, [vp, P(ArRenderParams), vp, vp, vp]),
+        "ar_diag_umma_gemm": (C.c_int, [C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp]),
+        "ar_diag_mlp": (C.c_int, [C.c_int, vp, vp, vp, vp, C.c_int, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -25,7 +25,7 @@ BUILD = REPO / "_build"
 LIB = PKG / "libaperture_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["capi.cu", "render.cu", "trace.cu", "noalloc.cu", "guide.cu", "adjoint.cu"]
+CU_SOURCES = ["capi.cu", "render.cu", "trace.cu", "noalloc.cu", "guide.cu", "adjoint.cu", "mlp.cu"]
 CPP_SOURCES = ["bvh_build.cpp"]
 HEADERS = ["ar_bvh.h", "ar_bvh_build.h", "ar_detmath.h", "ar_geom.h", "ar_guide.h", "ar_internal.h", "ar_rng.h",
            "ar_shade.h", "ar_spectral.h", "ar_traverse.cuh", "ar_vec.h"]

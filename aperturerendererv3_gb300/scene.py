@@ -29,6 +29,18 @@ from ._lib import (GLOBAL_SEED, OBJECT_CUBE, OBJECT_SPHERE, OBJECT_TRIANGLE, SHA
 Vec3 = Sequence[float]
 
 
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy
+
+
+def _torch_stream(device) -> int:
+    """torch's current stream as a cudaStream_t for the C ABI.  torch's default
+    stream has handle 0, which the C ABI reads as "the context's own stream";
+    the legacy default stream's own handle keeps the work ordered with torch."""
+    import torch
+    h = torch.cuda.current_stream(device).cuda_stream
+    return h if h else CUDA_STREAM_LEGACY
+
+
 def _f3(v: Vec3) -> tuple[float, float, float]:
     return (float(v[0]), float(v[1]), float(v[2]))
 
@@ -267,7 +279,7 @@ class SceneRenderer:
         if hasattr(texels, "data_ptr"):
             import torch
             t = texels.detach().to(torch.float32).contiguous()
-            s = torch.cuda.current_stream(t.device).cuda_stream
+            s = _torch_stream(t.device)
             check(self._ctx, self._lib.ar_scene_update_texels(self._ctx, t.data_ptr(), t.numel(), 1, s))
         else:
             a = np.ascontiguousarray(texels, np.float32).reshape(-1)
@@ -279,7 +291,7 @@ class SceneRenderer:
         self._build()
         p = self.params(size, cameraOrigin, cameraDirection, sampleNum, **kw)
         assert out.dtype == torch.float64 and out.is_contiguous() and out.numel() == 3 * p.width * p.height
-        s = torch.cuda.current_stream(out.device).cuda_stream
+        s = _torch_stream(out.device)
         check(self._ctx, self._lib.ar_render(self._ctx, C.byref(p), out.data_ptr(), 1, None, s))
 
     def adjoint(self, dl_dxyz, grad_out, size, cameraOrigin, cameraDirection, sampleNum: int, **kw) -> None:
@@ -295,7 +307,7 @@ class SceneRenderer:
         n = self.texel_count()
         if n and (grad_out.dtype != torch.float64 or not grad_out.is_contiguous() or grad_out.numel() != n):
             raise ValueError(f"grad_out must be a contiguous float64 tensor of {n} elements")
-        s = torch.cuda.current_stream(g.device).cuda_stream
+        s = _torch_stream(g.device)
         check(self._ctx, self._lib.ar_adjoint(self._ctx, C.byref(p), g.data_ptr(), grad_out.data_ptr(), s))
 
     def last_render_stats(self) -> tuple[float, int]:
@@ -333,7 +345,7 @@ class SceneRenderer:
         n = rays.shape[0]
         ids = torch.empty(n, dtype=torch.int32, device=rays.device)
         t = torch.empty(n, dtype=torch.float32, device=rays.device)
-        s = torch.cuda.current_stream(rays.device).cuda_stream if stream is None else stream
+        s = _torch_stream(rays.device) if stream is None else stream
         check(self._ctx, self._lib.ar_trace_closest(self._ctx, rays.data_ptr(), n, ids.data_ptr(), t.data_ptr(), s))
         return ids, t
 
@@ -343,7 +355,7 @@ class SceneRenderer:
         rays = rays.contiguous()
         n = rays.shape[0]
         hit = torch.empty(n, dtype=torch.int32, device=rays.device)
-        s = torch.cuda.current_stream(rays.device).cuda_stream if stream is None else stream
+        s = _torch_stream(rays.device) if stream is None else stream
         check(self._ctx, self._lib.ar_trace_any(self._ctx, rays.data_ptr(), n, hit.data_ptr(), s))
         return hit
 

@@ -1,6 +1,13 @@
 """Benchmark: Msamples/s of the spectral path tracer on one GB300 (or N replicas).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload cornell|terrain] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload terrain|cornell] [--impl ours|reference]
+
+The default workload is the guided-path-tracing terrain: 2048^2 fBm heightfield
+(8.38M triangles), 64 sphere lights and a sun, GGX materials, 1920x1080, 64 spp,
+depth 16, NEE + MIS, rendered by the plain method (the drop-in).  Beside the
+headline the line carries `extras`: the same workload with the voxel guide
+learning online, the replay adjoint's grads/s against central differences on
+the textured Cornell box, and closest-hit Mrays/s on 1M random triangles.
 
 A step renders the whole workload once (width x height x spp paths, each a full
 path up to max depth) with a fresh block of sample indices, so no work repeats.
@@ -128,22 +135,27 @@ def cpu_reference_run(workload: str, objs, mesh, cam, w: dict, sample_spp: int, 
     return st, wall
 
 
+def reference_sample(workload: str, size):
+    """Bounded sample of the workload for the reference CPU integrator: (size, spp per step)."""
+    if workload == "cornell":
+        return size, 2
+    return (32, 18), 1
+
+
 def run_reference(args, w) -> dict:
+    """The reference integrator (oracle/_ref, CPU, every host core) on a bounded
+    sample of the same workload.  One oracle call renders warmup + steps frames
+    of the sample (its BVH is built once per call, outside the timed loop, as
+    the reference builds its BVH before rendering)."""
     objs, mesh, cam = build_workload(args.workload)
     threads = os.cpu_count() or 1
     size = w["size"]
-    # bounded sample per step: a fraction of the frame at 1 spp
-    if args.workload == "cornell":
-        sample_size, sample_spp = size, 2
-    else:
-        sample_size, sample_spp = (32, 18), 1
-    vals = []
-    for i in range(args.warmup + args.steps):
-        st, wall = cpu_reference_run(args.workload, objs, mesh, cam, w, sample_spp, sample_size, threads)
-        if i >= args.warmup:
-            vals.append(st["msamples_per_s"])
-    value = float(np.mean(vals))
-    sample = f"{sample_size[0]}x{sample_size[1]}x{sample_spp} spp of the {args.workload} workload per step"
+    sample_size, sample_spp = reference_sample(args.workload, size)
+    st, _ = cpu_reference_run(args.workload, objs, mesh, cam, w, sample_spp * (args.warmup + args.steps),
+                              sample_size, threads)
+    value = float(st["msamples_per_s"])
+    sample = (f"{sample_size[0]}x{sample_size[1]}x{sample_spp} spp of the {args.workload} workload per step, "
+              f"{args.warmup + args.steps} steps in one call")
     return {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.prod(sample_size) * sample_spp / value / 1e3),
@@ -155,17 +167,125 @@ def run_reference(args, w) -> dict:
             "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def guided_extra(r, w, cam, steps: int) -> dict:
+    """Same workload with the voxel guide learning online (one frame per spp)."""
+    size, spp, depth = w["size"], w["spp"], w["depth"]
+    r.MarkNeedResetGuiding()
+    r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, guide=1)
+    ms = []
+    for k in range(steps):
+        r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, guide=1,
+                 first_frame=(k + 1) * spp)
+        ms.append(r.last_render_stats()[0])
+    n_probes, _ = r.guide_stats()
+    r.MarkNeedResetGuiding()
+    return {"value": size[0] * size[1] * spp / (float(np.mean(ms)) / 1e3) / 1e6, "unit": "Msamples/s",
+            "ms_per_step": float(np.mean(ms)), "steps": steps, "probes": n_probes}
+
+
+def adjoint_extra(device: int, steps: int) -> dict:
+    """Differentiable-rendering workload: the triangle Cornell box with 8 albedo
+    textures of 512^2 RGB texels (U[0.2, 0.8], seed 11) as parameters, target
+    rendered from a second texture set (seed 12) at 256 spp, L2 loss at 64 spp,
+    256x256, depth 8.  grads/s = texel parameters per second of ar_adjoint;
+    central finite differences need two renders per parameter."""
+    import torch
+    from aperturerendererv3_gb300 import SceneRenderer, configs
+    cam = configs.CORNELL_CAMERA
+    size, kw = (256, 256), dict(fov=cam["fov"], max_depth=8)
+    dev = torch.device("cuda", device)
+    objs, mesh, tx = configs.textured_cornell(configs.cornell_textures(512, seed=12))
+    rb = SceneRenderer(objs, device=device, mesh=mesh, textures=tx)
+    target = torch.empty((256, 256, 3), dtype=torch.float64, device=dev)
+    rb.render_into(target, size, cam["origin"], cam["direction"], 256, **kw)
+    rb.close()
+    objs, mesh, tx = configs.textured_cornell(configs.cornell_textures(512, seed=11))
+    r = SceneRenderer(objs, device=device, mesh=mesh, textures=tx)
+    img = torch.empty_like(target)
+    render_ms, adj_ms = [], []
+    grad = torch.empty(r.texel_count(), dtype=torch.float64, device=dev)
+    for k in range(steps + 1):
+        r.render_into(img, size, cam["origin"], cam["direction"], 64, **kw)
+        render_ms.append(r.last_render_stats()[0])
+        dl = (2.0 * (img - target)).float()
+        r.adjoint(dl, grad, size, cam["origin"], cam["direction"], 64, **kw)
+        adj_ms.append(r.last_render_stats()[0])
+    render_ms, adj_ms = float(np.mean(render_ms[1:])), float(np.mean(adj_ms[1:]))
+    n = r.texel_count()
+    adj_gps = n / (adj_ms / 1e3)
+    fd_gps = 1.0 / (2.0 * render_ms / 1e3)
+    return {"params": n, "adjoint_ms": adj_ms, "render_ms": render_ms, "grads_per_s": adj_gps,
+            "fd_grads_per_s": fd_gps, "speedup_vs_fd": adj_gps / fd_gps,
+            "loss": float(((img - target) ** 2).sum()), "workload": "textured Cornell 256x256, 64 spp, depth 8"}
+
+
+def bvh_stress_extra(device: int, steps: int) -> dict:
+    """BVH stress workload: 1M random triangles (centroids U[0,1]^3, vertices
+    +N(0, 0.005^2)), 1920x1080 primary rays plus one cosine-hemisphere bounce ray
+    per hit, closest hit through ar_trace_closest; Mrays/s of device time."""
+    import torch
+    from aperturerendererv3_gb300 import SceneRenderer, configs
+    from aperturerendererv3_gb300.scene import SceneObject, Material, TriangleMesh
+    tris = configs.random_triangles(1_000_000, seed=1)
+    v = tris.reshape(-1, 3)
+    mesh = TriangleMesh(v, np.arange(len(v), dtype=np.uint32).reshape(-1, 3), np.zeros(len(tris), np.int32),
+                        [Material.CreateDiffusePureColor((0.5, 0.5, 0.5))])
+    r = SceneRenderer([], device=device, mesh=mesh)
+    r.build()
+    cam = configs.BVH_STRESS_CAMERA
+    dev = torch.device("cuda", device)
+    prim = torch.as_tensor(configs.pinhole_rays(1920, 1080, cam["origin"], cam["direction"], cam["fov"]), device=dev)
+    ids, t = r.trace_closest(prim)
+    # one cosine bounce per hit, about the geometric normal facing the ray
+    hit = ids >= 0
+    tri = torch.as_tensor(tris, device=dev)[ids[hit].long()].view(-1, 3, 3)
+    n = torch.linalg.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    n = n / n.norm(dim=1, keepdim=True).clamp_min(1e-30)
+    d0 = prim[hit, 4:7]
+    n = torch.where((n * d0).sum(1, keepdim=True) > 0, -n, n)
+    p = prim[hit, 0:3] + d0 * t[hit, None]
+    g = torch.Generator(device=dev).manual_seed(2)
+    u1, u2 = torch.rand(len(n), device=dev, generator=g), torch.rand(len(n), device=dev, generator=g)
+    a = torch.where(n[:, 2:3].abs() < 0.999, torch.tensor([0.0, 0.0, 1.0], device=dev),
+                    torch.tensor([1.0, 0.0, 0.0], device=dev))
+    tt = torch.linalg.cross(a, n)
+    tt = tt / tt.norm(dim=1, keepdim=True)
+    bb = torch.linalg.cross(n, tt)
+    rr_, ph = torch.sqrt(u1), 2 * np.pi * u2
+    d1 = tt * (rr_ * torch.cos(ph))[:, None] + bb * (rr_ * torch.sin(ph))[:, None] + n * torch.sqrt(1 - u1)[:, None]
+    bounce = torch.cat([p, torch.full((len(n), 1), 1e-4, device=dev), d1,
+                        torch.full((len(n), 1), float("inf"), device=dev)], 1).float().contiguous()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(2):
+        r.trace_closest(prim)
+        r.trace_closest(bounce)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(steps):
+        r.trace_closest(prim)
+        r.trace_closest(bounce)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    nrays = len(prim) + len(bounce)
+    return {"value": nrays / (ms / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms, "primary_rays": len(prim),
+            "bounce_rays": len(bounce), "hit_fraction": float(hit.float().mean())}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="cornell", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="terrain", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None, help="WxH override (small profiling cases)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
     ap.add_argument("--guide", type=int, default=0, choices=[0, 1], help="1: voxel path guide on")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the guided, adjoint and BVH-stress measurements reported beside the headline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = dict(WORKLOADS[args.workload])
@@ -269,10 +389,20 @@ def main() -> None:
         "traversal": {k: prof[k] for k in ("extend_rays", "extend_node_visits", "extend_prim_tests", "shadow_rays",
                                            "shadow_node_visits", "shadow_prim_tests")},
     }
+    if not args.no_extras:
+        extras = {}
+        for name, fn in (("guided_voxel", lambda: guided_extra(r, w, cam, 3)),
+                         ("adjoint", lambda: adjoint_extra(local, 3)),
+                         ("bvh_stress", lambda: bvh_stress_extra(local, 5))):
+            try:
+                extras[name] = fn()
+            except Exception as e:  # an extra never hides the headline
+                extras[name] = {"error": str(e)}
+        out["extras"] = extras
     if rank == 0 and not args.no_cpu_baseline:
         try:
             threads = os.cpu_count() or 1
-            sample_size, sample_spp = ((size[0], size[1]), 2) if args.workload == "cornell" else ((32, 18), 1)
+            sample_size, sample_spp = reference_sample(args.workload, size)
             st, _ = cpu_reference_run(args.workload, objs, mesh, cam, w, sample_spp, sample_size, threads)
             out["cpu_baseline"] = {"value": st["msamples_per_s"], "unit": "Msamples/s", "cores": st["threads"],
                                    "kind": "reference",

@@ -49,6 +49,7 @@ typedef int ar_status;
 /* device error word bits */
 #define AR_DEVERR_TRAVERSAL_STACK 1u
 #define AR_DEVERR_QUEUE 2u
+#define AR_DEVERR_MLP 4u    /* a tensor-core wait of the MLP guide ran out (work skipped) */
 
 typedef struct ar_ctx ar_ctx;
 
@@ -218,6 +219,25 @@ ar_status ar_host_trace_closest(const float* tris, int ntri, const float* rays, 
  * sampling) for one probe: the functions the guided kernels run. */
 ar_status ar_host_guide_eval(const float* in, int n, float* out);
 int ar_abi_version(void);
+
+/* Diagnostic (no reference counterpart): one 128 x n x k BF16 tensor-core
+ * product through the shared-memory descriptors the MLP guide uses, D = A B^T
+ * with FP32 accumulation.  a: 128 x k row-major (a_mn = 0) or k x 128
+ * (a_mn = 1); b: n x k (b_mn = 0) or k x n (b_mn = 1); bf16 bit patterns, host
+ * memory; d: 128 x n floats, host.  swap exchanges the descriptors' two stride
+ * fields (for checking the layout convention).  n, k in {64, 128, 144}. */
+/* Diagnostic (no reference counterpart): the MLP guide's tensor-core forward
+ * and backward passes on given inputs.  params: AR_MLP_PARAMS floats (per
+ * layer W[64][in] row-major then b[64]; in = 144 for layer 0, 64 after).
+ * in6: n x 6 encoded inputs in [0, 1] (position in the scene box, then
+ * (reflected direction + 1) / 2); dirs: n x 3 record directions; lum: n record
+ * radiances (CIE Y).  Outputs (host): logits n x 64, grad AR_MLP_PARAMS
+ * (d mean loss / d params), loss (sum over records). */
+#define AR_MLP_PARAMS 25920
+ar_status ar_diag_mlp(int device, const float* params, const float* in6, const float* dirs, const float* lum, int n,
+                      float* logits, float* grad, float* loss);
+ar_status ar_diag_umma_gemm(int device, const uint16_t* a, const uint16_t* b, int a_mn, int b_mn, int n, int k,
+                            int swap, float* d);
 
 #ifdef __cplusplus
 }
