@@ -48,11 +48,13 @@ class ArRenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("cam_origin", F3), ("cam_dir", F3), ("fov_deg", C.c_float), ("use_nee", C.c_int32),
                 ("seed", C.c_uint64), ("first_frame", C.c_int32), ("wave_paths", C.c_int32),
-                ("profile", C.c_int32), ("guide", C.c_int32), ("guide_unit", C.c_float)]
+                ("profile", C.c_int32), ("guide", C.c_int32), ("guide_unit", C.c_float),
+                ("guide_train_steps", C.c_int32)]
 
 
 GUIDE_NONE = 0
 GUIDE_VOXEL = 1
+GUIDE_MLP = 2
 
 
 class ArRenderProfile(C.Structure):
@@ -74,7 +76,7 @@ EXPORTED = [
     "ar_get_error_word", "ar_clear_error_word", "ar_last_error", "ar_host_rgb_encode", "ar_host_lambda_encode",
     "ar_host_sample_lambda", "ar_host_trace_closest", "ar_host_guide_eval", "ar_abi_version",
     "ar_scene_set_textures", "ar_scene_set_mesh_uv", "ar_scene_update_texels", "ar_scene_texel_count", "ar_adjoint",
-    "ar_diag_umma_gemm", "ar_diag_mlp",
+    "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats",
 ]
 
 _lib = None
@@ -128,7 +130,8 @@ def load() -> C.CDLL:
         "ar_scene_texel_count": (C.c_int, [vp, P(C.c_int64)]),
         "ar_adjoint": (C.c_int, [vp, P(ArRenderParams), vp, vp, vp]),
         "ar_diag_umma_gemm": (C.c_int, [C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp]),
-        "ar_diag_mlp": (C.c_int, [C.c_int, vp, vp, vp, vp, C.c_int, vp, vp, vp]),
+        "ar_diag_mlp": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp]),
+        "ar_guide_mlp_stats": (C.c_int, [vp, P(C.c_int32), P(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

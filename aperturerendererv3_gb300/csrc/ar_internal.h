@@ -9,6 +9,7 @@
 
 #include "ar_bvh_build.h"
 #include "ar_guide.h"
+#include "ar_mlp.h"
 #include "ar_shade.h"
 #include "ar_traverse.cuh"
 
@@ -79,6 +80,8 @@ struct GuideSamples
     unsigned long long* key;  // packed voxel key, EMPTY = out of range
     int* count;
     int capacity;
+    float4* pos;              // MLP guide only: vertex position
+    float4* wr;               // MLP guide only: reflected view direction
 };
 // Device-side scene as the kernels see it (passed by value).
 struct DevScene
@@ -153,6 +156,11 @@ struct PathState
     // d(loss)/d(radiance)
     float* adj_total;
     float* adj_delta;
+    // MLP guide only: network inputs of the path's current hit and the 64
+    // quantised cell weights inferred for it
+    float4* q_pos;      // xyz hit position, w = 1 when the query is valid
+    float4* q_wr;       // xyz reflected view direction
+    uint8_t* q_dist;    // 64 per path
 };
 
 struct ShadowQueue
@@ -173,9 +181,10 @@ struct RenderLaunch
     uint64_t seed;
     int first_frame;
     int profile;
-    int guide;    // 0 none, 1 voxel probes
+    int guide;    // 0 none, 1 voxel probes, 2 MLP (voxel probes until the network has trained)
     int adjoint;  // 1: replay pass of ar_adjoint (gradient scatter, no output)
     float* grad;  // replay pass: float32 texel gradients
+    int mlp_ready;  // guide 2: sample from the network instead of the voxel probes
 };
 
 struct Ctx
@@ -255,7 +264,44 @@ struct Ctx
     GuideSamples gs{};
     int gs_capacity = 0;
     int pg_path_cap = 0;  // wavefront capacity the collection slots were sized for
+    // MLP guide
+    float* d_mlp_w32 = nullptr;   // master parameters
+    uint16_t* d_mlp_wbf = nullptr;
+    float* d_mlp_grad = nullptr;
+    float* d_mlp_m = nullptr;
+    float* d_mlp_v = nullptr;
+    float* d_mlp_loss = nullptr;  // loss sum of the last training step
+    int mlp_step = 0;
+    int mlp_steps_per_frame = 8;
+    int mlp_path_cap = 0;
+    int* d_mlp_list = nullptr;    // compacted queue of the paths the network is queried for
+    MlpBox mlp_box{};
 };
+
+// MLP guide (mlp.cu)
+struct MlpDev
+{
+    const uint16_t* wbf;
+    const float* w32;
+    MlpBox box;
+};
+cudaError_t mlp_prepare_kernels();
+cudaError_t launch_mlp_infer(const MlpDev& net, const float4* q_pos, const float4* q_wr, const int* queue,
+                             const int* count, int n_direct, uint8_t* out, float* logits, unsigned* err, int sms,
+                             cudaStream_t s);
+cudaError_t launch_mlp_train(const MlpDev& net, const float4* r_pos, const float4* r_wr, const float4* r_dir,
+                             const float4* r_rad, const int* count, int n_direct, int n_train, int offset, float* grad,
+                             float* loss_sum, unsigned* err, int sms, cudaStream_t s);
+cudaError_t launch_mlp_bias_start(float* w32, const float4* r_rad, const int* count, cudaStream_t s);
+cudaError_t launch_mlp_adam(float* w32, uint16_t* wbf, float* grad, float* m, float* v, int step, float lr,
+                            cudaStream_t s);
+cudaError_t launch_mlp_to_bf16(const float* w32, uint16_t* wbf, cudaStream_t s);
+// frames of training before the guide switches from the voxel probes to the network
+constexpr int AR_MLP_WARMUP_STEPS = 16;        // Adam steps (2 frames)
+constexpr int AR_MLP_STEPS_PER_FRAME = 8;       // Adam steps after every frame, each on its own record subset
+constexpr int AR_MLP_TRAIN_RECORDS = 1 << 14;  // records per step (spread over the frame's records)
+constexpr int AR_MLP_MAX_NDD = 3;               // the network guides the first non-delta vertices, the probes the rest
+constexpr float AR_MLP_LR = 1.0e-3f;
 
 // voxel guide (guide.cu)
 cudaError_t launch_guide_update(Ctx& c, long long* launches);

@@ -4,12 +4,14 @@
 // Network: 12-band frequency encoding of the shading point (position
 // normalised to the scene box) and of the reflected view direction (6 inputs x
 // 12 bands x sin/cos = 144 features), then 144 -> 64 -> 64 -> 64 -> 64 -> 64
-// with ReLU between layers.  The 64 outputs are log-radiance estimates for the
-// 8 x 8 cells of the same equal-area (Clarberg) sphere map the voxel probes
-// use; the guide samples cells in proportion to exp(output), quantised to 8
+// with ReLU between layers.  The 64 outputs estimate the log of the mean
+// incident radiance in the 8 x 8 cells of the same equal-area (Clarberg)
+// sphere map the voxel probes use; the guide samples cells in proportion to exp(output), quantised to 8
 // bits per cell (64 bytes per shading point), and a point uniformly inside the
 // cell, folded into the normal's hemisphere as the voxel guide folds its lobe.
 #pragma once
+#include <string.h>
+
 #include "ar_guide.h"
 
 #define AR_MLP_IN 144
@@ -49,6 +51,42 @@ AR_HD void mlp_inputs(const MlpBox& b, V3 p, V3 wr, float in6[6])
 
 // feature index of (input d, band j, cos?) in the 144-wide encoding
 AR_HD int mlp_feature(int d, int j, int c) { return d * 2 * AR_MLP_BANDS + 2 * j + c; }
+
+// unit vector <-> 32 bits (octahedral map, 16-bit signed fixed point per axis)
+AR_HD float mlp_pack_normal(V3 n)
+{
+    const float s = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
+    float u = n.x / fmaxf(s, 1e-20f), v = n.y / fmaxf(s, 1e-20f);
+    if (n.z < 0.0f)
+    {
+        const float pu = (1.0f - fabsf(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+        const float pv = (1.0f - fabsf(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+        u = pu;
+        v = pv;
+    }
+    const int iu = (int)lrintf(clampf(u, -1.0f, 1.0f) * 32767.0f);
+    const int iv = (int)lrintf(clampf(v, -1.0f, 1.0f) * 32767.0f);
+    const uint32_t bits = ((uint32_t)(uint16_t)(int16_t)iu) | ((uint32_t)(uint16_t)(int16_t)iv << 16);
+    float f;
+    memcpy(&f, &bits, 4);
+    return f;
+}
+
+AR_HD V3 mlp_unpack_normal(float f)
+{
+    uint32_t bits;
+    memcpy(&bits, &f, 4);
+    const float u = (float)(int16_t)(uint16_t)(bits & 0xffffu) / 32767.0f;
+    const float v = (float)(int16_t)(uint16_t)(bits >> 16) / 32767.0f;
+    const float z = 1.0f - fabsf(u) - fabsf(v);
+    V3 n = v3(u, v, z);
+    if (z < 0.0f)
+    {
+        n.x = (1.0f - fabsf(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+        n.y = (1.0f - fabsf(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+    }
+    return normalize(n);
+}
 
 AR_HD int mlp_cell(V3 d)
 {

@@ -165,6 +165,8 @@ void free_guide(Ctx& c)
     free_dev(c.gs.dir);
     free_dev(c.gs.key);
     free_dev(c.gs.count);
+    free_dev(c.gs.pos);
+    free_dev(c.gs.wr);
     free_dev(c.ps.maskq);
     free_dev(c.ps.pg_dir);
     free_dev(c.ps.pg_loc);
@@ -225,6 +227,8 @@ ar_status ensure_guide(ar_ctx* ctx, float unit, long long npix)
         free_dev(c.gs.dir);
         free_dev(c.gs.key);
         free_dev(c.gs.count);
+        free_dev(c.gs.pos);  // reallocated at the new size by ensure_mlp when the network is on
+        free_dev(c.gs.wr);
         AR_CUDA(ctx, alloc_dev(c.gs.radiance, nrec));
         AR_CUDA(ctx, alloc_dev(c.gs.dir, nrec));
         AR_CUDA(ctx, alloc_dev(c.gs.key, nrec));
@@ -243,6 +247,159 @@ ar_status ensure_guide(ar_ctx* ctx, float unit, long long npix)
     AR_CUDA(ctx, alloc_dev(c.ps.pg_vdir, ns));
     c.pg_path_cap = wave_cap;
     return AR_OK;
+}
+
+void object_bounds(const Object& o, float lo[3], float hi[3]);
+
+void free_mlp(Ctx& c)
+{
+    free_dev(c.d_mlp_w32);
+    free_dev(c.d_mlp_wbf);
+    free_dev(c.d_mlp_grad);
+    free_dev(c.d_mlp_m);
+    free_dev(c.d_mlp_v);
+    free_dev(c.d_mlp_loss);
+    free_dev(c.ps.q_pos);
+    free_dev(c.ps.q_wr);
+    free_dev(c.ps.q_dist);
+    free_dev(c.d_mlp_list);
+    c.mlp_step = 0;
+    c.mlp_path_cap = 0;
+}
+
+// Network state of the MLP guide: He-initialised weights (fixed seed; the
+// output layer scaled by 0.1 so the first distributions are near uniform),
+// Adam moments, per-path query buffers and the records' extra fields.  The
+// position box spans the non-emissive geometry (a distant sun would squeeze
+// everything else into a corner of the encoding).
+ar_status ensure_mlp(ar_ctx* ctx)
+{
+    Ctx& c = ctx->c;
+    if (!c.d_mlp_w32)
+    {
+        std::vector<float> w(AR_MLP_PARAMS, 0.0f);
+        uint64_t st = 0x853c49e6748fea9bull;
+        auto gauss = [&st]() {
+            // Box-Muller on a 64-bit LCG (Knuth MMIX constants)
+            st = st * 6364136223846793005ull + 1442695040888963407ull;
+            const double u1 = ((st >> 11) + 1.0) * (1.0 / 9007199254740993.0);
+            st = st * 6364136223846793005ull + 1442695040888963407ull;
+            const double u2 = (st >> 11) * (1.0 / 9007199254740992.0);
+            return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+        };
+        for (int l = 0; l < AR_MLP_LAYERS; ++l)
+        {
+            const int in = mlp_in_dim(l);
+            const double sd = std::sqrt(2.0 / in) * (l == AR_MLP_LAYERS - 1 ? 0.1 : 1.0);
+            for (int k = 0; k < 64 * in; ++k) w[mlp_w_offset(l) + k] = (float)(gauss() * sd);
+        }
+        AR_CUDA(ctx, alloc_dev(c.d_mlp_w32, (size_t)AR_MLP_PARAMS));
+        AR_CUDA(ctx, alloc_dev(c.d_mlp_wbf, (size_t)AR_MLP_PARAMS));
+        AR_CUDA(ctx, alloc_dev(c.d_mlp_grad, (size_t)AR_MLP_PARAMS));
+        AR_CUDA(ctx, alloc_dev(c.d_mlp_m, (size_t)AR_MLP_PARAMS));
+        AR_CUDA(ctx, alloc_dev(c.d_mlp_v, (size_t)AR_MLP_PARAMS));
+        AR_CUDA(ctx, alloc_dev(c.d_mlp_loss, 1));
+        AR_CUDA(ctx, cudaMemcpy(c.d_mlp_w32, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+        AR_CUDA(ctx, cudaMemset(c.d_mlp_grad, 0, AR_MLP_PARAMS * sizeof(float)));
+        AR_CUDA(ctx, cudaMemset(c.d_mlp_m, 0, AR_MLP_PARAMS * sizeof(float)));
+        AR_CUDA(ctx, cudaMemset(c.d_mlp_v, 0, AR_MLP_PARAMS * sizeof(float)));
+        AR_CUDA(ctx, cudaMemset(c.d_mlp_loss, 0, sizeof(float)));
+        AR_CUDA(ctx, launch_mlp_to_bf16(c.d_mlp_w32, c.d_mlp_wbf, c.stream));
+        AR_CUDA(ctx, mlp_prepare_kernels());
+        c.mlp_step = 0;
+        // box of the non-emissive geometry
+        float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
+        auto grow = [&](const float* a, const float* b) {
+            for (int k = 0; k < 3; ++k)
+            {
+                lo[k] = std::min(lo[k], a[k]);
+                hi[k] = std::max(hi[k], b[k]);
+            }
+        };
+        for (size_t i = 0; i < c.objects.size(); ++i)
+        {
+            if (c.materials[c.object_material[i]].shading == AR_MAT_LIGHT) continue;
+            float a[3], b[3];
+            if (c.object_type[i] == AR_OBJECT_TRIANGLE)
+            {
+                const float* t = &c.object_tri[9 * i];
+                for (int k = 0; k < 3; ++k)
+                {
+                    a[k] = std::min(t[k], std::min(t[3 + k], t[6 + k]));
+                    b[k] = std::max(t[k], std::max(t[3 + k], t[6 + k]));
+                }
+            }
+            else object_bounds(c.objects[i], a, b);
+            grow(a, b);
+        }
+        for (size_t t = 0; t < c.mesh_material.size(); ++t)
+        {
+            if (c.materials[c.mesh_material[t]].shading == AR_MAT_LIGHT) continue;
+            const float* v = &c.mesh_v[9 * t];
+            for (int j = 0; j < 3; ++j) grow(v + 3 * j, v + 3 * j);
+        }
+        if (!(lo[0] <= hi[0]))
+            for (int k = 0; k < 3; ++k)
+            {
+                lo[k] = c.bvh.root_lo[k];
+                hi[k] = c.bvh.root_hi[k];
+            }
+        for (int k = 0; k < 3; ++k)
+        {
+            const float ext = std::max(hi[k] - lo[k], 1e-6f);
+            c.mlp_box.lo[k] = lo[k] - 0.01f * ext;
+            c.mlp_box.inv[k] = 1.0f / (1.02f * ext);
+        }
+    }
+    if (c.mlp_path_cap != c.ps.capacity)
+    {
+        free_dev(c.ps.q_pos);
+        free_dev(c.ps.q_wr);
+        free_dev(c.ps.q_dist);
+        free_dev(c.d_mlp_list);
+        AR_CUDA(ctx, alloc_dev(c.d_mlp_list, (size_t)c.ps.capacity));
+        AR_CUDA(ctx, alloc_dev(c.ps.q_pos, (size_t)c.ps.capacity));
+        AR_CUDA(ctx, alloc_dev(c.ps.q_wr, (size_t)c.ps.capacity));
+        AR_CUDA(ctx, alloc_dev(c.ps.q_dist, 64 * (size_t)c.ps.capacity));
+        c.mlp_path_cap = c.ps.capacity;
+    }
+    if (!c.gs.pos)
+    {
+        AR_CUDA(ctx, alloc_dev(c.gs.pos, (size_t)c.gs.capacity));
+        AR_CUDA(ctx, alloc_dev(c.gs.wr, (size_t)c.gs.capacity));
+    }
+    return AR_OK;
+}
+
+// one Adam step of the network on the frame's radiance records
+cudaError_t mlp_train_frame(Ctx& c, long long* launches)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
+    MlpDev net;
+    net.wbf = c.d_mlp_wbf;
+    net.w32 = c.d_mlp_w32;
+    net.box = c.mlp_box;
+    cudaError_t e = cudaSuccess;
+    if (c.mlp_step == 0)
+    {
+        e = launch_mlp_bias_start(c.d_mlp_w32, c.gs.radiance, c.gs.count, c.stream);
+        if (launches) *launches += 1;
+    }
+    for (int k = 0; k < c.mlp_steps_per_frame && e == cudaSuccess; ++k)
+    {
+        // each step trains on its own subset of the frame's records; the loss of the last one is kept
+        e = cudaMemsetAsync(c.d_mlp_loss, 0, sizeof(float), c.stream);
+        if (e == cudaSuccess)
+            e = launch_mlp_train(net, c.gs.pos, c.gs.wr, c.gs.dir, c.gs.radiance, c.gs.count, 0,
+                                 AR_MLP_TRAIN_RECORDS, 1013 * k, c.d_mlp_grad, c.d_mlp_loss, c.d_err, sms, c.stream);
+        if (e == cudaSuccess)
+            e = launch_mlp_adam(c.d_mlp_w32, c.d_mlp_wbf, c.d_mlp_grad, c.d_mlp_m, c.d_mlp_v, c.mlp_step + 1,
+                                AR_MLP_LR, c.stream);
+        if (e == cudaSuccess) ++c.mlp_step;
+        if (launches) *launches += 2;
+    }
+    return e;
 }
 
 // Material::Create* semantics: which fields each shading model keeps, clamps.
@@ -450,6 +607,7 @@ ar_status ar_destroy(ar_ctx* ctx)
     if (c.stream) cudaStreamSynchronize(c.stream);
     free_scene(c);
     free_guide(c);
+    free_mlp(c);
     free_waves(c);
     free_dev(c.d_lut_rgb);
     free_dev(c.d_lut_lambda);
@@ -684,6 +842,7 @@ ar_status ar_scene_build(ar_ctx* ctx)
     // device upload (a rebuilt scene starts with an empty guide)
     free_scene(c);
     free_guide(c);
+    free_mlp(c);
     std::vector<Object> objs(c.objects);
     if (objs.empty()) objs.resize(1);
     AR_CUDA(ctx, alloc_dev(c.d_nodes, c.bvh.nodes.size() * sizeof(ar_wide_node)));
@@ -776,7 +935,7 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     const long long npix = (long long)rl.width * rl.height;
     const long long total = npix * rl.spp;
     rl.guide = prm->guide;
-    if (rl.guide != 0 && rl.guide != 1) return fail(ctx, AR_ERR_INVALID, "render: unknown guide mode");
+    if (rl.guide < 0 || rl.guide > 2) return fail(ctx, AR_ERR_INVALID, "render: unknown guide mode");
     int cap = prm->wave_paths > 0 ? prm->wave_paths : (1 << 21);
     if ((long long)cap > total) cap = (int)total;
     // guided frames learn from the previous frame: waves never straddle frames
@@ -788,6 +947,13 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
         st = ensure_guide(ctx, prm->guide_unit, npix);
         if (st != AR_OK) return st;
     }
+    if (rl.guide == 2)
+    {
+        st = ensure_mlp(ctx);
+        if (st != AR_OK) return st;
+    }
+    c.mlp_steps_per_frame = prm->guide_train_steps > 0 ? prm->guide_train_steps : AR_MLP_STEPS_PER_FRAME;
+    rl.mlp_ready = (rl.guide == 2 && c.mlp_step >= AR_MLP_WARMUP_STEPS) ? 1 : 0;
     if (c.accum_pixels < (size_t)npix)
     {
         free_dev(c.d_accum);
@@ -816,8 +982,14 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
         first += n;
         if (rl.guide && e == cudaSuccess && first % npix == 0)
         {
-            // end of a frame: learn from its radiance records (core/scene.cu:258-273)
-            e = launch_guide_update(c, &launches);
+            // end of a frame: learn from its radiance records (core/scene.cu:258-273); the
+            // network trains first (the probe update clears the record count)
+            if (rl.guide == 2)
+            {
+                e = mlp_train_frame(c, &launches);
+                rl.mlp_ready = c.mlp_step >= AR_MLP_WARMUP_STEPS ? 1 : 0;
+            }
+            if (e == cudaSuccess) e = launch_guide_update(c, &launches);
             c.guide.probe_count = 1;
         }
     }
@@ -974,6 +1146,22 @@ ar_status ar_guide_reset(ar_ctx* ctx, int32_t* n_probes)
     AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
     if (n_probes) *n_probes = guide_probe_count(c);
     free_guide(c);
+    free_mlp(c);
+    return AR_OK;
+}
+
+ar_status ar_guide_mlp_stats(ar_ctx* ctx, int32_t* steps, float* last_loss)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
+    if (steps) *steps = c.mlp_step;
+    if (last_loss)
+    {
+        *last_loss = 0.0f;
+        if (c.d_mlp_loss) AR_CUDA(ctx, cudaMemcpy(last_loss, c.d_mlp_loss, sizeof(float), cudaMemcpyDeviceToHost));
+    }
     return AR_OK;
 }
 

@@ -6,20 +6,16 @@
 
 #include <cuda_bf16.h>
 
-#include "ar_mlp.h"
+#include "ar_internal.h"
 #include "ar_umma.cuh"
 #include "../../include/aperture/ar.h"
 
 namespace ar
 {
 // ------------------------------------------------------------------ MLP guide
-// Network parameters as the kernels see them.
-struct MlpDev
-{
-    const uint16_t* wbf;  // bf16 weights at mlp_w_offset (bias slots unused)
-    const float* w32;     // float32 master parameters (biases read from here)
-    MlpBox box;
-};
+// Network parameters as the kernels see them: MlpDev (ar_internal.h), bf16
+// weights at mlp_w_offset (bias slots unused) and the float32 master block
+// the biases are read from.
 
 namespace mlpk
 {
@@ -27,8 +23,9 @@ constexpr int W_BYTES = 64 * 144 * 2 + 4 * 64 * 64 * 2;  // weight tiles, all la
 constexpr int X_BYTES = 128 * 144 * 2;                   // encoded inputs of one tile
 constexpr int H_BYTES = 128 * 64 * 2;                    // one hidden layer of one tile
 constexpr int DY_BYTES = 128 * 128 * 2;                  // layer gradient, M padded to 128
-constexpr int INF_WG = 3;                                // warpgroups (tiles in flight) per CTA
-constexpr int INF_SMEM = W_BYTES + INF_WG * (X_BYTES + H_BYTES) + 5 * 64 * 4;
+constexpr int INF_WG = 4;                                // warpgroups (tiles in flight) per CTA
+// per warpgroup one buffer: the encoded inputs, then (layer 0 done) the hidden layer
+constexpr int INF_SMEM = W_BYTES + INF_WG * X_BYTES + 5 * 64 * 4;
 constexpr int TR_SMEM = W_BYTES + X_BYTES + 4 * H_BYTES + 2 * DY_BYTES + 2 * 5 * 64 * 4;
 constexpr uint32_t TR_TMEM_COLS = 512;
 // TMEM columns of the weight-gradient accumulators (working accumulator at 0)
@@ -139,14 +136,14 @@ __global__ void __launch_bounds__(128 * mlpk::INF_WG, 1)
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* W = smem;
     const int wg = threadIdx.x >> 7, row = threadIdx.x & 127, warp_in_wg = (threadIdx.x >> 5) & 3;
-    uint8_t* X = smem + W_BYTES + wg * (X_BYTES + H_BYTES);
-    uint8_t* H = X + X_BYTES;
-    float* sbias = reinterpret_cast<float*>(smem + W_BYTES + INF_WG * (X_BYTES + H_BYTES));
+    uint8_t* X = smem + W_BYTES + wg * X_BYTES;
+    uint8_t* H = X;  // the layer-0 product has completed before the first hidden row is written
+    float* sbias = reinterpret_cast<float*>(smem + W_BYTES + INF_WG * X_BYTES);
     __shared__ uint64_t mbar[INF_WG];
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag[INF_WG];
     load_weights(W, net.wbf, sbias, net.w32);
-    if (threadIdx.x < 32) umma::tmem_alloc(&tmem_slot, 256);
+    if (threadIdx.x < 32) umma::tmem_alloc(&tmem_slot, 64 * INF_WG);
     if (threadIdx.x < INF_WG)
     {
         umma::mbar_init(&mbar[threadIdx.x], 1);
@@ -244,17 +241,21 @@ __global__ void __launch_bounds__(128 * mlpk::INF_WG, 1)
     }
     umma::fence_before_sync();
     __syncthreads();
-    if (threadIdx.x < 32) umma::tmem_free(tmem_slot, 256);
+    if (threadIdx.x < 32) umma::tmem_free(tmem_slot, 64 * INF_WG);
 }
 
 // Training: forward, loss gradient and backward over tiles of 128 radiance
 // records; weight gradients accumulate in TMEM for all of a CTA's tiles and are
-// added to the float32 gradient block at the end.  Loss per record:
-// 0.5 (y[cell(dir)] - log(Y + 1e-3))^2, averaged over the records used.
+// added to the float32 gradient block at the end.  Loss per record (Poisson
+// log-likelihood of the record's radiance Y under the cell's predicted mean
+// exp(y), the cell being the record direction's): exp(y) - Y y, averaged over
+// the records used; its minimiser is exp(y) = E[Y | position, cell], the mean
+// radiance a voxel probe's texel holds.
 __global__ void __launch_bounds__(128, 1)
     k_mlp_train(MlpDev net, const float4* __restrict__ r_pos, const float4* __restrict__ r_wr,
                 const float4* __restrict__ r_dir, const float4* __restrict__ r_rad, const int* __restrict__ count_ptr,
-                int n_direct, int n_train, float* __restrict__ grad, float* __restrict__ loss_sum, unsigned* err)
+                int n_direct, int n_train, int offset, float* __restrict__ grad, float* __restrict__ loss_sum,
+                unsigned* err)
 {
     using namespace mlpk;
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -296,16 +297,26 @@ __global__ void __launch_bounds__(128, 1)
     {
         const int s = tile * 128 + row;
         const bool valid = s < n_use;
-        const int rec = valid ? s * stride : 0;
+        const int rec = valid ? (int)(((long long)s * stride + offset) % count) : 0;
         float in6[6] = {0, 0, 0, 0, 0, 0};
-        int cell = 0;
+        int cell = 0, cell_m = -1;
         float target = 0.0f;
         if (valid)
         {
             const float4 a = r_pos[rec], w = r_wr[rec], d = r_dir[rec], L = r_rad[rec];
             mlp_inputs(net.box, v3(a.x, a.y, a.z), v3(w.x, w.y, w.z), in6);
-            cell = mlp_cell(v3(d.x, d.y, d.z));
-            target = __logf(fmaxf(L.y, 0.0f) + 1.0e-3f);
+            const V3 dd = normalize(v3(d.x, d.y, d.z));
+            cell = mlp_cell(dd);
+            target = fmaxf(L.y, 0.0f);
+            // a zero-radiance virtual record below the surface, mirrored from the record's direction:
+            // cells under the tangent plane see no records otherwise, and the sampler folds them up
+            const V3 nn = mlp_unpack_normal(w.w);
+            const float dn = dot(dd, nn);
+            if (dn > 0.0f)
+            {
+                cell_m = mlp_cell(dd - nn * (2.0f * dn));
+                if (cell_m == cell) cell_m = -1;
+            }
         }
         encode_row(X, row, in6);
         wg_publish(0);
@@ -346,18 +357,26 @@ __global__ void __launch_bounds__(128, 1)
             }
             else
             {
-                float dy = 0.0f;
+                float dy = 0.0f, dym = 0.0f;
                 if (valid)
                 {
-                    const float y = v[cell] + b[cell];
-                    dy = (y - target) * inv_n;
-                    my_loss += 0.5f * (y - target) * (y - target);
+                    const float y = fminf(v[cell] + b[cell], 30.0f);
+                    const float ey = __expf(y);
+                    dy = (ey - target) * inv_n;
+                    my_loss += ey - target * y;
                     atomicAdd(&sdb[4 * 64 + cell], dy);
+                    if (cell_m >= 0)
+                    {
+                        const float eym = __expf(fminf(v[cell_m] + b[cell_m], 30.0f));
+                        dym = eym * inv_n;
+                        my_loss += eym;
+                        atomicAdd(&sdb[4 * 64 + cell_m], dym);
+                    }
                 }
                 for (int c = 0; c < 8; ++c)
                 {
                     float g[8];
-                    for (int i = 0; i < 8; ++i) g[i] = (8 * c + i == cell) ? dy : 0.0f;
+                    for (int i = 0; i < 8; ++i) g[i] = (8 * c + i == cell) ? dy : ((8 * c + i == cell_m) ? dym : 0.0f);
                     store8(DY, 128, row, 8 * c, g);
                 }
             }
@@ -496,13 +515,52 @@ cudaError_t launch_mlp_infer(const MlpDev& net, const float4* q_pos, const float
 }
 
 cudaError_t launch_mlp_train(const MlpDev& net, const float4* r_pos, const float4* r_wr, const float4* r_dir,
-                             const float4* r_rad, const int* count, int n_direct, int n_train, float* grad,
+                             const float4* r_rad, const int* count, int n_direct, int n_train, int offset, float* grad,
                              float* loss_sum, unsigned* err, int sms, cudaStream_t s)
 {
     const int tiles = (n_train + 127) / 128;
     const int grid = std::max(1, std::min(sms, tiles));
-    k_mlp_train<<<grid, 128, mlpk::TR_SMEM, s>>>(net, r_pos, r_wr, r_dir, r_rad, count, n_direct, n_train, grad,
-                                                  loss_sum, err);
+    k_mlp_train<<<grid, 128, mlpk::TR_SMEM, s>>>(net, r_pos, r_wr, r_dir, r_rad, count, n_direct, n_train, offset,
+                                                  grad, loss_sum, err);
+    return cudaGetLastError();
+}
+
+// Output biases start at the log of the first frame's mean record radiance (a
+// data-dependent start: the outputs predict log mean radiance, far from zero,
+// and the sampled distribution only depends on differences between outputs).
+__global__ void k_mlp_bias_start(float* __restrict__ w32, const float4* __restrict__ r_rad, const int* __restrict__ count)
+{
+    __shared__ float ssum[256];
+    __shared__ int scnt[256];
+    const int n = *count;
+    const int use = min(n, 65536);
+    const int stride = use > 0 ? max(1, n / use) : 1;
+    float sum = 0.0f;
+    int cnt = 0;
+    for (int i = threadIdx.x; i < use; i += blockDim.x)
+    {
+        sum += fmaxf(r_rad[(long long)i * stride % n].y, 0.0f);
+        ++cnt;
+    }
+    ssum[threadIdx.x] = sum;
+    scnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o)
+        {
+            ssum[threadIdx.x] += ssum[threadIdx.x + o];
+            scnt[threadIdx.x] += scnt[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 64 && scnt[0] > 0)
+        w32[mlp_b_offset(AR_MLP_LAYERS - 1) + threadIdx.x] = __logf(ssum[0] / (float)scnt[0] + 1.0e-6f);
+}
+
+cudaError_t launch_mlp_bias_start(float* w32, const float4* r_rad, const int* count, cudaStream_t s)
+{
+    k_mlp_bias_start<<<1, 256, 0, s>>>(w32, r_rad, count);
     return cudaGetLastError();
 }
 
@@ -647,8 +705,8 @@ extern "C" ar_status ar_diag_umma_gemm(int device, const uint16_t* a, const uint
     return st ? AR_ERR_DEVICE : AR_OK;
 }
 
-extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* in6, const float* dirs, const float* lum,
-                                 int n, float* logits, float* grad, float* loss)
+extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* in6, const float* dirs, const float* nrm,
+                                 const float* lum, int n, float* logits, float* grad, float* loss)
 {
     using namespace ar;
     static_assert(AR_MLP_PARAMS == 25920, "parameter block size");
@@ -659,7 +717,10 @@ extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* i
     {
         const float* x = in6 + 6 * (size_t)i;
         pos[i] = make_float4(x[0], x[1], x[2], 1.0f);
-        wr[i] = make_float4(2.0f * x[3] - 1.0f, 2.0f * x[4] - 1.0f, 2.0f * x[5] - 1.0f, 0.0f);
+        // no normal: one pointing away from the record direction (no mirrored record)
+        const V3 dn = nrm ? v3(nrm[3 * (size_t)i], nrm[3 * (size_t)i + 1], nrm[3 * (size_t)i + 2])
+                          : -v3(dirs[3 * (size_t)i], dirs[3 * (size_t)i + 1], dirs[3 * (size_t)i + 2]);
+        wr[i] = make_float4(2.0f * x[3] - 1.0f, 2.0f * x[4] - 1.0f, 2.0f * x[5] - 1.0f, mlp_pack_normal(normalize(dn)));
         dir[i] = make_float4(dirs[3 * (size_t)i], dirs[3 * (size_t)i + 1], dirs[3 * (size_t)i + 2], 0.0f);
         rad[i] = make_float4(0.0f, lum[i], 0.0f, 0.0f);
     }
@@ -699,7 +760,7 @@ extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* i
     if (e == cudaSuccess) e = mlp_prepare_kernels();
     if (e == cudaSuccess) e = launch_mlp_to_bf16(w32, wbf, 0);
     if (e == cudaSuccess) e = launch_mlp_infer(net, dp, dw, nullptr, nullptr, n, nullptr, dlog, derr, sms, 0);
-    if (e == cudaSuccess) e = launch_mlp_train(net, dp, dw, dd, dr, nullptr, n, n, dgrad, dloss, derr, sms, 0);
+    if (e == cudaSuccess) e = launch_mlp_train(net, dp, dw, dd, dr, nullptr, n, n, 0, dgrad, dloss, derr, sms, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     unsigned herr = 0;
     if (e == cudaSuccess) e = cudaMemcpy(logits, dlog, (size_t)n * 64 * 4, cudaMemcpyDeviceToHost);

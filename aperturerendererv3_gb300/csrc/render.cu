@@ -235,6 +235,45 @@ __global__ void __launch_bounds__(AR_BLOCK) k_extend(DevScene sc, PathState ps, 
     }
 }
 
+// MLP guide: the network inputs (position and reflected view direction) of
+// the queued paths that hit a surface at one of their first AR_MLP_MAX_NDD
+// non-delta vertices, outside media; those paths are appended to `list` (the
+// inference queue) and flagged in q_pos.w, the others flagged off.
+__global__ void __launch_bounds__(AR_BLOCK) k_mlp_query(DevScene sc, PathState ps, const int* __restrict__ queue,
+                                                      const int* __restrict__ counter, int* list, int* list_counter)
+{
+    const int n = *counter;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride)
+    {
+        const int q = base + lane_id();
+        bool want = false;
+        int p = 0;
+        if (q < n)
+        {
+            p = queue[q];
+            const int slot = ps.hit_slot[p];
+            const int ndd = (int)(ps.depths[p] >> 16);
+            want = slot >= 0 && ndd < AR_MLP_MAX_NDD && (ps.flags[p] & 1u) == 0u;
+            if (want)
+            {
+                const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
+                Hit h;
+                hit_context(sc, slot, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), ps.hit_t[p], &h);
+                const V3 wr = reflect(v3(rd.x, rd.y, rd.z), h.nrm);
+                ps.q_pos[p] = make_float4(h.pos.x, h.pos.y, h.pos.z, 1.0f);
+                ps.q_wr[p] = make_float4(wr.x, wr.y, wr.z, 0.0f);
+            }
+            else
+            {
+                ps.q_pos[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+        }
+        const int slot_out = warp_append_slot(list_counter, want);
+        if (want) list[slot_out] = p;
+    }
+}
+
 // ---------------------------------------------------------------- shade
 struct ShadeParams
 {
@@ -242,6 +281,7 @@ struct ShadeParams
     int max_depth;
     int frame;    // frame index of the wave (guided rendering: mixture probability)
     float* grad;  // replay adjoint: float32 texel gradients (3 per texel)
+    int mlp_ready;  // MLP guide: the network has trained long enough to replace the voxel probes
 };
 
 // CollectRadiance (core/render/render.cuh:353-432) on the path's collection
@@ -275,7 +315,7 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
             ps.pg_dir[ndd * cap + p] = make_float4(nextDir.x, nextDir.y, nextDir.z, w);
             ps.pg_loc[ndd * cap + p] = make_float4(hitLoc.x, hitLoc.y, hitLoc.z, 1.0f);
             const V3 vd = reflect(rayDir, hitNrm);
-            ps.pg_vdir[ndd * cap + p] = make_float4(vd.x, vd.y, vd.z, 0.0f);
+            ps.pg_vdir[ndd * cap + p] = make_float4(vd.x, vd.y, vd.z, mlp_pack_normal(hitNrm));
         }
     }
     if (advance)
@@ -294,7 +334,7 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
     }
 }
 
-template <bool GUIDE, bool ADJ>
+template <int GUIDE, bool ADJ>
 __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
                                                   const int* __restrict__ counter, int* next_queue, int* next_counter,
                                                   int* shadow_counter, ShadeParams prm)
@@ -404,12 +444,62 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
             const Probe* probe = nullptr;
             V3 maskq = v3(1.0f, 1.0f, 1.0f);
             float pgProb = 0.0f;
+            bool mlp_on = false;           // GUIDE == 2: this vertex mixes in the network's distribution
+            uint32_t qw[16];               // its 64 quantised cell weights
+            float q_total = 1.0f;
             if constexpr (GUIDE)
             {
                 const float4 mq = ps.maskq[p];
                 maskq = v3(mq.x, mq.y, mq.z);
                 pgProb = guide_probability(prm.frame);
-                if (h.hit && !S.delta && !S.pure_light && !media.inside && sc.guide.probe_count > 0)
+                const bool eligible = h.hit && !S.delta && !S.pure_light && !media.inside;
+                if constexpr (GUIDE == 2)
+                {
+                    if (eligible && prm.mlp_ready && ps.q_pos[p].w > 0.0f)
+                    {
+                        const uint4* src = reinterpret_cast<const uint4*>(ps.q_dist + 64 * (size_t)p);
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            const uint4 u = src[k];
+                            qw[4 * k] = u.x;
+                            qw[4 * k + 1] = u.y;
+                            qw[4 * k + 2] = u.z;
+                            qw[4 * k + 3] = u.w;
+                        }
+                        const uint8_t* q = reinterpret_cast<const uint8_t*>(qw);
+                        q_total = mlp_total(q);
+                        mlp_on = true;
+                        const float pB = S.pdf;
+                        const float pP = mlp_hemisphere_pdf(q, 1.0f / q_total, S.next_dir, h.nrm);
+                        if (pB > 1.0e-12f && pP > 1.0e-12f)
+                        {
+                            if (R() < pgProb)
+                            {
+                                const GuideSample g = mlp_sample_hemisphere(q, q_total, R, h.nrm);
+                                if (dot(g.dir, h.nrm) > 1.0e-12f)
+                                {
+                                    const float pBs = bsdf_pdf(lb, mat, h.nrm, rayD, g.dir);
+                                    S.next_dir = g.dir;
+                                    S.brdf = eval_bsdf_cos(lambda, lb, mat, rayD, g.dir, h, media);
+                                    S.pdf = (1.0f - pgProb) * fmaxf(pBs, 1.0e-12f) + pgProb * g.pdf;
+                                }
+                                else
+                                {
+                                    mlp_on = false;
+                                }
+                            }
+                            else
+                            {
+                                S.pdf = (1.0f - pgProb) * pB + pgProb * pP;
+                            }
+                        }
+                        else
+                        {
+                            mlp_on = false;
+                        }
+                    }
+                }
+                if (!mlp_on && eligible && sc.guide.probe_count > 0)
                 {
                     const VoxelKey key = voxel_key(h.pos, reflect(rayD, h.nrm), sc.guide.inv_unit);
                     const int idx = guide_lookup(sc.guide, guide_pack(key));
@@ -574,6 +664,10 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                                     if (probe)
                                         pBsdf = (1.0f - pgProb) * pBsdf +
                                                 pgProb * octahedron_hemisphere_pdf(*probe, L, h.nrm, maskq);
+                                    if (mlp_on)
+                                        pBsdf = (1.0f - pgProb) * pBsdf +
+                                                pgProb * mlp_hemisphere_pdf(reinterpret_cast<const uint8_t*>(qw),
+                                                                            1.0f / q_total, L, h.nrm);
                                 }
                                 const float misW = power_heuristic(pLight, pBsdf);
                                 vUn = mask * (contribution * misW) * d65;
@@ -761,6 +855,11 @@ __global__ void k_guide_emit(DevScene sc, PathState ps, int n, GuideSamples gs)
         gs.radiance[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
         gs.dir[slot] = make_float4(d.x, d.y, d.z, 0.0f);
         gs.key[slot] = packed;
+        if (gs.pos)
+        {
+            gs.pos[slot] = make_float4(l.x, l.y, l.z, 1.0f);
+            gs.wr[slot] = make_float4(vd.x, vd.y, vd.z, vd.w);  // w: the packed surface normal
+        }
     }
 }
 
@@ -854,6 +953,11 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     prm.max_depth = rl.max_depth;
     prm.frame = rl.first_frame + (int)(first_path / ((long long)rl.width * rl.height));
     prm.grad = rl.grad;
+    prm.mlp_ready = rl.mlp_ready;
+    MlpDev net;
+    net.wbf = c.d_mlp_wbf;
+    net.w32 = c.d_mlp_w32;
+    net.box = c.mlp_box;
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
@@ -865,14 +969,26 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         }
         {
             StageScope st(c, ST_SHADE);
-            if (rl.guide)
-                k_shade<true, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
-                                                                 c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
+            if (rl.guide == 2 && rl.mlp_ready)
+            {
+                // network inference for every queued hit (tensor cores), before shading
+                cudaMemsetAsync(&cnt[3], 0, sizeof(int), s);
+                k_mlp_query<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], &cnt[cur], c.d_mlp_list, &cnt[3]);
+                launch_mlp_infer(net, c.ps.q_pos, c.ps.q_wr, c.d_mlp_list, &cnt[3], 0, c.ps.q_dist, nullptr, c.d_err,
+                                 sms, s);
+                L += 2;
+            }
+            if (rl.guide == 2)
+                k_shade<2, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
+                                                              c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
+            else if (rl.guide)
+                k_shade<1, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
+                                                              c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
             else if (rl.adjoint)
-                k_shade<false, true><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
+                k_shade<0, true><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
                                                                  c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
             else
-                k_shade<false, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
+                k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
                                                                   c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
         }
         {
@@ -919,13 +1035,14 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     prm.max_depth = rl.max_depth;
     prm.frame = rl.first_frame;
     prm.grad = nullptr;
+    prm.mlp_ready = 0;
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
         cudaMemsetAsync(&cnt[nxt], 0, sizeof(int), s);
         cudaMemsetAsync(&cnt[2], 0, sizeof(int), s);
         k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[cur], err);
-        k_shade<false, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[cur], wb.queue[nxt], &cnt[nxt],
+        k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[cur], wb.queue[nxt], &cnt[nxt],
                                                    &cnt[2], prm);
         k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[2], err);
     }

@@ -227,7 +227,7 @@ class SceneRenderer:
 
     def params(self, size, cameraOrigin, cameraDirection, sampleNum, fov=60.0, max_depth=1000, use_nee=True,
                seed=GLOBAL_SEED, first_frame=0, wave_paths=0, profile=False, guide=0,
-               guide_unit=0.0) -> ArRenderParams:
+               guide_unit=0.0, guide_train_steps=0) -> ArRenderParams:
         p = ArRenderParams()
         p.width, p.height = int(size[0]), int(size[1])
         p.spp = int(sampleNum)
@@ -242,21 +242,24 @@ class SceneRenderer:
         p.profile = int(profile)  # 1: stage times, 2: traversal counters, 3: both
         p.guide = int(guide)
         p.guide_unit = float(guide_unit)
+        p.guide_train_steps = int(guide_train_steps)
         return p
 
     def Render(self, size, cameraOrigin, cameraDirection, sampleNum: int = 1024, *, fov: float = 60.0,
                max_depth: int = 1000, use_nee: bool = True, seed: int = GLOBAL_SEED, first_frame: int = 0,
                per_sample: bool = False, wave_paths: int = 0, profile: bool = False, guide: int = 0,
-               guide_unit: float = 0.0):
+               guide_unit: float = 0.0, guide_train_steps: int = 0):
         """Mean linear XYZ per pixel, shape (height, width, 3), float64.
 
         With per_sample=True also returns every sample's XYZ, shape
         (sampleNum, height, width, 3), float32.  guide=1 turns on the voxel
         path guide: frames render one sample per pixel each and the probes learn
-        after every frame (and persist across calls until ResetGuiding)."""
+        after every frame (and persist across calls until MarkNeedResetGuiding);
+        guide=2 adds the tensor-core MLP guide, trained online on the same
+        records and sampled instead of the probes once it has trained."""
         self._build()
         p = self.params(size, cameraOrigin, cameraDirection, sampleNum, fov, max_depth, use_nee, seed, first_frame,
-                        wave_paths, profile, guide, guide_unit)
+                        wave_paths, profile, guide, guide_unit, guide_train_steps)
         w, h = p.width, p.height
         out = np.zeros((h, w, 3), np.float64)
         ps = np.zeros((p.spp, h, w, 3), np.float32) if per_sample else None
@@ -325,6 +328,12 @@ class SceneRenderer:
         n, cap = C.c_int32(), C.c_int32()
         check(self._ctx, self._lib.ar_guide_stats(self._ctx, C.byref(n), C.byref(cap)))
         return n.value, cap.value
+
+    def mlp_stats(self) -> tuple[int, float]:
+        """MLP guide: (training steps taken, loss sum of the last step)."""
+        n, loss = C.c_int32(), C.c_float()
+        check(self._ctx, self._lib.ar_guide_mlp_stats(self._ctx, C.byref(n), C.byref(loss)))
+        return n.value, loss.value
 
     def render_profile(self) -> dict:
         prof = _lib.ArRenderProfile()

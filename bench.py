@@ -183,6 +183,53 @@ def guided_extra(r, w, cam, steps: int) -> dict:
             "ms_per_step": float(np.mean(ms)), "steps": steps, "probes": n_probes}
 
 
+def rel_mse(img, ref) -> float:
+    """mean over pixels of sum_c (I - I_ref)^2 / (I_ref^2 + 1e-2)."""
+    return float((((img - ref) ** 2) / (ref ** 2 + 1e-2)).sum(-1).mean())
+
+
+def guide_compare_extra(r, w, cam, ref_spp: int = 2048, chunk: int = 4) -> dict:
+    """Voxel guide vs MLP guide at equal wall time, each learning from scratch
+    (training included), scored by rel-MSE against a converged plain render of
+    the same view (ref_spp samples per pixel, FP64 accumulation, disjoint
+    sample streams).  Both render in calls of `chunk` frames; the voxel guide
+    renders the workload's spp, the MLP guide as many chunks as fit in the
+    voxel guide's wall time."""
+    import numpy as np
+    size, spp, depth = w["size"], w["spp"], w["depth"]
+    kw = dict(fov=cam["fov"], max_depth=depth)
+    ref = r.Render(size, cam["origin"], cam["direction"], ref_spp, first_frame=1 << 20, **kw)
+    ref_ms = r.last_render_stats()[0]
+    out = {"reference": {"spp": ref_spp, "ms": ref_ms, "kind": "plain render, FP64 accumulation"}}
+
+    def run(mode, frames=None, budget=None, steps=0):
+        r.MarkNeedResetGuiding()
+        acc, n = None, 0
+        t0 = time.perf_counter()
+        while frames is None or n < frames:
+            img = r.Render(size, cam["origin"], cam["direction"], chunk, guide=mode, first_frame=n,
+                           guide_train_steps=steps, **kw)
+            acc = img * chunk if acc is None else acc + img * chunk
+            n += chunk
+            if budget is not None and time.perf_counter() - t0 >= budget:
+                break
+        return acc / n, n, time.perf_counter() - t0
+
+    vox, n_vox, t_vox = run(1, frames=spp)
+    out["voxel"] = {"spp": n_vox, "s": t_vox, "rel_mse": rel_mse(vox, ref)}
+    for key, steps_per_frame in (("mlp", 8), ("mlp_32_steps", 32)):
+        mlp, n_mlp, t_mlp = run(2, budget=t_vox, steps=steps_per_frame)
+        steps, loss = r.mlp_stats()
+        out[key] = {"spp": n_mlp, "s": t_mlp, "rel_mse": rel_mse(mlp, ref), "train_steps": steps,
+                    "steps_per_frame": steps_per_frame, "last_loss_sum": loss}
+    r.MarkNeedResetGuiding()
+    plain, n_plain, t_plain = run(0, budget=t_vox)
+    out["plain"] = {"spp": n_plain, "s": t_plain, "rel_mse": rel_mse(plain, ref)}
+    out["mlp_over_voxel"] = out["mlp"]["rel_mse"] / out["voxel"]["rel_mse"]
+    out["epsilon"] = 1e-2
+    return out
+
+
 def adjoint_extra(device: int, steps: int) -> dict:
     """Differentiable-rendering workload: the triangle Cornell box with 8 albedo
     textures of 512^2 RGB texels (U[0.2, 0.8], seed 11) as parameters, target
@@ -392,6 +439,7 @@ def main() -> None:
     if not args.no_extras:
         extras = {}
         for name, fn in (("guided_voxel", lambda: guided_extra(r, w, cam, 3)),
+                         ("guide_compare", lambda: guide_compare_extra(r, w, cam)),
                          ("adjoint", lambda: adjoint_extra(local, 3)),
                          ("bvh_stress", lambda: bvh_stress_extra(local, 5))):
             try:

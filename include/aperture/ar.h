@@ -94,8 +94,9 @@ typedef struct ar_render_params
     int32_t first_frame;     /* frame index of the first sample */
     int32_t wave_paths;      /* paths in flight per wave, 0 = automatic */
     int32_t profile;         /* 1 = per-stage device times, 2 = traversal counters, 3 = both */
-    int32_t guide;           /* AR_GUIDE_NONE or AR_GUIDE_VOXEL (SceneSetting::bUsePathGuiding_) */
+    int32_t guide;           /* AR_GUIDE_NONE, AR_GUIDE_VOXEL (SceneSetting::bUsePathGuiding_) or AR_GUIDE_MLP */
     float guide_unit;        /* voxel size of the guide (0 = 0.05, PATH_GUIDING_RESOLUTION_UNIT) */
+    int32_t guide_train_steps; /* AR_GUIDE_MLP: Adam steps after each frame (0 = 8) */
 } ar_render_params;
 
 /* Path guiding modes.  With AR_GUIDE_VOXEL, ar_render renders one frame (one
@@ -104,6 +105,14 @@ typedef struct ar_render_params
  * persist across ar_render calls until ar_guide_reset or a scene rebuild. */
 #define AR_GUIDE_NONE 0
 #define AR_GUIDE_VOXEL 1
+/* AR_GUIDE_MLP (no reference counterpart): the voxel probes learn as with
+ * AR_GUIDE_VOXEL and, after every frame, a small network (12-band encoding of
+ * position and reflected direction, 5 layers of width 64, BF16 tensor-core
+ * kernels with FP32 accumulation, one Adam step at lr 1e-3 on up to 65,536 of
+ * the frame's radiance records) trains alongside; once it has trained for 4
+ * frames, the guide samples the network's 64-cell directional distribution
+ * instead of the probes. */
+#define AR_GUIDE_MLP 2
 
 /* Per-stage profile of the last ar_render with params->profile = 1. */
 typedef struct ar_render_profile
@@ -201,6 +210,8 @@ ar_status ar_last_render_profile(ar_ctx* ctx, ar_render_profile* out);
 ar_status ar_guide_reset(ar_ctx* ctx, int32_t* n_probes);
 /* Number of probes the voxel guide holds. */
 ar_status ar_guide_stats(ar_ctx* ctx, int32_t* n_probes, int32_t* capacity);
+/* MLP guide: training steps taken and the loss sum of the last one. */
+ar_status ar_guide_mlp_stats(ar_ctx* ctx, int32_t* steps, float* last_loss);
 
 ar_status ar_get_error_word(ar_ctx* ctx, uint32_t* word);
 ar_status ar_clear_error_word(ar_ctx* ctx);
@@ -230,12 +241,15 @@ int ar_abi_version(void);
  * and backward passes on given inputs.  params: AR_MLP_PARAMS floats (per
  * layer W[64][in] row-major then b[64]; in = 144 for layer 0, 64 after).
  * in6: n x 6 encoded inputs in [0, 1] (position in the scene box, then
- * (reflected direction + 1) / 2); dirs: n x 3 record directions; lum: n record
+ * (reflected direction + 1) / 2); dirs: n x 3 record directions; nrm: n x 3
+ * surface normals (NULL: no mirrored zero-radiance records); lum: n record
  * radiances (CIE Y).  Outputs (host): logits n x 64, grad AR_MLP_PARAMS
- * (d mean loss / d params), loss (sum over records). */
+ * (d mean loss / d params), loss (sum over records of exp(y) - Y y, y the
+ * output of the record direction's cell, plus exp(y') at the cell of the
+ * direction mirrored below the surface). */
 #define AR_MLP_PARAMS 25920
-ar_status ar_diag_mlp(int device, const float* params, const float* in6, const float* dirs, const float* lum, int n,
-                      float* logits, float* grad, float* loss);
+ar_status ar_diag_mlp(int device, const float* params, const float* in6, const float* dirs, const float* nrm,
+                      const float* lum, int n, float* logits, float* grad, float* loss);
 ar_status ar_diag_umma_gemm(int device, const uint16_t* a, const uint16_t* b, int a_mn, int b_mn, int n, int k,
                             int swap, float* d);
 

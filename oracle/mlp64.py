@@ -3,8 +3,9 @@
 TEST INFRASTRUCTURE ONLY.  The network is the one the GPU trains
 (aperturerendererv3_gb300/csrc/ar_mlp.h): a 12-band sin/cos encoding of six
 inputs in [0, 1] (144 features), then 144 -> 64 -> 64 -> 64 -> 64 -> 64 with
-ReLU between layers; loss per record 0.5 (y[cell(dir)] - log(Y + 1e-3))^2,
-averaged over the records.  `cell` is the 8 x 8 cell of the equal-area sphere
+ReLU between layers; loss per record exp(y) - Y y at the output of the
+record direction's cell (Poisson log-likelihood, minimised by exp(y) = mean
+Y), averaged over the records.  `cell` is the 8 x 8 cell of the equal-area sphere
 map the voxel probes use (core/guiding/octahedron.cuh:87-145, restated here).
 
 With bf16=True the oracle rounds where the tensor-core kernels hold bf16
@@ -129,18 +130,38 @@ def forward(params, in6, bf16_ops=True):
     return y, acts
 
 
-def loss_and_grad(params, in6, dirs, lum, bf16_ops=True):
-    """(logits, loss sum, d mean-loss / d params) in float64."""
+def mirrored_cells(dirs, nrm, c):
+    """Cell of each direction mirrored below the surface (-1: none, or the same cell)."""
+    d = np.asarray(dirs, np.float64)
+    d = d / np.linalg.norm(d, axis=1, keepdims=True)
+    nn = np.asarray(nrm, np.float64)
+    nn = nn / np.linalg.norm(nn, axis=1, keepdims=True)
+    dn = (d * nn).sum(1)
+    m = d - 2.0 * dn[:, None] * nn
+    cm = cell(m)
+    cm[(dn <= 0) | (cm == c)] = -1
+    return cm
+
+
+def loss_and_grad(params, in6, dirs, lum, bf16_ops=True, nrm=None):
+    """(logits, loss sum, d mean-loss / d params) in float64.  With normals,
+    each record also adds a zero-radiance record at its mirrored cell."""
     Ws, bs = unpack(params, bf16_ops)
     r = bf16 if bf16_ops else (lambda a: a)
     y, acts = forward(params, in6, bf16_ops)
     n = len(y)
     c = cell(dirs)
-    t = np.log(np.maximum(np.asarray(lum, np.float64), 0.0) + 1e-3)
-    yc = y[np.arange(n), c]
-    loss = float(0.5 * ((yc - t) ** 2).sum())
+    t = np.maximum(np.asarray(lum, np.float64), 0.0)
+    yc = np.minimum(y[np.arange(n), c], 30.0)
+    loss = float((np.exp(yc) - t * yc).sum())
     dy = np.zeros_like(y)
-    dy[np.arange(n), c] = (yc - t) / n
+    dy[np.arange(n), c] = (np.exp(yc) - t) / n
+    if nrm is not None:
+        cm = mirrored_cells(dirs, nrm, c)
+        k = np.flatnonzero(cm >= 0)
+        em = np.exp(np.minimum(y[k, cm[k]], 30.0))
+        loss += float(em.sum())
+        dy[k, cm[k]] += em / n
     grad = np.zeros(PARAMS)
     g = dy
     for l in range(4, -1, -1):

@@ -51,3 +51,33 @@ def test_guide_on_terrain_mesh(cuda_device):
     assert np.all(np.isfinite(img)) and img.mean() > 0
     assert r.guide_stats()[0] > 0
     assert r.error_word() == 0
+
+
+@pytest.mark.parametrize("name,objs,mesh,cam", scenes())
+def test_mlp_guide_trains_and_stays_unbiased(cuda_device, name, objs, mesh, cam):
+    """guide=2: the network trains after every frame (eight Adam steps), takes over
+    from the voxel probes after its warm-up, and the image converges to the
+    same mean as unguided rendering."""
+    size, spp = (64, 64), 256
+    r = SceneRenderer(objs, mesh=mesh)
+    plain = r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=16)
+    guided = r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=16, guide=2)
+    steps, loss = r.mlp_stats()
+    assert steps == 8 * spp  # eight Adam steps per frame
+    assert np.isfinite(loss) and loss > 0
+    assert r.error_word() == 0
+    assert np.all(np.isfinite(guided))
+    m_plain, m_guided = plain[..., 1].mean(), guided[..., 1].mean()
+    assert abs(m_guided - m_plain) < 0.03 * m_plain, (m_plain, m_guided)
+    r.MarkNeedResetGuiding()
+    assert r.mlp_stats()[0] == 0
+
+
+def test_mlp_guide_on_terrain(cuda_device):
+    objs, mesh = configs.terrain_scene(res=96, n_spheres=8, seed=7)
+    cam = configs.TERRAIN_CAMERA
+    r = SceneRenderer(objs, mesh=mesh)
+    img = r.Render((96, 54), cam["origin"], cam["direction"], 16, fov=cam["fov"], max_depth=16, guide=2)
+    assert np.all(np.isfinite(img)) and img.mean() > 0
+    assert r.mlp_stats()[0] == 8 * 16
+    assert r.error_word() == 0

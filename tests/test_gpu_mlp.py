@@ -40,7 +40,7 @@ def test_tensor_core_descriptors(cuda_device, a_mn, b_mn, n, k):
     assert np.abs(d - ref).max() <= 1e-5 * np.abs(ref).max()
 
 
-def run_gpu(params, in6, dirs, lum):
+def run_gpu(params, in6, dirs, lum, nrm=None):
     n = len(in6)
     logits = np.zeros((n, 64), np.float32)
     grad = np.zeros(mlp64.PARAMS, np.float32)
@@ -49,8 +49,9 @@ def run_gpu(params, in6, dirs, lum):
     x = np.ascontiguousarray(in6, np.float32)
     d = np.ascontiguousarray(dirs, np.float32)
     y = np.ascontiguousarray(lum, np.float32)
-    rc = _lib.load().ar_diag_mlp(0, p.ctypes.data, x.ctypes.data, d.ctypes.data, y.ctypes.data, n, logits.ctypes.data,
-                                 grad.ctypes.data, loss.ctypes.data)
+    nn = None if nrm is None else np.ascontiguousarray(nrm, np.float32)
+    rc = _lib.load().ar_diag_mlp(0, p.ctypes.data, x.ctypes.data, d.ctypes.data, None if nn is None else nn.ctypes.data,
+                                 y.ctypes.data, n, logits.ctypes.data, grad.ctypes.data, loss.ctypes.data)
     assert rc == 0
     return logits.astype(np.float64), float(loss[0]), grad.astype(np.float64)
 
@@ -59,8 +60,8 @@ def agg(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
-@pytest.mark.parametrize("n", [300, 5000])
-def test_forward_backward_against_fp64_oracle(cuda_device, n):
+@pytest.mark.parametrize("n,with_normals", [(300, False), (5000, False), (5000, True)])
+def test_forward_backward_against_fp64_oracle(cuda_device, n, with_normals):
     rng = np.random.default_rng(n)
     params = mlp64.init_params(3).astype(np.float64)
     # exercise the biases and a full-scale output layer too
@@ -73,8 +74,15 @@ def test_forward_backward_against_fp64_oracle(cuda_device, n):
     dirs = rng.standard_normal((n, 3)).astype(np.float32)
     dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
     lum = rng.gamma(0.5, 2.0, n).astype(np.float32)
-    y_gpu, loss_gpu, g_gpu = run_gpu(params, in6, dirs, lum)
-    y_ref, loss_ref, g_ref = mlp64.loss_and_grad(params, in6, dirs, lum, bf16_ops=True)
+    nrm = None
+    if with_normals:
+        # normals on the records' side of the surface, octahedrally quantised as the renderer stores them
+        nrm = rng.standard_normal((n, 3))
+        nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+        nrm *= np.sign((nrm * dirs).sum(1, keepdims=True) + 1e-12)
+        nrm = nrm.astype(np.float32)
+    y_gpu, loss_gpu, g_gpu = run_gpu(params, in6, dirs, lum, nrm)
+    y_ref, loss_ref, g_ref = mlp64.loss_and_grad(params, in6, dirs, lum, bf16_ops=True, nrm=nrm)
     assert agg(y_gpu, y_ref) < 5e-3, agg(y_gpu, y_ref)
     assert abs(loss_gpu - loss_ref) < 5e-3 * loss_ref
     for l, ind in enumerate(mlp64.DIMS):
@@ -83,6 +91,6 @@ def test_forward_backward_against_fp64_oracle(cuda_device, n):
         assert agg(g_gpu[sw], g_ref[sw]) < 2e-2, (l, agg(g_gpu[sw], g_ref[sw]))
         assert agg(g_gpu[sb], g_ref[sb]) < 2e-2, (l, agg(g_gpu[sb], g_ref[sb]))
     # against the exact FP64 network: bf16 operands cost a few per cent at most
-    y64, _, g64 = mlp64.loss_and_grad(params, in6, dirs, lum, bf16_ops=False)
+    y64, _, g64 = mlp64.loss_and_grad(params, in6, dirs, lum, bf16_ops=False, nrm=nrm)
     assert agg(y_gpu, y64) < 3e-2
     assert agg(g_gpu, g64) < 1e-1
