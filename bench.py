@@ -330,7 +330,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None, help="WxH override (small profiling cases)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
-    ap.add_argument("--guide", type=int, default=0, choices=[0, 1], help="1: voxel path guide on")
+    ap.add_argument("--guide", type=int, default=0, choices=[0, 1, 2], help="1: voxel path guide, 2: MLP guide")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the guided, adjoint and BVH-stress measurements reported beside the headline")
     args = ap.parse_args()
@@ -420,7 +420,7 @@ def main() -> None:
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": args.workload, "width": size[0], "height": size[1], "spp": spp, "max_depth": depth,
-                   "guide": "voxel" if args.guide else "none", "paths_per_step": samples, "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "guide": ["none", "voxel", "mlp"][args.guide], "paths_per_step": samples, "parallelism": "replicas" if world > 1 else "single-gpu",
                    "l2": "inputs larger than L2 (path state ~170 B x 2M paths in flight)"},
         "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 100,
                 "d2h_bytes_per_step": size[0] * size[1] * 3 * 8},
