@@ -44,6 +44,11 @@ class ArObject(C.Structure):
                 ("rotation_deg", F3), ("v0", F3), ("v1", F3), ("v2", F3)]
 
 
+class ArMedium(C.Structure):
+    _fields_ = [("box_lo", F3), ("box_hi", F3), ("sigma_t", C.c_float), ("albedo", C.c_float), ("g", C.c_float),
+                ("emission", C.c_float)]
+
+
 class ArRenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("cam_origin", F3), ("cam_dir", F3), ("fov_deg", C.c_float), ("use_nee", C.c_int32),
@@ -55,6 +60,7 @@ class ArRenderParams(C.Structure):
 GUIDE_NONE = 0
 GUIDE_VOXEL = 1
 GUIDE_MLP = 2
+SDF_SPHERE, SDF_BOX, SDF_TORUS = 0, 1, 2
 
 
 class ArRenderProfile(C.Structure):
@@ -76,7 +82,8 @@ EXPORTED = [
     "ar_get_error_word", "ar_clear_error_word", "ar_last_error", "ar_host_rgb_encode", "ar_host_lambda_encode",
     "ar_host_sample_lambda", "ar_host_trace_closest", "ar_host_guide_eval", "ar_abi_version",
     "ar_scene_set_textures", "ar_scene_set_mesh_uv", "ar_scene_update_texels", "ar_scene_texel_count", "ar_adjoint",
-    "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats",
+    "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats", "ar_scene_set_sdf_union", "ar_scene_set_medium",
+    "ar_adjoint_medium",
 ]
 
 _lib = None
@@ -132,6 +139,9 @@ def load() -> C.CDLL:
         "ar_diag_umma_gemm": (C.c_int, [C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp]),
         "ar_diag_mlp": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp]),
         "ar_guide_mlp_stats": (C.c_int, [vp, P(C.c_int32), P(C.c_float)]),
+        "ar_scene_set_sdf_union": (C.c_int, [vp, vp, C.c_int, C.c_float, C.c_int32]),
+        "ar_scene_set_medium": (C.c_int, [vp, P(ArMedium)]),
+        "ar_adjoint_medium": (C.c_int, [vp, P(ArRenderParams), vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -15,6 +15,10 @@
   textured_cornell()    the triangle Cornell box with a 512^2 albedo texture on
                         every wall and box (U[0.2, 0.8] from a seed): the
                         differentiable-rendering workload.
+  combined_scene()      the terrain plus 32 smooth-union SDF primitives (spheres,
+                        boxes, tori; radii U[0.05, 0.3]) and a homogeneous
+                        medium (sigma_t 0.5, albedo 0.8, HG g 0.3) over it: the
+                        large combined workload.
   terrain_scene()       2048^2 fBm heightfield (8 octaves, amplitude 0.2), 64
                         emissive spheres, a distant sun sphere, GGX materials
                         with roughness U[0.05, 0.6].
@@ -26,8 +30,8 @@ import math
 
 import numpy as np
 
-from .scene import Material, SceneObject, TriangleMesh
-from ._lib import OBJECT_CUBE, OBJECT_SPHERE
+from .scene import Material, Medium, SceneObject, SdfUnion, TriangleMesh
+from ._lib import OBJECT_CUBE, OBJECT_SPHERE, SDF_BOX, SDF_SPHERE, SDF_TORUS
 
 GREY = (0.73, 0.73, 0.73)
 RED = (0.63, 0.065, 0.05)
@@ -254,3 +258,34 @@ def terrain_scene(res: int = 2048, n_spheres: int = 64, seed: int = 7):
     objs.append(SceneObject((-20.0, 40.0, -30.0), (1.0, 1.0, 1.0), Material.CreateLight((400.0, 380.0, 330.0)),
                             (0.0, 0.0, 0.0), OBJECT_SPHERE))
     return objs, mesh
+
+
+COMBINED_CAMERA = dict(origin=(0.5, 0.55, 1.75), direction=(0.0, -0.3, -1.0), fov=45.0)
+
+
+def sdf_blobs(n: int = 32, seed: int = 5, k: float = 0.08) -> SdfUnion:
+    """n SDF primitives (spheres, boxes, tori; radii U[0.05, 0.3]) above the
+    terrain's unit square, in one smooth union."""
+    rng = np.random.default_rng(seed)
+    prims = []
+    for i in range(n):
+        kind = (SDF_SPHERE, SDF_BOX, SDF_TORUS)[i % 3]
+        r = float(rng.uniform(0.05, 0.3))
+        c = (float(rng.uniform(0.15, 0.85)), float(rng.uniform(0.15, 0.45)), float(rng.uniform(0.15, 0.85)))
+        if kind == SDF_SPHERE:
+            size = (r, 0.0, 0.0)
+        elif kind == SDF_BOX:
+            size = (r, 0.6 * r, 0.8 * r)
+        else:
+            size = (r, 0.3 * r, 0.0)
+        prims.append((kind, c, size))
+    return SdfUnion(prims, k, Material.CreateGGXPureColor((0.8, 0.55, 0.35), 0.3, 0.0, 0.5))
+
+
+COMBINED_MEDIUM = Medium((-0.05, -0.15, -0.05), (1.05, 0.9, 1.05), sigma_t=0.5, albedo=0.8, g=0.3, emission=0.05)
+
+
+def combined_scene(res: int = 2048, n_spheres: int = 64, seed: int = 7):
+    """(objects, mesh, sdf, medium) of the large combined workload."""
+    objs, mesh = terrain_scene(res=res, n_spheres=n_spheres, seed=seed)
+    return objs, mesh, sdf_blobs(), COMBINED_MEDIUM

@@ -24,6 +24,7 @@
 #define AR_PRIM_KIND_TRI 0u
 #define AR_PRIM_KIND_BOX 1u
 #define AR_PRIM_KIND_SPHERE 2u
+#define AR_PRIM_KIND_SDF 3u
 #define AR_PRIM_ID_MASK 0x3fffffffu
 
 struct ar_wide_node

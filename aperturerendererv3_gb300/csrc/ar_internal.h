@@ -108,6 +108,7 @@ struct DevScene
     const int4* tex_info;
     const float* prim_uv;
     int tex_count;
+    BoxMedium medium;  // participating medium (on = 0: none)
 };
 
 // stage ids for the per-stage profile
@@ -185,6 +186,7 @@ struct RenderLaunch
     int adjoint;  // 1: replay pass of ar_adjoint (gradient scatter, no output)
     float* grad;  // replay pass: float32 texel gradients
     int mlp_ready;  // guide 2: sample from the network instead of the voxel probes
+    double* grad_medium;  // replay pass of ar_adjoint_medium: d loss / d (albedo, emission)
 };
 
 struct Ctx
@@ -234,6 +236,14 @@ struct Ctx
     long long grad32_n = 0;
     float* d_adj = nullptr;              // 2 floats per wave path
     int adj_capacity = 0;
+    double* d_grad_medium = nullptr;     // d loss / d (medium albedo, medium emission)
+    // smooth-union SDF object and the participating medium
+    std::vector<float> sdf_prims;        // 8 floats per primitive
+    float sdf_k = 0.0f;
+    int sdf_material = -1;
+    float4* d_sdf = nullptr;
+    SdfUnion sdf{};
+    BoxMedium medium{};
     // wavefront buffers
     PathState ps{};
     ShadowQueue sq{};

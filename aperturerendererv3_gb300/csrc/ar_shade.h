@@ -774,6 +774,71 @@ AR_HD float sphere_light_pdf_omega(const Object& o, float selectProb, V3 sp, V3 
     return area_to_solid_angle_pdf(sp, lp, ln, pATotal);
 }
 
+// ---------------------------------------------------------------- participating medium
+// Homogeneous medium filling an axis-aligned box (no reference counterpart):
+// extinction sigma_t, single-scattering albedo, Henyey-Greenstein phase g, and
+// an emission radiance released where light is absorbed (white, scaled like
+// emitters by D65).  Free flights are sampled in the box; shadow rays carry the
+// box chord's transmittance.
+struct BoxMedium
+{
+    int on;
+    V3 lo, hi;
+    float sigma_t, albedo, g, emission;
+};
+
+// the part [t0, t1] of the ray's [tmin, tmax] inside the box
+AR_HD bool medium_segment(const BoxMedium& m, V3 o, V3 d, float tmin, float tmax, float* t0, float* t1)
+{
+    const V3 inv = v3(inv_safe(d.x), inv_safe(d.y), inv_safe(d.z));
+    const V3 a = (m.lo - o) * inv, b = (m.hi - o) * inv;
+    const V3 tn = vmin(a, b), tf = vmax(a, b);
+    *t0 = fmaxf(fmaxf(fmaxf(tn.x, tn.y), tn.z), tmin);
+    *t1 = fminf(fminf(fminf(tf.x, tf.y), tf.z), tmax);
+    return *t0 < *t1;
+}
+
+AR_HD float medium_transmittance(const BoxMedium& m, V3 o, V3 d, float dist)
+{
+    if (!m.on) return 1.0f;
+    float t0, t1;
+    if (!medium_segment(m, o, d, 0.0f, dist, &t0, &t1)) return 1.0f;
+    return arm_expf(-m.sigma_t * (t1 - t0));
+}
+
+// HenyeyGreensteinPDF, SampleHenyeyGreensteinBase, SampleHenyeyGreenstein (core/render/sample.cuh:110-145)
+AR_HD float hg_pdf(float cosTheta, float g)
+{
+    const float g2 = g * g;
+    const float x = fmaxf(1.0f + g2 - 2.0f * g * cosTheta, 1e-20f);
+    return (1.0f - g2) / (4.0f * AR_PI_F * x * sqrtf(x));
+}
+
+AR_HD float hg_sample_cos(float e, float g)
+{
+    if (fabsf(g) < 0.0001f) return e * 2.0f - 1.0f;
+    const float g2 = g * g;
+    const float t0 = (1.0f - g2) / (1.0f - g + 2.0f * g * e);
+    return (1.0f + g2 - t0 * t0) / (2.0f * g);
+}
+
+AR_HD DirSample hg_sample(float e0, float e1, V3 v, float g)
+{
+    const float cosTheta = hg_sample_cos(e0, g);
+    const float phi = 2.0f * AR_PI_F * e1;
+    const float sinTheta = sqrtf(fmaxf(0.0f, 1.0f - cosTheta * cosTheta));
+    const V3 w = normalize(v);
+    const V3 a = (fabsf(w.z) > 0.70710678f) ? v3(0.0f, 1.0f, 0.0f) : v3(0.0f, 0.0f, 1.0f);
+    const V3 v2 = normalize(cross(w, a));
+    const V3 v3_ = cross(v2, w);
+    float sp, cp;
+    arm_sincosf(phi, &sp, &cp);
+    DirSample out;
+    out.dir = v3_ * (sinTheta * cp) + v2 * (sinTheta * sp) + w * cosTheta;
+    out.pdf = hg_pdf(cosTheta, g);
+    return out;
+}
+
 // ---------------------------------------------------------------- sky
 // core/render/render.cuh:58-73
 AR_HD V3 sky_lighting(V3 d)

@@ -13,6 +13,7 @@
 #pragma once
 #include "ar_bvh.h"
 #include "ar_geom.h"
+#include "ar_sdf.h"
 #include "ar_shade.h"
 
 #define AR_TRAV_STACK 40
@@ -26,7 +27,11 @@ struct TravScene
     const float4* __restrict__ slots;      // 3 float4 per primitive slot
     const Object* __restrict__ objects;    // analytic object table, indexed by primitive id
     int node_count;
+    SdfUnion sdf;                          // the smooth-union SDF object (count 0: none)
 };
+
+// SDF march tolerance for a ray starting at intersect_eps-sized offsets (SDF_EPS, core/config.cuh:74)
+AR_HD float sdf_eps(float tmin) { return 0.5f * fmaxf(tmin, 1.0e-3f); }
 
 struct TravResult
 {
@@ -62,7 +67,7 @@ AR_HD uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, int s)
 }
 
 // Intersects one primitive slot; returns t (or -1 on miss) and the id.
-AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3 d, int* id_out)
+AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3 d, int* id_out, float tmin = 0.0f)
 {
     const float4 a = AR_LDG(&sc.slots[3 * (size_t)slot + 0]);
     const uint32_t tag = AR_F2U(a.w);
@@ -77,6 +82,7 @@ AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3
         if (tri_intersect(sh, o, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &t, &b0, &b1, &b2)) return t;
         return -1.0f;
     }
+    if (kind == AR_PRIM_KIND_SDF) return sdf_march(sc.sdf, o, d, sdf_eps(tmin));
     const Object ob = sc.objects[id];
     Hit h;
     h.hit = false;
@@ -157,7 +163,7 @@ AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, floa
                 {
                     int id;
                     ++n_tests;
-                    const float t = prim_hit(sc, first + k, sh, o, d, &id);
+                    const float t = prim_hit(sc, first + k, sh, o, d, &id, tmin);
                     if (!(t >= tmin)) continue;  // also rejects misses (-1)
                     if (AnyHit)
                     {

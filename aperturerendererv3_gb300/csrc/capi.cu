@@ -46,6 +46,8 @@ DevScene dev_scene(const Ctx& c)
     s.camera_inside = c.camera_inside;
     s.stats = (c.profile & 2) ? c.d_stats : nullptr;
     s.guide = c.guide;
+    s.trav.sdf = c.sdf;
+    s.medium = c.medium;
     s.texels = c.d_texels;
     s.tex_info = c.d_tex_info;
     s.prim_uv = c.d_prim_uv;
@@ -96,6 +98,8 @@ void free_scene(Ctx& c)
     free_dev(c.d_texels);
     free_dev(c.d_tex_info);
     free_dev(c.d_prim_uv);
+    free_dev(c.d_sdf);
+    c.sdf = SdfUnion{};
     c.tex_count = 0;
     c.texel_floats = 0;
     c.built = false;
@@ -619,6 +623,7 @@ ar_status ar_destroy(ar_ctx* ctx)
     free_dev(c.d_stats);
     free_dev(c.d_grad32);
     free_dev(c.d_adj);
+    free_dev(c.d_grad_medium);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete ctx;
     return AR_OK;
@@ -723,6 +728,49 @@ ar_status ar_scene_set_mesh_uv(ar_ctx* ctx, const float* uv, int nt)
     return AR_OK;
 }
 
+ar_status ar_scene_set_sdf_union(ar_ctx* ctx, const float* prims, int n, float smooth_k, int32_t material)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    if (n < 0 || n > AR_SDF_MAX_PRIMS || (n > 0 && !prims)) return fail(ctx, AR_ERR_INVALID, "sdf union: bad pointer or count");
+    if (n > 0 && !(smooth_k > 0.0f)) return fail(ctx, AR_ERR_INVALID, "sdf union: smooth width must be positive");
+    Ctx& c = ctx->c;
+    for (int i = 0; i < n; ++i)
+    {
+        const int kind = (int)prims[8 * i];
+        if (kind != AR_SDF_SPHERE && kind != AR_SDF_BOX && kind != AR_SDF_TORUS)
+            return fail(ctx, AR_ERR_INVALID, "sdf union: unknown primitive kind");
+    }
+    c.sdf_prims.assign(prims, prims + 8 * (size_t)n);
+    c.sdf_k = smooth_k;
+    c.sdf_material = material;
+    c.built = false;
+    return AR_OK;
+}
+
+ar_status ar_scene_set_medium(ar_ctx* ctx, const ar_medium* m)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (!m)
+    {
+        c.medium = BoxMedium{};
+        return AR_OK;
+    }
+    if (!(m->sigma_t > 0.0f) || !(m->albedo >= 0.0f && m->albedo <= 1.0f) || !(m->g > -1.0f && m->g < 1.0f) ||
+        !(m->emission >= 0.0f))
+        return fail(ctx, AR_ERR_INVALID, "medium: sigma_t > 0, albedo in [0, 1], |g| < 1, emission >= 0");
+    for (int k = 0; k < 3; ++k)
+        if (!(m->box_lo[k] < m->box_hi[k])) return fail(ctx, AR_ERR_INVALID, "medium: empty box");
+    c.medium.on = 1;
+    c.medium.lo = v3(m->box_lo[0], m->box_lo[1], m->box_lo[2]);
+    c.medium.hi = v3(m->box_hi[0], m->box_hi[1], m->box_hi[2]);
+    c.medium.sigma_t = m->sigma_t;
+    c.medium.albedo = m->albedo;
+    c.medium.g = m->g;
+    c.medium.emission = m->emission;
+    return AR_OK;
+}
+
 ar_status ar_scene_texel_count(ar_ctx* ctx, int64_t* n_floats)
 {
     if (!ctx || !n_floats) return AR_ERR_INVALID;
@@ -754,7 +802,8 @@ ar_status ar_scene_build(ar_ctx* ctx)
     AR_CUDA(ctx, cudaSetDevice(c.device));
     const int nobj = (int)c.objects.size();
     const int nmesh = (int)c.mesh_material.size();
-    const long long nprim = (long long)nobj + nmesh;
+    const int nsdf = c.sdf_prims.empty() ? 0 : 1;  // the smooth-union SDF is one primitive, after the mesh
+    const long long nprim = (long long)nobj + nmesh + nsdf;
     const int nmat = (int)c.materials.size();
     if (nprim == 0) return fail(ctx, AR_ERR_INVALID, "scene is empty");
     for (int i = 0; i < nobj; ++i)
@@ -766,6 +815,34 @@ ar_status ar_scene_build(ar_ctx* ctx)
         if (c.materials[i].albedo_tex >= ntex) return fail(ctx, AR_ERR_INVALID, "material texture index out of range");
     if (!c.mesh_uv.empty() && c.mesh_uv.size() != 6 * (size_t)nmesh)
         return fail(ctx, AR_ERR_INVALID, "mesh uv count differs from the mesh's triangle count");
+    if (nsdf && (c.sdf_material < 0 || c.sdf_material >= nmat || c.materials[c.sdf_material].shading == AR_MAT_LIGHT))
+        return fail(ctx, AR_ERR_INVALID, "sdf union: material index out of range or a light");
+    float sdf_lo[3] = {3e38f, 3e38f, 3e38f}, sdf_hi[3] = {-3e38f, -3e38f, -3e38f};
+    for (size_t i = 0; i < c.sdf_prims.size() / 8; ++i)
+    {
+        const float* q = &c.sdf_prims[8 * i];
+        const int kind = (int)q[0];
+        float h[3];
+        if (kind == AR_SDF_SPHERE) h[0] = h[1] = h[2] = q[4];
+        else if (kind == AR_SDF_BOX)
+        {
+            h[0] = q[4];
+            h[1] = q[5];
+            h[2] = q[6];
+        }
+        else
+        {
+            h[0] = h[2] = q[4] + q[5];
+            h[1] = q[5];
+        }
+        for (int k = 0; k < 3; ++k)
+        {
+            // the smooth union reaches at most k / 4 beyond its primitives
+            const float pad = 0.25f * c.sdf_k + 1e-4f * (fabsf(q[1 + k]) + h[k]) + 1e-6f;
+            sdf_lo[k] = std::min(sdf_lo[k], q[1 + k] - fabsf(h[k]) - pad);
+            sdf_hi[k] = std::max(sdf_hi[k], q[1 + k] + fabsf(h[k]) + pad);
+        }
+    }
 
     // primitives for the BVH
     std::vector<arbvh::PrimInput> prims((size_t)nprim);
@@ -785,10 +862,20 @@ ar_status ar_scene_build(ar_ctx* ctx)
                 object_bounds(c.objects[i], p.lo, p.hi);
             }
         }
-        else
+        else if (i < (long long)nobj + nmesh)
         {
             prim_material[i] = c.mesh_material[i - nobj];
             tv = &c.mesh_v[9 * (size_t)(i - nobj)];
+        }
+        else
+        {
+            prim_material[i] = c.sdf_material;
+            p.kind = AR_PRIM_KIND_SDF;
+            for (int k = 0; k < 3; ++k)
+            {
+                p.lo[k] = sdf_lo[k];
+                p.hi[k] = sdf_hi[k];
+            }
         }
         if (tv)
         {
@@ -898,6 +985,17 @@ ar_status ar_scene_build(ar_ctx* ctx)
         AR_CUDA(ctx, cudaMemcpy(c.d_prim_uv, uv.data(), uv.size() * sizeof(float), cudaMemcpyHostToDevice));
         c.tex_count = ntex;
         c.texel_floats = (long long)c.tex_texels.size();
+    }
+    if (nsdf)
+    {
+        const int n = (int)(c.sdf_prims.size() / 8);
+        AR_CUDA(ctx, alloc_dev(c.d_sdf, 2 * (size_t)n));
+        AR_CUDA(ctx, cudaMemcpy(c.d_sdf, c.sdf_prims.data(), c.sdf_prims.size() * sizeof(float), cudaMemcpyHostToDevice));
+        c.sdf.prims = c.d_sdf;
+        c.sdf.count = n;
+        c.sdf.k = c.sdf_k;
+        c.sdf.lo = v3(sdf_lo[0], sdf_lo[1], sdf_lo[2]);
+        c.sdf.hi = v3(sdf_hi[0], sdf_hi[1], sdf_hi[2]);
     }
     std::vector<Material> mats(c.materials);
     AR_CUDA(ctx, alloc_dev(c.d_materials, std::max<size_t>(mats.size(), 1)));
@@ -1025,17 +1123,22 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     return AR_OK;
 }
 
-ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* prm, const float* dl_dxyz, double* grad_texels, void* stream)
+} // extern "C"
+
+namespace
 {
-    if (!ctx || !prm || !dl_dxyz || !grad_texels) return AR_ERR_INVALID;
+// Replay adjoint driver: per wave a radiance pass, the per-path seed and the
+// replay pass that scatters gradients (texels into float32, folded into
+// grad_texels in float64 after each wave; medium parameters into grad_medium).
+ar_status run_adjoint(ar_ctx* ctx, const ar_render_params* prm, const float* dl_dxyz, double* grad_texels,
+                      double* grad_medium, void* stream)
+{
     Ctx& c = ctx->c;
     if (prm->guide != AR_GUIDE_NONE) return fail(ctx, AR_ERR_INVALID, "adjoint: guided rendering is not differentiated");
     if (prm->profile) return fail(ctx, AR_ERR_INVALID, "adjoint: profiling is not supported");
     RenderLaunch rl;
     ar_status st = prepare_launch(ctx, prm, rl);
     if (st != AR_OK) return st;
-    if (c.texel_floats == 0) return fail(ctx, AR_ERR_STATE, "adjoint: the scene has no textures");
-    // the caller's buffers are ordered on its stream: finish that work first
     if (stream) AR_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
     const long long npix = (long long)rl.width * rl.height;
     const long long total = npix * rl.spp;
@@ -1051,14 +1154,18 @@ ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* prm, const float* dl_d
     }
     c.ps.adj_total = c.d_adj;
     c.ps.adj_delta = c.d_adj + c.ps.capacity;
-    if (c.grad32_n < c.texel_floats)
+    if (grad_texels)
     {
-        free_dev(c.d_grad32);
-        AR_CUDA(ctx, alloc_dev(c.d_grad32, (size_t)c.texel_floats));
-        AR_CUDA(ctx, cudaMemset(c.d_grad32, 0, (size_t)c.texel_floats * sizeof(float)));
-        c.grad32_n = c.texel_floats;
+        if (c.grad32_n < c.texel_floats)
+        {
+            free_dev(c.d_grad32);
+            AR_CUDA(ctx, alloc_dev(c.d_grad32, (size_t)c.texel_floats));
+            AR_CUDA(ctx, cudaMemset(c.d_grad32, 0, (size_t)c.texel_floats * sizeof(float)));
+            c.grad32_n = c.texel_floats;
+        }
+        AR_CUDA(ctx, cudaMemsetAsync(grad_texels, 0, (size_t)c.texel_floats * sizeof(double), c.stream));
     }
-    AR_CUDA(ctx, cudaMemsetAsync(grad_texels, 0, (size_t)c.texel_floats * sizeof(double), c.stream));
+    if (grad_medium) AR_CUDA(ctx, cudaMemsetAsync(grad_medium, 0, 2 * sizeof(double), c.stream));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1067,14 +1174,15 @@ ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* prm, const float* dl_d
     cudaError_t e = cudaSuccess;
     RenderLaunch replay = rl;
     replay.adjoint = 1;
-    replay.grad = c.d_grad32;
+    replay.grad = grad_texels ? c.d_grad32 : nullptr;
+    replay.grad_medium = grad_medium;
     for (long long first = 0; first < total && e == cudaSuccess;)
     {
         const int n = (int)std::min<long long>(cap, total - first);
         e = launch_render_wave(c, rl, first, n, nullptr, &launches);                           // radiance of each path
         if (e == cudaSuccess) e = launch_adjoint_seed(c, rl, n, dl_dxyz, &launches);           // its adjoint
         if (e == cudaSuccess) e = launch_render_wave(c, replay, first, n, nullptr, &launches);  // replay + scatter
-        if (e == cudaSuccess) e = launch_grad_fold(c, grad_texels, c.texel_floats, &launches);
+        if (e == cudaSuccess && grad_texels) e = launch_grad_fold(c, grad_texels, c.texel_floats, &launches);
         first += n;
     }
     cudaEventRecord(e1, c.stream);
@@ -1090,6 +1198,31 @@ ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* prm, const float* dl_d
     unsigned int word = 0;
     AR_CUDA(ctx, cudaMemcpy(&word, c.d_err, sizeof(word), cudaMemcpyDeviceToHost));
     if (word) return fail(ctx, AR_ERR_DEVICE, "device error word set: " + std::to_string(word));
+    return AR_OK;
+}
+} // namespace
+
+extern "C" {
+
+ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* prm, const float* dl_dxyz, double* grad_texels, void* stream)
+{
+    if (!ctx || !prm || !dl_dxyz || !grad_texels) return AR_ERR_INVALID;
+    if (!ctx->c.built) return fail(ctx, AR_ERR_STATE, "adjoint before ar_scene_build");
+    if (ctx->c.texel_floats == 0) return fail(ctx, AR_ERR_STATE, "adjoint: the scene has no textures");
+    return run_adjoint(ctx, prm, dl_dxyz, grad_texels, nullptr, stream);
+}
+
+ar_status ar_adjoint_medium(ar_ctx* ctx, const ar_render_params* prm, const float* dl_dxyz, double* grad2, void* stream)
+{
+    if (!ctx || !prm || !dl_dxyz || !grad2) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (!c.built) return fail(ctx, AR_ERR_STATE, "adjoint before ar_scene_build");
+    if (!c.medium.on) return fail(ctx, AR_ERR_STATE, "adjoint: the scene has no medium");
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    if (!c.d_grad_medium) AR_CUDA(ctx, alloc_dev(c.d_grad_medium, 2));
+    const ar_status st = run_adjoint(ctx, prm, dl_dxyz, nullptr, c.d_grad_medium, stream);
+    if (st != AR_OK) return st;
+    AR_CUDA(ctx, cudaMemcpy(grad2, c.d_grad_medium, 2 * sizeof(double), cudaMemcpyDeviceToHost));
     return AR_OK;
 }
 
@@ -1228,6 +1361,7 @@ ar_status ar_host_trace_closest(const float* tris, int ntri, const float* rays, 
     sc.slots = reinterpret_cast<const float4*>(bvh.slots.data());
     sc.objects = nullptr;
     sc.node_count = (int)bvh.nodes.size();
+    sc.sdf = SdfUnion{};
     unsigned int errw = 0;
     unsigned long long stats[2] = {0, 0};
     for (int r = 0; r < nray; ++r)

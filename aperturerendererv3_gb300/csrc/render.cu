@@ -107,6 +107,12 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
         tri_frame(o, d, t, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &h->pos, &h->nrm);
         h->local_pos = v3(0.0f, 0.0f, 0.0f);
     }
+    else if (kind == AR_PRIM_KIND_SDF)
+    {
+        h->pos = o + d * t;
+        h->nrm = sdf_normal(sc.trav.sdf, h->pos, 1.0e-4f);
+        h->local_pos = h->pos;
+    }
     else
     {
         const Object ob = sc.trav.objects[id];
@@ -215,7 +221,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_extend(DevScene sc, PathState ps, 
             // inside a medium: intersect only the enclosing object (render.cuh:89-92)
             const int s = sc.prim_slot[mobj];
             int id;
-            const float th = prim_hit(sc.trav, s, make_shear(d), o, d, &id);
+            const float th = prim_hit(sc.trav, s, make_shear(d), o, d, &id, tmin);
             if (th >= tmin)
             {
                 t = th;
@@ -280,8 +286,9 @@ struct ShadeParams
     int use_nee;
     int max_depth;
     int frame;    // frame index of the wave (guided rendering: mixture probability)
-    float* grad;  // replay adjoint: float32 texel gradients (3 per texel)
+    float* grad;  // replay adjoint: float32 texel gradients (3 per texel), or null
     int mlp_ready;  // MLP guide: the network has trained long enough to replace the voxel probes
+    double* grad_medium;  // replay adjoint: d loss / d (medium albedo, medium emission), or null
 };
 
 // CollectRadiance (core/render/render.cuh:353-432) on the path's collection
@@ -344,6 +351,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
     __syncthreads();
     const int n = *counter;
     const int stride = gridDim.x * blockDim.x;
+    float g_med_albedo = 0.0f, g_med_emission = 0.0f;  // replay adjoint of the medium parameters
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride)
     {
         const int q = base + lane_id();
@@ -392,11 +400,33 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
             h.local_pos = v3(0, 0, 0);
             if (slot >= 0) hit_context(sc, slot, rayO, rayD, ps.hit_t[p], &h);
 
+            // ---- participating medium: a free flight sampled in the medium box
+            // ends the segment early with probability 1 - transmittance
+            bool scatter = false;
+            if (sc.medium.on)
+            {
+                float m0, m1;
+                if (medium_segment(sc.medium, rayO, rayD, 0.0f, h.hit ? h.dist : 3.0e38f, &m0, &m1))
+                {
+                    const float ts = m0 - arm_logf(R()) / sc.medium.sigma_t;
+                    if (ts < m1)
+                    {
+                        scatter = true;
+                        h.hit = false;
+                        h.obj = -1;
+                        h.light = -1;
+                        h.dist = ts;
+                        h.pos = rayO + rayD * ts;
+                        h.nrm = v3(0.0f, 0.0f, 0.0f);
+                    }
+                }
+            }
+
             // ---- Trace (render.cuh:109-155)
             BsdfSample S = bsdf_sample_default();
             Material mat;
             mat.shading = AR_MAT_DIFFUSE;
-            if (!h.hit && media.inside)
+            if (!h.hit && !scatter && media.inside)
             {
                 S.miss_thin = true;
                 S.brdf = 1.0f;
@@ -424,6 +454,19 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                     }
                 }
                 S = evaluate_material(lambda, lb, R, mat, rayD, h, media);
+            }
+            else if (scatter)
+            {
+                // Henyey-Greenstein phase sampling; throughput x albedo
+                const float e0 = R();
+                const float e1 = R();
+                const DirSample ph = hg_sample(e0, e1, rayD, sc.medium.g);
+                S.next_dir = ph.dir;
+                S.pdf = ph.pdf;
+                S.brdf = sc.medium.albedo * ph.pdf;
+                S.delta = false;
+                S.emissive = v3(0.0f, 0.0f, 0.0f);
+                S.media = media;
             }
             else
             {
@@ -540,7 +583,13 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
 
             // ---- emission (render.cuh:647-723)
             V3 endpointLe = v3(0.0f, 0.0f, 0.0f);
-            if (!h.hit)
+            float medium_unit = 0.0f;  // emission released at this scattering point per unit emission
+            if (scatter)
+            {
+                medium_unit = mask * (1.0f - sc.medium.albedo) * d65;
+                radiance = radiance + medium_unit * sc.medium.emission;
+            }
+            else if (!h.hit)
             {
                 if (!S.miss_thin)
                 {
@@ -574,7 +623,18 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                 // replay adjoint: every contribution still to come on this path
                 // (NEE here, emission and NEE further on) carries this vertex's
                 // albedo once; radiance holds the contributions that do not
-                if (texel >= 0 && mat.shading == AR_MAT_DIFFUSE)
+                if (scatter && prm.grad_medium)
+                {
+                    // later contributions carry this albedo once; the emission here carries (1 - albedo)
+                    const float dlt = ps.adj_delta[p];
+                    const float a = sc.medium.albedo;
+                    const float rest = ps.adj_total[p] - radiance;
+                    if (a > 1.0e-8f) g_med_albedo += dlt * rest / a;
+                    // d/d albedo of (1 - albedo) x emission x mask, and d/d emission
+                    g_med_albedo -= dlt * mask * sc.medium.emission * d65;
+                    g_med_emission += dlt * medium_unit;
+                }
+                if (prm.grad && texel >= 0 && mat.shading == AR_MAT_DIFFUSE)
                 {
                     const float rest = ps.adj_total[p] - radiance;
                     const float dlt = ps.adj_delta[p];
@@ -596,7 +656,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                                  false, rayD, h.pos, h.nrm);
             }
 
-            const bool ended = (!h.hit && !S.miss_thin) || S.terminate;
+            const bool ended = (!h.hit && !S.miss_thin && !scatter) || S.terminate;
             if (!ended)
             {
                 // ---- NEE (render.cuh:766-827, 206-343)
@@ -647,18 +707,21 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                             const V3 lun = ls.point - h.pos;
                             const float dist2 = fmaxf(dot(lun, lun), (float)1.0e-12);
                             const V3 L = lun * arm_rsqrtf(dist2);
-                            const float cosX = fmaxf(0.0f, dot(h.nrm, L));
+                            const float cosX = scatter ? 1.0f : fmaxf(0.0f, dot(h.nrm, L));
                             const float cosY = fmaxf(0.0f, dot(ls.normal, -L));
                             float vUn = vZero;
                             bool validUn = false;
                             if (!(cosX <= 0.0f || cosY <= 0.0f))
                             {
-                                const float brdfCos = eval_bsdf_cos(lambda, lb, mat, rayD, L, h, media_default());
+                                const float brdfCos =
+                                    scatter ? sc.medium.albedo * hg_pdf(dot(rayD, L), sc.medium.g)
+                                            : eval_bsdf_cos(lambda, lb, mat, rayD, L, h, media_default());
                                 const float G = (cosY / dist2);
                                 const float le = interact(sc.materials[ls.material].emissive_c, lb);
                                 const float contribution = brdfCos * le * (G / pATotal);
                                 const float pLight = area_to_solid_angle_pdf(h.pos, ls.point, ls.normal, ls.p_facet * ls.p_a);
-                                float pBsdf = fmaxf(bsdf_pdf(lb, mat, h.nrm, rayD, L), 0.0f);
+                                float pBsdf = scatter ? hg_pdf(dot(rayD, L), sc.medium.g)
+                                                      : fmaxf(bsdf_pdf(lb, mat, h.nrm, rayD, L), 0.0f);
                                 if constexpr (GUIDE)
                                 {
                                     if (probe)
@@ -671,6 +734,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                                 }
                                 const float misW = power_heuristic(pLight, pBsdf);
                                 vUn = mask * (contribution * misW) * d65;
+                                if (sc.medium.on) vUn *= medium_transmittance(sc.medium, h.pos, L, sqrtf(dist2));
                                 validUn = true;
                             }
                             // shadow segment (intersection.cuh:285-310)
@@ -761,6 +825,22 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
             sq.d[sqi] = make_float4(sh_d.x, sh_d.y, sh_d.z, sh_vun);
             sq.v_occ[sqi] = sh_vocc;
             sq.valid_unocc[sqi] = sh_valid ? 1 : 0;
+        }
+    }
+    if constexpr (ADJ)
+    {
+        if (prm.grad_medium)
+        {
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                g_med_albedo += __shfl_xor_sync(0xffffffffu, g_med_albedo, o);
+                g_med_emission += __shfl_xor_sync(0xffffffffu, g_med_emission, o);
+            }
+            if (lane_id() == 0 && (g_med_albedo != 0.0f || g_med_emission != 0.0f))
+            {
+                atomicAdd(prm.grad_medium, (double)g_med_albedo);
+                atomicAdd(prm.grad_medium + 1, (double)g_med_emission);
+            }
         }
     }
 }
@@ -953,6 +1033,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     prm.max_depth = rl.max_depth;
     prm.frame = rl.first_frame + (int)(first_path / ((long long)rl.width * rl.height));
     prm.grad = rl.grad;
+    prm.grad_medium = rl.grad_medium;
     prm.mlp_ready = rl.mlp_ready;
     MlpDev net;
     net.wbf = c.d_mlp_wbf;
@@ -1035,6 +1116,7 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     prm.max_depth = rl.max_depth;
     prm.frame = rl.first_frame;
     prm.grad = nullptr;
+    prm.grad_medium = nullptr;
     prm.mlp_ready = 0;
     for (int b = 0; b < rl.max_depth; ++b)
     {

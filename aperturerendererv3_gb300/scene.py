@@ -24,7 +24,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (GLOBAL_SEED, OBJECT_CUBE, OBJECT_SPHERE, OBJECT_TRIANGLE, SHADING_DIFFUSE, SHADING_GGX,
-                   SHADING_GLASS, SHADING_LIGHT, ArMaterial, ArObject, ArRenderParams, check)
+                   SHADING_GLASS, SHADING_LIGHT, ArMaterial, ArMedium, ArObject, ArRenderParams, check)
 
 Vec3 = Sequence[float]
 
@@ -124,6 +124,38 @@ class TriangleMesh:
         return np.asarray(self.vertices, np.float32)[np.asarray(self.indices, np.int64)].reshape(-1, 9)
 
 
+@dataclass
+class SdfUnion:
+    """Smooth union of SDF primitives: (kind, centre, size) with kind one of
+    SDF_SPHERE (size[0] = radius), SDF_BOX (half extents), SDF_TORUS (about +y:
+    size[0] major, size[1] minor radius); smooth width k; one material."""
+    prims: list
+    smooth_k: float
+    material: Material
+
+    def array(self) -> np.ndarray:
+        rows = [[float(k), *map(float, c), *map(float, sz), 0.0] for k, c, sz in self.prims]
+        return np.ascontiguousarray(np.array(rows, np.float32).reshape(-1, 8))
+
+
+@dataclass
+class Medium:
+    """Homogeneous participating medium filling an axis-aligned box."""
+    box_lo: tuple
+    box_hi: tuple
+    sigma_t: float
+    albedo: float
+    g: float = 0.0
+    emission: float = 0.0
+
+    def to_c(self) -> ArMedium:
+        m = ArMedium()
+        m.box_lo[:] = _f3(self.box_lo)
+        m.box_hi[:] = _f3(self.box_hi)
+        m.sigma_t, m.albedo, m.g, m.emission = self.sigma_t, self.albedo, self.g, self.emission
+        return m
+
+
 def flatten(objects: Iterable[SceneObject], mesh: TriangleMesh | None = None):
     """Material table + C object array + mesh arrays for the C ABI."""
     objects = list(objects)
@@ -158,7 +190,8 @@ class SceneRenderer:
     """GPU path tracer for one scene (drop-in for the reference's SceneRenderer)."""
 
     def __init__(self, sceneObjects: Iterable[SceneObject], device: int = 0, mesh: TriangleMesh | None = None,
-                 textures: Sequence[np.ndarray] | None = None):
+                 textures: Sequence[np.ndarray] | None = None, sdf: SdfUnion | None = None,
+                 medium: Medium | None = None):
         lib = _lib.load()
         self._lib = lib
         ctx = C.c_void_p()
@@ -169,6 +202,8 @@ class SceneRenderer:
         self.objects = list(sceneObjects)
         self.mesh = mesh
         self.textures = list(textures) if textures is not None else []
+        self.sdf = sdf
+        self.medium = medium
         self.device = device
         self.bDirty = True
 
@@ -190,6 +225,11 @@ class SceneRenderer:
         if not self.bDirty:
             return
         mats, arr, n, mesh_ids = flatten(self.objects, self.mesh)
+        sdf_mat = -1
+        if self.sdf is not None:
+            if self.sdf.material not in mats:
+                mats.append(self.sdf.material)
+            sdf_mat = mats.index(self.sdf.material)
         carr = (ArMaterial * max(1, len(mats)))(*[m.to_c() for m in mats])
         check(self._ctx, self._lib.ar_scene_set_materials(self._ctx, carr, len(mats)))
         check(self._ctx, self._lib.ar_scene_set_objects(self._ctx, arr, n))
@@ -213,8 +253,24 @@ class SceneRenderer:
                                                              len(self.textures)))
         else:
             check(self._ctx, self._lib.ar_scene_set_textures(self._ctx, None, None, 0))
+        if self.sdf is not None:
+            a = self.sdf.array()
+            check(self._ctx, self._lib.ar_scene_set_sdf_union(self._ctx, a.ctypes.data, len(a), float(self.sdf.smooth_k),
+                                                              sdf_mat))
+        else:
+            check(self._ctx, self._lib.ar_scene_set_sdf_union(self._ctx, None, 0, 0.0, -1))
         check(self._ctx, self._lib.ar_scene_build(self._ctx))
+        self.set_medium(self.medium)
         self.bDirty = False
+
+    def set_medium(self, medium: Medium | None) -> None:
+        """Sets (or, with None, removes) the participating medium; no rebuild needed."""
+        self.medium = medium
+        if medium is None:
+            check(self._ctx, self._lib.ar_scene_set_medium(self._ctx, None))
+        else:
+            m = medium.to_c()
+            check(self._ctx, self._lib.ar_scene_set_medium(self._ctx, C.byref(m)))
 
     def build(self) -> None:
         self._build()
@@ -312,6 +368,19 @@ class SceneRenderer:
             raise ValueError(f"grad_out must be a contiguous float64 tensor of {n} elements")
         s = _torch_stream(g.device)
         check(self._ctx, self._lib.ar_adjoint(self._ctx, C.byref(p), g.data_ptr(), grad_out.data_ptr(), s))
+
+    def adjoint_medium(self, dl_dxyz, size, cameraOrigin, cameraDirection, sampleNum: int, **kw) -> tuple[float, float]:
+        """(d loss / d albedo, d loss / d emission) of the medium, given
+        dl_dxyz = d(loss)/d(image) (CUDA float32, (height, width, 3))."""
+        import torch
+        self._build()
+        p = self.params(size, cameraOrigin, cameraDirection, sampleNum, **kw)
+        g = dl_dxyz.detach().to(torch.float32).contiguous()
+        if g.numel() != 3 * p.width * p.height:
+            raise ValueError("dl_dxyz must hold 3 floats per pixel")
+        out = (C.c_double * 2)()
+        check(self._ctx, self._lib.ar_adjoint_medium(self._ctx, C.byref(p), g.data_ptr(), out, _torch_stream(g.device)))
+        return out[0], out[1]
 
     def last_render_stats(self) -> tuple[float, int]:
         ms, n = C.c_float(), C.c_int64()

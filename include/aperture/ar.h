@@ -147,6 +147,32 @@ ar_status ar_scene_set_mesh_uv(ar_ctx* ctx, const float* uv, int n_triangles);
 ar_status ar_scene_update_texels(ar_ctx* ctx, const float* texels, int64_t n_floats, int is_device, void* stream);
 /* Texel floats of the built scene (3 per texel, all textures). */
 ar_status ar_scene_texel_count(ar_ctx* ctx, int64_t* n_floats);
+
+/* Smooth-union SDF object (no reference counterpart; the reference's OBJ_SDF
+ * marches one analytic shape per object, core/object/sdf/sdf_base.cuh:53-163):
+ * the surface where the polynomial smooth minimum (width smooth_k) of the
+ * primitives' signed distances is zero, in world space, one primitive of the
+ * scene with id n_objects + n_mesh_triangles.  prims: n x 8 floats (kind,
+ * centre xyz, size xyz, 0): sphere (size.x = radius), box (half extents),
+ * torus about +y (size.x = major, size.y = minor radius).  n = 0 removes it.
+ * Takes effect at ar_scene_build. */
+#define AR_SDF_SPHERE 0
+#define AR_SDF_BOX 1
+#define AR_SDF_TORUS 2
+ar_status ar_scene_set_sdf_union(ar_ctx* ctx, const float* prims, int n, float smooth_k, int32_t material);
+
+/* Homogeneous participating medium filling an axis-aligned box (no reference
+ * counterpart): extinction sigma_t, single-scattering albedo, Henyey-Greenstein
+ * g (core/render/sample.cuh:110-145), and an emission radiance released where
+ * light is absorbed (white, scaled like emitters by D65).  Free flights are
+ * sampled inside the box, NEE shadow rays carry the box chord's transmittance.
+ * Takes effect immediately (no rebuild); NULL removes it. */
+typedef struct ar_medium
+{
+    float box_lo[3], box_hi[3];
+    float sigma_t, albedo, g, emission;
+} ar_medium;
+ar_status ar_scene_set_medium(ar_ctx* ctx, const ar_medium* medium);
 /* Builds the BVH, the light table and the spectral LUTs; uploads the scene. */
 ar_status ar_scene_build(ar_ctx* ctx);
 /* BVH statistics: nodes, primitive slots, depth, bytes on the device. */
@@ -199,6 +225,14 @@ ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* params, double*
  * is rejected. */
 ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* params, const float* dl_dxyz, double* grad_texels,
                      void* stream);
+
+/* Replay adjoint of the medium's scalar parameters (no reference counterpart):
+ * grad2 (host) = d(loss)/d(albedo), d(loss)/d(emission), from dl_dxyz as for
+ * ar_adjoint.  Every scattering event multiplies what follows by the albedo
+ * and releases (1 - albedo) x emission; roulette and NEE decisions are held
+ * fixed. */
+ar_status ar_adjoint_medium(ar_ctx* ctx, const ar_render_params* params, const float* dl_dxyz, double* grad2,
+                            void* stream);
 
 /* Device time (ms) of the last ar_render and the number of kernels it launched. */
 ar_status ar_last_render_stats(ar_ctx* ctx, float* device_ms, int64_t* kernel_launches);

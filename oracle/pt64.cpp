@@ -23,6 +23,11 @@
 //              (core/spectrum/spectrum_basis.cuh:2262-2469) evaluated in double
 //   path       Russian roulette (core/render/render.cuh:829-859), NEE
 //              acceptance, sky (core/render/render.cuh:58-73), XYZ clamp (:967)
+//   additions  the smooth-union SDF object (sphere tracing as RaymarchLocal,
+//              core/object/sdf/sdf_base.cuh:53-105) and the homogeneous medium
+//              in a box (free flights, Henyey-Greenstein phase from
+//              core/render/sample.cuh:110-145, box-chord transmittance on NEE),
+//              with the replay adjoint of the medium's albedo and emission
 // Random numbers come from the same per-sample PCG32 streams as the GPU
 // integrator (ar_rng.h), so each oracle sample follows the GPU sample's path
 // up to floating-point decisions.  The replay adjoint of albedo textures
@@ -99,6 +104,7 @@ enum
 {
     OBJ_CUBE = 0,
     OBJ_SPHERE = 1,
+    OBJ_SDF = 2,
     OBJ_TRIANGLE = 3,
     MAT_DIFFUSE = 0,
     MAT_LIGHT = 1,
@@ -146,6 +152,13 @@ struct Scene
     std::vector<int> tex_off, tex_w, tex_h;
     std::vector<R> texels;
     Tables tab;
+    // smooth-union SDF (primitives: kind, centre, size) and the medium
+    std::vector<std::array<R, 7>> sdf;
+    R sdf_k = 0;
+    R sdf_lo[3] = {0, 0, 0}, sdf_hi[3] = {0, 0, 0};
+    bool med_on = false;
+    R med_lo[3] = {0, 0, 0}, med_hi[3] = {0, 0, 0};
+    R med_sigma = 0, med_albedo = 0, med_g = 0, med_emission = 0;
     // BVH
     struct Node
     {
@@ -514,9 +527,73 @@ static bool sphere_hit(V o, V d, const Obj& ob, Hit* h, bool full)
     return true;
 }
 
-static R prim_t(const Scene& S, int p, V o, V d)
+// ---- smooth-union SDF
+static R sdf_prim(const std::array<R, 7>& q, V p)
+{
+    const V c = v(q[1], q[2], q[3]);
+    const V x = p - c;
+    const int kind = (int)q[0];
+    if (kind == 0) return length(x) - q[4];
+    if (kind == 1)
+    {
+        const V d = v(std::fabs(x.x) - q[4], std::fabs(x.y) - q[5], std::fabs(x.z) - q[6]);
+        const V dp = v(std::max(d.x, 0.0), std::max(d.y, 0.0), std::max(d.z, 0.0));
+        return length(dp) + std::min(std::max(d.x, std::max(d.y, d.z)), 0.0);
+    }
+    const R rxz = std::sqrt(x.x * x.x + x.z * x.z) - q[4];
+    return std::sqrt(rxz * rxz + x.y * x.y) - q[5];
+}
+
+static R sdf_eval(const Scene& S, V p)
+{
+    R d = sdf_prim(S.sdf[0], p);
+    for (size_t i = 1; i < S.sdf.size(); ++i)
+    {
+        const R b = sdf_prim(S.sdf[i], p);
+        const R h = std::max(S.sdf_k - std::fabs(d - b), 0.0) / S.sdf_k;
+        d = std::min(d, b) - h * h * S.sdf_k * 0.25;
+    }
+    return d;
+}
+
+static bool slab(const R lo[3], const R hi[3], V o, V d, R* t0, R* t1)
+{
+    R a0 = -1e300, a1 = 1e300;
+    const R oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    for (int k = 0; k < 3; ++k)
+    {
+        const R inv = inv_safe(dd[k]);
+        R x = (lo[k] - oo[k]) * inv, y = (hi[k] - oo[k]) * inv;
+        if (x > y) std::swap(x, y);
+        a0 = std::max(a0, x);
+        a1 = std::min(a1, y);
+    }
+    *t0 = a0;
+    *t1 = a1;
+    return a0 <= a1;
+}
+
+// first surface crossing in the bounds (the sign at the origin decides which), or -1
+static R sdf_march(const Scene& S, V o, V d, R eps)
+{
+    R t0, t1;
+    if (S.sdf.empty() || !slab(S.sdf_lo, S.sdf_hi, o, d, &t0, &t1) || t1 <= 0) return -1.0;
+    const bool inside = sdf_eval(S, o) <= 0.0;
+    R t = std::max(0.0, t0);
+    for (int i = 0; i < 512; ++i)
+    {
+        const R dist = sdf_eval(S, o + d * t);
+        if (inside ? (dist > 0 && dist < eps) : (dist < 0 && -dist < eps)) return t;
+        t += std::max(std::fabs(dist), eps * 0.5);
+        if (t > t1) break;
+    }
+    return -1.0;
+}
+
+static R prim_t(const Scene& S, int p, V o, V d, R tmin)
 {
     Hit h;
+    if (S.prim_type[p] == OBJ_SDF) return sdf_march(S, o, d, 0.5 * std::max(tmin, 1e-3));
     if (S.prim_type[p] == OBJ_TRIANGLE)
     {
         R t;
@@ -626,7 +703,7 @@ static int trace(const Scene& S, V o, V d, R tmin, R tmax, bool any, R* tout)
             for (int i = n.first; i < n.first + n.count; ++i)
             {
                 const int p = S.order[i];
-                const R t = prim_t(S, p, o, d);
+                const R t = prim_t(S, p, o, d, tmin);
                 if (!(t >= tmin) || !(t < tmax)) continue;
                 if (t < bt || (t == bt && best >= 0 && p < best))
                 {
@@ -666,6 +743,15 @@ static void hit_record(const Scene& S, int p, V o, V d, R t, Hit* h)
         h->nrm = n;
     }
     else if (S.prim_type[p] == OBJ_CUBE) box_hit(o, d, S.objs[p], h, true);
+    else if (S.prim_type[p] == OBJ_SDF)
+    {
+        h->pos = o + d * t;
+        const R e = 1e-4;
+        const V p0 = h->pos;
+        h->nrm = normalize(v(sdf_eval(S, p0 + v(e, 0, 0)) - sdf_eval(S, p0 - v(e, 0, 0)),
+                             sdf_eval(S, p0 + v(0, e, 0)) - sdf_eval(S, p0 - v(0, e, 0)),
+                             sdf_eval(S, p0 + v(0, 0, e)) - sdf_eval(S, p0 - v(0, 0, e))));
+    }
     else sphere_hit(o, d, S.objs[p], h, true);
 }
 
@@ -1051,6 +1137,44 @@ static V sky(V d)
 
 static R intersect_eps(int depth) { return 1e-3 * std::exp(std::min(depth * 0.5, 4.0)); }
 
+// ---- medium
+static R hg_pdf(R c, R g)
+{
+    const R g2 = g * g;
+    const R x = std::max(1 + g2 - 2 * g * c, 1e-20);
+    return (1 - g2) / (4 * PI * x * std::sqrt(x));
+}
+
+static V hg_sample(R e0, R e1, V vin, R g, R* pdf)
+{
+    R c;
+    if (std::fabs(g) < 0.0001) c = e0 * 2 - 1;
+    else
+    {
+        const R g2 = g * g;
+        const R t0 = (1 - g2) / (1 - g + 2 * g * e0);
+        c = (1 + g2 - t0 * t0) / (2 * g);
+    }
+    const R phi = 2 * PI * e1;
+    const R s = std::sqrt(std::max(0.0, 1 - c * c));
+    const V w = normalize(vin);
+    const V a = std::fabs(w.z) > 0.70710678 ? v(0, 1, 0) : v(0, 0, 1);
+    const V v2 = normalize(cross(w, a));
+    const V v3_ = cross(v2, w);
+    *pdf = hg_pdf(c, g);
+    return v3_ * (s * std::cos(phi)) + v2 * (s * std::sin(phi)) + w * c;
+}
+
+static R med_transmittance(const Scene& S, V o, V d, R dist)
+{
+    if (!S.med_on) return 1.0;
+    R t0, t1;
+    if (!slab(S.med_lo, S.med_hi, o, d, &t0, &t1)) return 1.0;
+    t0 = std::max(t0, 0.0);
+    t1 = std::min(t1, dist);
+    return t0 < t1 ? std::exp(-S.med_sigma * (t1 - t0)) : 1.0;
+}
+
 // ------------------------------------------------------------------ integrator
 struct Params
 {
@@ -1066,10 +1190,18 @@ struct TexVertex
     R before;        // radiance gathered before this vertex's albedo applies
 };
 
+struct MedVertex
+{
+    R after;  // radiance gathered once this scattering point's emission is added
+    R mask;   // throughput arriving at it
+    R d65;
+};
+
 struct PathOut
 {
     R radiance, lambda, pdf;
     std::vector<TexVertex> tv;
+    std::vector<MedVertex> mv;
 };
 
 struct Cam
@@ -1096,6 +1228,7 @@ static void trace_path(const Scene& S, LutCache& L, const Params& P, const Cam& 
     out->lambda = lambda;
     out->pdf = lpdf;
     out->tv.clear();
+    out->mv.clear();
     const auto lam = query_lambda(S.tab, lambda);
     const R d65 = d65_norm(S.tab, lambda);
     R radiance = 0, mask = 1;
@@ -1113,7 +1246,7 @@ static void trace_path(const Scene& S, LutCache& L, const Params& P, const Cam& 
         int prim = -1;
         if (inside && media_obj >= 0)
         {
-            const R th = prim_t(S, media_obj, rayO, rayD);
+            const R th = prim_t(S, media_obj, rayO, rayD, tmin);
             if (th >= tmin)
             {
                 t = th;
@@ -1122,6 +1255,28 @@ static void trace_path(const Scene& S, LutCache& L, const Params& P, const Cam& 
         }
         else prim = trace(S, rayO, rayD, tmin, 1e300, false, &t);
         if (prim >= 0) hit_record(S, prim, rayO, rayD, t, &h);
+        bool scatter = false;
+        if (S.med_on)
+        {
+            R m0, m1;
+            if (slab(S.med_lo, S.med_hi, rayO, rayD, &m0, &m1))
+            {
+                m0 = std::max(m0, 0.0);
+                m1 = std::min(m1, h.hit ? h.t : 1e300);
+                if (m0 < m1)
+                {
+                    const R ts = m0 - std::log(rnd()) / S.med_sigma;
+                    if (ts < m1)
+                    {
+                        scatter = true;
+                        h.hit = false;
+                        prim = -1;
+                        h.pos = rayO + rayD * ts;
+                        h.nrm = v(0, 0, 0);
+                    }
+                }
+            }
+        }
         const R eps = intersect_eps(ndd);
         Shade sh{&S, &L, lam, lambda, Mat{MAT_DIFFUSE, v(1, 1, 1), v(0, 0, 0), 0, 0, 0, -1}, 0};
         Sample smp;
@@ -1129,7 +1284,7 @@ static void trace_path(const Scene& S, LutCache& L, const Params& P, const Cam& 
         V emissive = v(0, 0, 0);
         int texel = -1;
         V dalb = v(0, 0, 0);
-        if (!h.hit && inside)
+        if (!h.hit && !scatter && inside)
         {
             miss_thin = true;
             smp.brdf = 1;
@@ -1152,6 +1307,14 @@ static void trace_path(const Scene& S, LutCache& L, const Params& P, const Cam& 
             emissive = sh.m.emissive;
             inside = inside;  // diffuse / GGX keep the medium flag
         }
+        else if (scatter)
+        {
+            const R e0 = rnd(), e1 = rnd();
+            R pd;
+            smp.dir = hg_sample(e0, e1, rayD, S.med_g, &pd);
+            smp.pdf = pd;
+            smp.brdf = S.med_albedo * pd;
+        }
         else if (!miss_thin)
         {
             smp.brdf = 1;
@@ -1165,7 +1328,12 @@ static void trace_path(const Scene& S, LutCache& L, const Params& P, const Cam& 
             h.pos = h.pos + h.nrm * (signd(dot(h.nrm, smp.dir)) * off * (rnd() + 0.5));
         }
         // emission
-        if (!h.hit)
+        if (scatter)
+        {
+            radiance += mask * (1 - S.med_albedo) * S.med_emission * d65;
+            if (want_grad) out->mv.push_back(MedVertex{radiance, mask, d65});
+        }
+        else if (!h.hit)
         {
             if (!miss_thin) radiance += mask * interact(L, lam, emissive, nullptr) * d65;
         }
@@ -1187,7 +1355,7 @@ static void trace_path(const Scene& S, LutCache& L, const Params& P, const Cam& 
         }
         if (want_grad && texel >= 0 && sh.m.shading == MAT_DIFFUSE && sh.alb > 1e-8)
             out->tv.push_back(TexVertex{texel, dalb / sh.alb, radiance});
-        const bool ended = (!h.hit && !miss_thin) || smp.terminate;
+        const bool ended = (!h.hit && !miss_thin && !scatter) || smp.terminate;
         if (ended) break;
         if (!miss_thin)
         {
@@ -1226,17 +1394,17 @@ static void trace_path(const Scene& S, LutCache& L, const Params& P, const Cam& 
                     const V lun = ls.point - h.pos;
                     const R dist2 = std::max(dot(lun, lun), 1e-12);
                     const V Ld = lun / std::sqrt(dist2);
-                    const R cosX = std::max(0.0, dot(h.nrm, Ld)), cosY = std::max(0.0, dot(ls.normal, -Ld));
+                    const R cosX = scatter ? 1.0 : std::max(0.0, dot(h.nrm, Ld)), cosY = std::max(0.0, dot(ls.normal, -Ld));
                     R vUn = 0;
                     bool validUn = false;
                     if (!(cosX <= 0 || cosY <= 0))
                     {
-                        const R f = eval_cos(sh, rayD, Ld, h.nrm);
+                        const R f = scatter ? S.med_albedo * hg_pdf(dot(rayD, Ld), S.med_g) : eval_cos(sh, rayD, Ld, h.nrm);
                         const R le = interact(L, lam, S.mats[lmat].emissive, nullptr);
                         const R contribution = f * le * ((cosY / dist2) / pAT);
                         const R pLight = area_to_omega(h.pos, ls.point, ls.normal, ls.p_facet * ls.p_a);
-                        const R pBsdf = std::max(bsdf_pdf(sh, h.nrm, rayD, Ld), 0.0);
-                        vUn = mask * (contribution * power(pLight, pBsdf)) * d65;
+                        const R pBsdf = scatter ? hg_pdf(dot(rayD, Ld), S.med_g) : std::max(bsdf_pdf(sh, h.nrm, rayD, Ld), 0.0);
+                        vUn = mask * (contribution * power(pLight, pBsdf)) * d65 * med_transmittance(S, h.pos, Ld, std::sqrt(dist2));
                         validUn = true;
                     }
                     V dirS = ls.point - h.pos;
@@ -1318,7 +1486,8 @@ static void xyz_of(const Scene& S, const PathOut& po, R out[3], bool on[3])
     }
 }
 
-static void run(const Scene& S, const Params& P, double* mean, double* per_sample, const double* dl, double* grad)
+static void run(const Scene& S, const Params& P, double* mean, double* per_sample, const double* dl, double* grad,
+                double* grad_med = nullptr)
 {
     const Cam cam = make_cam(P);
     bool cam_inside = false;
@@ -1328,6 +1497,7 @@ static void run(const Scene& S, const Params& P, double* mean, double* per_sampl
     const int nt = std::max(1, P.threads);
     std::atomic<long long> next(0);
     std::vector<std::vector<double>> gpart(grad ? nt : 0);
+    std::vector<std::array<double, 2>> mpart(nt, std::array<double, 2>{0.0, 0.0});
     auto work = [&](int tid) {
         LutCache L{&S.tab, {}};
         PathOut po;
@@ -1343,14 +1513,14 @@ static void run(const Scene& S, const Params& P, double* mean, double* per_sampl
             for (int s = 0; s < P.spp; ++s)
             {
                 const uint32_t frame = (uint32_t)(P.first_frame + s);
-                trace_path(S, L, P, cam, cam_inside, (uint32_t)pix, frame, grad != nullptr, &po);
+                trace_path(S, L, P, cam, cam_inside, (uint32_t)pix, frame, grad != nullptr || grad_med != nullptr, &po);
                 R c[3];
                 bool on[3];
                 xyz_of(S, po, c, on);
                 for (int k = 0; k < 3; ++k) acc[k] += c[k];
                 if (per_sample)
                     for (int k = 0; k < 3; ++k) per_sample[((size_t)s * npix + pix) * 3 + k] = c[k];
-                if (G)
+                if (G || grad_med)
                 {
                     const V xyz = lambda_to_xyz(S.tab, po.lambda);
                     const R xs[3] = {xyz.x, xyz.y, xyz.z};
@@ -1358,12 +1528,20 @@ static void run(const Scene& S, const Params& P, double* mean, double* per_sampl
                     for (int k = 0; k < 3; ++k)
                         if (on[k]) delta += dl[3 * pix + k] * xs[k] / po.pdf;
                     delta /= P.spp;
-                    for (const TexVertex& tv : po.tv)
+                    if (G)
+                        for (const TexVertex& tv : po.tv)
+                        {
+                            const R w = delta * (po.radiance - tv.before);
+                            (*G)[3 * (size_t)tv.texel + 0] += w * tv.dalb.x;
+                            (*G)[3 * (size_t)tv.texel + 1] += w * tv.dalb.y;
+                            (*G)[3 * (size_t)tv.texel + 2] += w * tv.dalb.z;
+                        }
+                    for (const MedVertex& mv : po.mv)
                     {
-                        const R w = delta * (po.radiance - tv.before);
-                        (*G)[3 * (size_t)tv.texel + 0] += w * tv.dalb.x;
-                        (*G)[3 * (size_t)tv.texel + 1] += w * tv.dalb.y;
-                        (*G)[3 * (size_t)tv.texel + 2] += w * tv.dalb.z;
+                        // what follows carries the albedo once; the emission here carries (1 - albedo)
+                        if (S.med_albedo > 1e-8) mpart[tid][0] += delta * (po.radiance - mv.after) / S.med_albedo;
+                        mpart[tid][0] -= delta * mv.mask * S.med_emission * mv.d65;
+                        mpart[tid][1] += delta * mv.mask * (1 - S.med_albedo) * mv.d65;
                     }
                 }
             }
@@ -1380,6 +1558,15 @@ static void run(const Scene& S, const Params& P, double* mean, double* per_sampl
         std::memset(grad, 0, S.texels.size() * sizeof(double));
         for (auto& g : gpart)
             for (size_t k = 0; k < g.size(); ++k) grad[k] += g[k];
+    }
+    if (grad_med)
+    {
+        grad_med[0] = grad_med[1] = 0.0;
+        for (auto& m : mpart)
+        {
+            grad_med[0] += m[0];
+            grad_med[1] += m[1];
+        }
     }
 }
 
@@ -1414,7 +1601,7 @@ int pt64_version(void) { return 1; }
 pt64_scene* pt64_create(const float* mats, int n_mat, const float* objs, int n_obj, const float* tri, const int32_t* tri_mat,
                         const float* tri_uv, int n_tri, const int32_t* tex_sizes, const float* texels, int n_tex,
                         const float* cmf, const float* d65, const float* rgb_mlp, int rgb_n, const float* lam_mlp, int lam_n,
-                        char* err, int err_len)
+                        const float* sdf, int n_sdf, float sdf_k, int sdf_mat, char* err, int err_len)
 {
     auto fail = [&](const char* m) -> pt64_scene* {
         if (err && err_len > 0)
@@ -1467,7 +1654,37 @@ pt64_scene* pt64_create(const float* mats, int n_mat, const float* objs, int n_o
         }
         S->mats.push_back(r);
     }
-    const int np = n_obj + n_tri;
+    const int np = n_obj + n_tri + (n_sdf > 0 ? 1 : 0);
+    if (n_sdf > 0)
+    {
+        for (int i = 0; i < n_sdf; ++i)
+        {
+            std::array<R, 7> q;
+            for (int k = 0; k < 7; ++k) q[k] = sdf[8 * (size_t)i + k];
+            S->sdf.push_back(q);
+            R h[3];
+            const int kind = (int)q[0];
+            if (kind == 0) h[0] = h[1] = h[2] = q[4];
+            else if (kind == 1)
+            {
+                h[0] = q[4];
+                h[1] = q[5];
+                h[2] = q[6];
+            }
+            else
+            {
+                h[0] = h[2] = q[4] + q[5];
+                h[1] = q[5];
+            }
+            for (int k = 0; k < 3; ++k)
+            {
+                const R pad = 0.25 * sdf_k + 1e-4 * (std::fabs(q[1 + k]) + h[k]) + 1e-6;
+                if (i == 0 || q[1 + k] - std::fabs(h[k]) - pad < S->sdf_lo[k]) S->sdf_lo[k] = q[1 + k] - std::fabs(h[k]) - pad;
+                if (i == 0 || q[1 + k] + std::fabs(h[k]) + pad > S->sdf_hi[k]) S->sdf_hi[k] = q[1 + k] + std::fabs(h[k]) + pad;
+            }
+        }
+        S->sdf_k = sdf_k;
+    }
     S->prim_type.resize(np);
     S->prim_mat.resize(np);
     S->objs.resize(np);
@@ -1479,7 +1696,12 @@ pt64_scene* pt64_create(const float* mats, int n_mat, const float* objs, int n_o
     {
         int type, mat;
         std::array<R, 9> T{};
-        if (i < n_obj)
+        if (i >= n_obj + n_tri)
+        {
+            type = OBJ_SDF;
+            mat = sdf_mat;
+        }
+        else if (i < n_obj)
         {
             const float* o = objs + 20 * (size_t)i;
             type = (int)o[0];
@@ -1515,6 +1737,12 @@ pt64_scene* pt64_create(const float* mats, int n_mat, const float* objs, int n_o
             {
                 S->lo[i][k] = std::min(T[k], std::min(T[3 + k], T[6 + k]));
                 S->hi[i][k] = std::max(T[k], std::max(T[3 + k], T[6 + k]));
+            }
+        else if (type == OBJ_SDF)
+            for (int k = 0; k < 3; ++k)
+            {
+                S->lo[i][k] = S->sdf_lo[k];
+                S->hi[i][k] = S->sdf_hi[k];
             }
         else
         {
@@ -1615,6 +1843,36 @@ int pt64_render(const pt64_scene* s, const int32_t* ip, const double* dp, uint64
     const Params P = to_params(ip, dp, seed);
     if (P.width <= 0 || P.height <= 0 || P.spp <= 0 || P.max_depth <= 0) return -1;
     run(*reinterpret_cast<const Scene*>(s), P, mean, per_sample, nullptr, nullptr);
+    return 0;
+}
+
+void pt64_set_medium(pt64_scene* s, const double* m)
+{
+    Scene* S = reinterpret_cast<Scene*>(s);
+    if (!m)
+    {
+        S->med_on = false;
+        return;
+    }
+    S->med_on = true;
+    for (int k = 0; k < 3; ++k)
+    {
+        S->med_lo[k] = m[k];
+        S->med_hi[k] = m[3 + k];
+    }
+    S->med_sigma = m[6];
+    S->med_albedo = m[7];
+    S->med_g = m[8];
+    S->med_emission = m[9];
+}
+
+int pt64_adjoint_medium(const pt64_scene* s, const int32_t* ip, const double* dp, uint64_t seed, const double* dl_dxyz,
+                        double* grad2)
+{
+    if (!s || !ip || !dp || !dl_dxyz || !grad2) return -1;
+    const Params P = to_params(ip, dp, seed);
+    if (P.width <= 0 || P.height <= 0 || P.spp <= 0 || P.max_depth <= 0) return -1;
+    run(*reinterpret_cast<const Scene*>(s), P, nullptr, nullptr, dl_dxyz, nullptr, grad2);
     return 0;
 }
 

@@ -40,7 +40,10 @@ def load() -> C.CDLL:
         vp, i32 = C.c_void_p, C.c_int
         lib.pt64_create.restype = vp
         lib.pt64_create.argtypes = [vp, i32, vp, i32, vp, vp, vp, i32, vp, vp, i32, vp, vp, vp, i32, vp, i32,
-                                    C.c_char_p, i32]
+                                    vp, i32, C.c_float, i32, C.c_char_p, i32]
+        lib.pt64_set_medium.argtypes = [vp, vp]
+        lib.pt64_adjoint_medium.restype = i32
+        lib.pt64_adjoint_medium.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
         lib.pt64_destroy.argtypes = [vp]
         lib.pt64_render.restype = i32
         lib.pt64_render.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
@@ -73,7 +76,7 @@ def _material_row(m) -> list:
 class Scene64:
     """An FP64 oracle scene built from the product's scene description classes."""
 
-    def __init__(self, objects, mesh=None, textures=None):
+    def __init__(self, objects, mesh=None, textures=None, sdf=None, medium=None):
         lib = load()
         objects = list(objects)
         table: dict = {}
@@ -97,6 +100,10 @@ class Scene64:
             tri_mat = remap[np.asarray(mesh.material_ids, np.int64)].astype(np.int32)
             if mesh.uv is not None:
                 tri_uv = np.ascontiguousarray(mesh.uv, np.float32).reshape(-1, 6)
+        sdf_arr, sdf_mat = None, -1
+        if sdf is not None:
+            sdf_mat = mid(sdf.material)
+            sdf_arr = sdf.array()
         m_arr = np.ascontiguousarray(np.array([_material_row(m) for m in mats], np.float32).reshape(-1, 14))
         o_arr = np.ascontiguousarray(np.array(orows, np.float32).reshape(-1, 20))
         textures = list(textures) if textures is not None else []
@@ -106,14 +113,25 @@ class Scene64:
         self.texel_count = int(sum(t.size for t in textures))
         cmf, d65, rgb, lam = _tables()
         err = C.create_string_buffer(256)
-        keep = [m_arr, o_arr, tri, tri_mat, tri_uv, sizes, texels, cmf, d65, rgb, lam]
+        keep = [m_arr, o_arr, tri, tri_mat, tri_uv, sizes, texels, cmf, d65, rgb, lam, sdf_arr]
         self._keep = keep
         ptr = lambda a: None if a is None or a.size == 0 else a.ctypes.data
         self._h = lib.pt64_create(ptr(m_arr), len(m_arr), ptr(o_arr), len(o_arr), ptr(tri), ptr(tri_mat), ptr(tri_uv),
                                   len(tri), ptr(sizes), texels.ctypes.data, len(textures), cmf.ctypes.data,
-                                  d65.ctypes.data, rgb.ctypes.data, rgb.size, lam.ctypes.data, lam.size, err, 256)
+                                  d65.ctypes.data, rgb.ctypes.data, rgb.size, lam.ctypes.data, lam.size,
+                                  ptr(sdf_arr), 0 if sdf_arr is None else len(sdf_arr),
+                                  0.0 if sdf is None else float(sdf.smooth_k), sdf_mat, err, 256)
         if not self._h:
             raise ValueError(f"FP64 oracle: {err.value.decode()}")
+        self.set_medium(medium)
+
+    def set_medium(self, medium):
+        if medium is None:
+            load().pt64_set_medium(self._h, None)
+            return
+        m = np.array([*medium.box_lo, *medium.box_hi, medium.sigma_t, medium.albedo, medium.g, medium.emission],
+                     np.float64)
+        load().pt64_set_medium(self._h, m.ctypes.data)
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -139,6 +157,18 @@ class Scene64:
         if rc != 0:
             raise ValueError("FP64 oracle: bad render parameters")
         return (mean, ps) if per_sample else mean
+
+    def adjoint_medium(self, dl_dxyz, size, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
+                       seed=0x9E3779B97F4A7C15, first_frame=0, threads=0):
+        """(d loss / d medium albedo, d loss / d medium emission) given d(loss)/d(mean image)."""
+        ip, dp = self._params(size, origin, direction, spp, fov, max_depth, use_nee, first_frame,
+                              threads or os.cpu_count() or 1)
+        dl = np.ascontiguousarray(dl_dxyz, np.float64)
+        g = np.zeros(2, np.float64)
+        rc = load().pt64_adjoint_medium(self._h, ip.ctypes.data, dp.ctypes.data, seed, dl.ctypes.data, g.ctypes.data)
+        if rc != 0:
+            raise ValueError("FP64 oracle: bad adjoint parameters")
+        return float(g[0]), float(g[1])
 
     def adjoint(self, dl_dxyz, size, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
                 seed=0x9E3779B97F4A7C15, first_frame=0, threads=0):
