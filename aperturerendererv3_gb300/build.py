@@ -27,8 +27,6 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["capi.cu", "render.cu", "trace.cu", "noalloc.cu", "guide.cu", "adjoint.cu", "mlp.cu"]
 CPP_SOURCES = ["bvh_build.cpp"]
-HEADERS = ["ar_bvh.h", "ar_bvh_build.h", "ar_detmath.h", "ar_geom.h", "ar_guide.h", "ar_internal.h", "ar_rng.h",
-           "ar_shade.h", "ar_spectral.h", "ar_traverse.cuh", "ar_vec.h"]
 
 
 def nvcc() -> str:
@@ -84,8 +82,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     write_tables(BUILD / "spectral_tables.inc")
     nv = nvcc()
     common = ["-std=c++17", "-O3", "-I", str(CSRC), "-I", str(BUILD), "-I", str(REPO / "include")]
-    deps = [CSRC / h for h in HEADERS] + [BUILD / "spectral_tables.inc", REPO / "include" / "aperture" / "ar.h",
-                                          Path(__file__)]
+    # every header of csrc/ counts: a translation unit is rebuilt when any of them changes
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh"))
+    deps = headers + [BUILD / "spectral_tables.inc", REPO / "include" / "aperture" / "ar.h", Path(__file__)]
     jobs = []
     for src in CU_SOURCES:
         obj = BUILD / (src + ".o")

@@ -243,6 +243,7 @@ struct Ctx
     int sdf_material = -1;
     float4* d_sdf = nullptr;
     SdfUnion sdf{};
+    int sdf_id = -1;                     // primitive id of the SDF object
     BoxMedium medium{};
     // wavefront buffers
     PathState ps{};

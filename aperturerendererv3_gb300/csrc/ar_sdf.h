@@ -67,11 +67,20 @@ AR_HD bool sdf_bounds_interval(const SdfUnion& s, V3 o, V3 d, float* t0, float* 
     return *t0 <= *t1 && *t1 > 0.0f;
 }
 
-// distance to the first surface crossing in the bounds, or -1
-AR_HD float sdf_march(const SdfUnion& s, V3 o, V3 d, float eps)
+// The march and the normal are called out of line: inlined into the BVH
+// traversal loop they would raise its register count for every ray.
+#if defined(__CUDACC__)
+#define AR_SDF_CALL static __host__ __device__ __noinline__
+#else
+#define AR_SDF_CALL inline
+#endif
+
+// distance to the first surface crossing in the bounds before tmax, or -1
+AR_SDF_CALL float sdf_march(const SdfUnion& s, V3 o, V3 d, float eps, float tmax)
 {
     float t0, t1;
-    if (s.count <= 0 || !sdf_bounds_interval(s, o, d, &t0, &t1)) return -1.0f;
+    if (s.count <= 0 || !sdf_bounds_interval(s, o, d, &t0, &t1) || t0 >= tmax) return -1.0f;
+    t1 = fminf(t1, tmax);
     const bool start_inside = sdf_union(s, o) <= 0.0f;
     const float min_step = eps * 0.5f;
     float t = fmaxf(0.0f, t0);
@@ -87,7 +96,7 @@ AR_HD float sdf_march(const SdfUnion& s, V3 o, V3 d, float eps)
 }
 
 // outward normal by central differences (sdfNormalUnit, core/object/sdf/sdf_base.cuh:40-51)
-AR_HD V3 sdf_normal(const SdfUnion& s, V3 p, float h)
+AR_SDF_CALL V3 sdf_normal(const SdfUnion& s, V3 p, float h)
 {
     const float dx = sdf_union(s, p + v3(h, 0, 0)) - sdf_union(s, p - v3(h, 0, 0));
     const float dy = sdf_union(s, p + v3(0, h, 0)) - sdf_union(s, p - v3(0, h, 0));

@@ -27,8 +27,12 @@ struct TravScene
     const float4* __restrict__ slots;      // 3 float4 per primitive slot
     const Object* __restrict__ objects;    // analytic object table, indexed by primitive id
     int node_count;
-    SdfUnion sdf;                          // the smooth-union SDF object (count 0: none)
+    SdfUnion sdf;                          // the smooth-union SDF object (count 0: none); not in the BVH
+    int sdf_id;                            // its primitive id
 };
+
+// hit slot of the SDF object (marched after the BVH traversal)
+#define AR_SLOT_SDF (-2)
 
 // SDF march tolerance for a ray starting at intersect_eps-sized offsets (SDF_EPS, core/config.cuh:74)
 AR_HD float sdf_eps(float tmin) { return 0.5f * fmaxf(tmin, 1.0e-3f); }
@@ -82,7 +86,7 @@ AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3
         if (tri_intersect(sh, o, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &t, &b0, &b1, &b2)) return t;
         return -1.0f;
     }
-    if (kind == AR_PRIM_KIND_SDF) return sdf_march(sc.sdf, o, d, sdf_eps(tmin));
+    (void)tmin;
     const Object ob = sc.objects[id];
     Hit h;
     h.hit = false;

@@ -47,6 +47,7 @@ DevScene dev_scene(const Ctx& c)
     s.stats = (c.profile & 2) ? c.d_stats : nullptr;
     s.guide = c.guide;
     s.trav.sdf = c.sdf;
+    s.trav.sdf_id = c.sdf_id;
     s.medium = c.medium;
     s.texels = c.d_texels;
     s.tex_info = c.d_tex_info;
@@ -806,6 +807,7 @@ ar_status ar_scene_build(ar_ctx* ctx)
     const long long nprim = (long long)nobj + nmesh + nsdf;
     const int nmat = (int)c.materials.size();
     if (nprim == 0) return fail(ctx, AR_ERR_INVALID, "scene is empty");
+    if ((long long)nobj + nmesh == 0) return fail(ctx, AR_ERR_INVALID, "scene has no object or triangle besides the SDF");
     for (int i = 0; i < nobj; ++i)
         if (c.object_material[i] < 0 || c.object_material[i] >= nmat) return fail(ctx, AR_ERR_INVALID, "object material index out of range");
     for (int i = 0; i < nmesh; ++i)
@@ -844,10 +846,12 @@ ar_status ar_scene_build(ar_ctx* ctx)
         }
     }
 
-    // primitives for the BVH
-    std::vector<arbvh::PrimInput> prims((size_t)nprim);
+    // primitives for the BVH (the SDF object, if any, is marched after the BVH traversal)
+    const long long nbvh = (long long)nobj + nmesh;
+    std::vector<arbvh::PrimInput> prims((size_t)nbvh);
     std::vector<int> prim_material((size_t)nprim), prim_light((size_t)nprim, -1);
-    for (long long i = 0; i < nprim; ++i)
+    if (nsdf) prim_material[nbvh] = c.sdf_material;
+    for (long long i = 0; i < nbvh; ++i)
     {
         arbvh::PrimInput& p = prims[i];
         p.id = (uint32_t)i;
@@ -862,20 +866,10 @@ ar_status ar_scene_build(ar_ctx* ctx)
                 object_bounds(c.objects[i], p.lo, p.hi);
             }
         }
-        else if (i < (long long)nobj + nmesh)
+        else
         {
             prim_material[i] = c.mesh_material[i - nobj];
             tv = &c.mesh_v[9 * (size_t)(i - nobj)];
-        }
-        else
-        {
-            prim_material[i] = c.sdf_material;
-            p.kind = AR_PRIM_KIND_SDF;
-            for (int k = 0; k < 3; ++k)
-            {
-                p.lo[k] = sdf_lo[k];
-                p.hi[k] = sdf_hi[k];
-            }
         }
         if (tv)
         {
@@ -996,6 +990,7 @@ ar_status ar_scene_build(ar_ctx* ctx)
         c.sdf.k = c.sdf_k;
         c.sdf.lo = v3(sdf_lo[0], sdf_lo[1], sdf_lo[2]);
         c.sdf.hi = v3(sdf_hi[0], sdf_hi[1], sdf_hi[2]);
+        c.sdf_id = (int)nbvh;
     }
     std::vector<Material> mats(c.materials);
     AR_CUDA(ctx, alloc_dev(c.d_materials, std::max<size_t>(mats.size(), 1)));
@@ -1362,6 +1357,7 @@ ar_status ar_host_trace_closest(const float* tris, int ntri, const float* rays, 
     sc.objects = nullptr;
     sc.node_count = (int)bvh.nodes.size();
     sc.sdf = SdfUnion{};
+    sc.sdf_id = -1;
     unsigned int errw = 0;
     unsigned long long stats[2] = {0, 0};
     for (int r = 0; r < nray; ++r)

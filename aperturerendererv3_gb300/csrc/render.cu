@@ -92,6 +92,18 @@ cudaError_t launch_prepare_materials(Material* mats, int n, const float* lut, cu
 // Full hit record for primitive slot `slot` at distance t (the traversal's t).
 __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, V3 d, float t, Hit* h)
 {
+    if (slot == AR_SLOT_SDF)
+    {
+        const int id = sc.trav.sdf_id;
+        h->hit = true;
+        h->obj = id;
+        h->light = sc.prim_light[id];
+        h->dist = t;
+        h->pos = o + d * t;
+        h->nrm = sdf_normal(sc.trav.sdf, h->pos, 1.0e-4f);
+        h->local_pos = h->pos;
+        return;
+    }
     const float4 a = __ldg(&sc.trav.slots[3 * (size_t)slot + 0]);
     const uint32_t tag = __float_as_uint(a.w);
     const uint32_t kind = tag >> AR_PRIM_KIND_SHIFT;
@@ -107,12 +119,6 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
         tri_frame(o, d, t, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &h->pos, &h->nrm);
         h->local_pos = v3(0.0f, 0.0f, 0.0f);
     }
-    else if (kind == AR_PRIM_KIND_SDF)
-    {
-        h->pos = o + d * t;
-        h->nrm = sdf_normal(sc.trav.sdf, h->pos, 1.0e-4f);
-        h->local_pos = h->pos;
-    }
     else
     {
         const Object ob = sc.trav.objects[id];
@@ -126,6 +132,7 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
 // texel index (in RGB units) or -1 when the primitive is not a triangle.
 __device__ __forceinline__ int albedo_texel(const DevScene& sc, int tex, int slot, int prim, V3 pos)
 {
+    if (slot < 0) return -1;
     const float4 a = __ldg(&sc.trav.slots[3 * (size_t)slot + 0]);
     if ((__float_as_uint(a.w) >> AR_PRIM_KIND_SHIFT) != AR_PRIM_KIND_TRI) return -1;
     const float4 b = __ldg(&sc.trav.slots[3 * (size_t)slot + 1]);
@@ -234,6 +241,16 @@ __global__ void __launch_bounds__(AR_BLOCK) k_extend(DevScene sc, PathState ps, 
                                                  sc.stats ? sc.stats + 0 : nullptr);
             t = r.t;
             slot = r.slot;
+            if (sc.trav.sdf.count > 0)
+            {
+                // the SDF object has the largest primitive id: a BVH hit at equal t wins
+                const float ts = sdf_march(sc.trav.sdf, o, d, sdf_eps(tmin), slot < 0 ? 3.0e38f : t);
+                if (ts >= tmin && (slot < 0 || ts < t))
+                {
+                    t = ts;
+                    slot = AR_SLOT_SDF;
+                }
+            }
         }
         if (sc.stats) atomicAdd(&sc.stats[4], 1ull);
         ps.hit_t[p] = t;
@@ -260,7 +277,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_mlp_query(DevScene sc, PathState p
             p = queue[q];
             const int slot = ps.hit_slot[p];
             const int ndd = (int)(ps.depths[p] >> 16);
-            want = slot >= 0 && ndd < AR_MLP_MAX_NDD && (ps.flags[p] & 1u) == 0u;
+            want = slot != -1 && ndd < AR_MLP_MAX_NDD && (ps.flags[p] & 1u) == 0u;
             if (want)
             {
                 const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
@@ -398,7 +415,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
             h.pos = v3(0, 0, 0);
             h.nrm = v3(0, 0, 0);
             h.local_pos = v3(0, 0, 0);
-            if (slot >= 0) hit_context(sc, slot, rayO, rayD, ps.hit_t[p], &h);
+            if (slot != -1) hit_context(sc, slot, rayO, rayD, ps.hit_t[p], &h);
 
             // ---- participating medium: a free flight sampled in the medium box
             // ends the segment early with probability 1 - transmittance
@@ -857,7 +874,12 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shadow(DevScene sc, PathState ps, 
         const TravResult r = traverse<true>(sc.trav, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, o.w, err,
                                             sc.stats ? sc.stats + 2 : nullptr);
         if (sc.stats) atomicAdd(&sc.stats[5], 1ull);
-        const bool occluded = r.slot >= 0;
+        bool occluded = r.slot >= 0;
+        if (!occluded && sc.trav.sdf.count > 0)
+        {
+            const float ts = sdf_march(sc.trav.sdf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), sdf_eps(0.0f), o.w);
+            occluded = ts >= 0.0f && ts < o.w;
+        }
         ps.radiance[p] = ps.radiance[p] + (occluded ? sq.v_occ[i] : d.w);
         const bool valid = occluded ? true : (sq.valid_unocc[i] != 0);
         ps.flags[p] = (ps.flags[p] & ~2u) | (valid ? 2u : 0u);

@@ -15,15 +15,27 @@ __global__ void __launch_bounds__(256) k_trace(TravScene sc, const float4* __res
     {
         const float4 a = __ldg(&rays[2 * (size_t)i]);
         const float4 b = __ldg(&rays[2 * (size_t)i + 1]);
-        const TravResult r = traverse<AnyHit>(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, err);
+        const V3 o = v3(a.x, a.y, a.z), d = v3(b.x, b.y, b.z);
+        TravResult r = traverse<AnyHit>(sc, o, d, a.w, b.w, err);
+        if (sc.sdf.count > 0 && (!AnyHit || r.slot < 0))
+        {
+            // the SDF object (largest primitive id: a BVH hit at equal t wins)
+            const float ts = sdf_march(sc.sdf, o, d, sdf_eps(a.w), r.slot < 0 ? b.w : r.t);
+            if (ts >= a.w && ts < b.w && (r.slot < 0 || ts < r.t))
+            {
+                r.t = ts;
+                r.slot = AR_SLOT_SDF;
+                r.id = sc.sdf_id;
+            }
+        }
         if (AnyHit)
         {
-            out[i] = r.slot >= 0 ? 1 : 0;
+            out[i] = r.slot != -1 ? 1 : 0;
         }
         else
         {
             out[i] = r.id;
-            if (tout) tout[i] = r.slot >= 0 ? r.t : -1.0f;
+            if (tout) tout[i] = r.slot != -1 ? r.t : -1.0f;
         }
     }
 }

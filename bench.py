@@ -43,16 +43,23 @@ WORKLOADS = {
     "cornell": dict(size=(256, 256), spp=16, depth=8),
     # 1920x1080, 64 spp, depth 16 terrain (8.4M triangles), 64 sphere lights + sun
     "terrain": dict(size=(1920, 1080), spp=64, depth=16),
+    # the terrain with 32 smooth-union SDF primitives in a participating medium,
+    # 3840x2160, 256 spp, depth 24, MLP guide with the voxel guide as fallback
+    "combined": dict(size=(3840, 2160), spp=256, depth=24, guide=2),
 }
 
 
 def build_workload(name: str):
+    """(objects, mesh, camera, extra SceneRenderer arguments)."""
     from aperturerendererv3_gb300 import configs
     if name == "cornell":
-        return configs.cornell_triangles(), None, configs.CORNELL_CAMERA
+        return configs.cornell_triangles(), None, configs.CORNELL_CAMERA, {}
     if name == "terrain":
         objs, mesh = configs.terrain_scene()
-        return objs, mesh, configs.TERRAIN_CAMERA
+        return objs, mesh, configs.TERRAIN_CAMERA, {}
+    if name == "combined":
+        objs, mesh, sdf, med = configs.combined_scene()
+        return objs, mesh, configs.COMBINED_CAMERA, dict(sdf=sdf, medium=med)
     raise KeyError(name)
 
 
@@ -147,7 +154,10 @@ def run_reference(args, w) -> dict:
     sample of the same workload.  One oracle call renders warmup + steps frames
     of the sample (its BVH is built once per call, outside the timed loop, as
     the reference builds its BVH before rendering)."""
-    objs, mesh, cam = build_workload(args.workload)
+    if args.workload == "combined":
+        return {"impl": "reference", "unavailable": "the reference integrator has no participating media and no "
+                "smooth-union SDF objects (the combined workload's features)"}
+    objs, mesh, cam, _ = build_workload(args.workload)
     threads = os.cpu_count() or 1
     size = w["size"]
     sample_size, sample_spp = reference_sample(args.workload, size)
@@ -266,6 +276,33 @@ def adjoint_extra(device: int, steps: int) -> dict:
             "loss": float(((img - target) ** 2).sum()), "workload": "textured Cornell 256x256, 64 spp, depth 8"}
 
 
+def combined_extra(device: int, spp: int = 16) -> dict:
+    """The combined workload (terrain + 32-primitive smooth-union SDF + medium,
+    3840x2160, depth 24, MLP guide over the voxel guide) at `spp` frames per
+    render, and the replay adjoint of the medium's albedo and emission."""
+    import torch
+    from aperturerendererv3_gb300 import SceneRenderer
+    objs, mesh, cam, extra = build_workload("combined")
+    r = SceneRenderer(objs, device=device, mesh=mesh, **extra)
+    r.build()
+    size, depth = (3840, 2160), 24
+    kw = dict(fov=cam["fov"], max_depth=depth)
+    r.Render(size, cam["origin"], cam["direction"], 2, guide=2, **kw)
+    img = r.Render(size, cam["origin"], cam["direction"], spp, guide=2, first_frame=2, **kw)
+    ms = r.last_render_stats()[0]
+    out = {"value": size[0] * size[1] * spp / (ms / 1e3) / 1e6, "unit": "Msamples/s", "ms": ms, "spp": spp,
+           "mlp_steps": r.mlp_stats()[0], "error_word": r.error_word()}
+    r.MarkNeedResetGuiding()
+    # medium adjoint of a plain render (guided rendering is not differentiated), 4 spp
+    plain = r.Render(size, cam["origin"], cam["direction"], 4, **kw)
+    target = np.full_like(plain, plain.mean())
+    dl = torch.as_tensor(2.0 * (plain - target), device=f"cuda:{device}").float()
+    ga, ge = r.adjoint_medium(dl, size, cam["origin"], cam["direction"], 4, **kw)
+    out["adjoint_medium"] = {"ms": r.last_render_stats()[0], "spp": 4, "d_albedo": ga, "d_emission": ge}
+    r.close()
+    return out
+
+
 def bvh_stress_extra(device: int, steps: int) -> dict:
     """BVH stress workload: 1M random triangles (centroids U[0,1]^3, vertices
     +N(0, 0.005^2)), 1920x1080 primary rays plus one cosine-hemisphere bounce ray
@@ -359,8 +396,10 @@ def main() -> None:
     torch.cuda.set_device(local)
     from aperturerendererv3_gb300 import SceneRenderer
 
-    objs, mesh, cam = build_workload(args.workload)
-    r = SceneRenderer(objs, device=local, mesh=mesh)
+    objs, mesh, cam, extra_args = build_workload(args.workload)
+    r = SceneRenderer(objs, device=local, mesh=mesh, **extra_args)
+    if "guide" in w and args.guide == 0:
+        args.guide = w["guide"]
     r.build()
     size, spp, depth = w["size"], w["spp"], w["depth"]
     samples = size[0] * size[1] * spp
@@ -441,6 +480,8 @@ def main() -> None:
         for name, fn in (("guided_voxel", lambda: guided_extra(r, w, cam, 3)),
                          ("guide_compare", lambda: guide_compare_extra(r, w, cam)),
                          ("adjoint", lambda: adjoint_extra(local, 3)),
+                         ("combined", lambda: combined_extra(local) if args.workload != "combined" else
+                          {"note": "the headline is the combined workload"}),
                          ("bvh_stress", lambda: bvh_stress_extra(local, 5))):
             try:
                 extras[name] = fn()
