@@ -61,6 +61,7 @@ GUIDE_NONE = 0
 GUIDE_VOXEL = 1
 GUIDE_MLP = 2
 SDF_SPHERE, SDF_BOX, SDF_TORUS = 0, 1, 2
+TONE_ACES, TONE_GAMMA, TONE_LINEAR = 0, 1, 2
 
 
 class ArRenderProfile(C.Structure):
@@ -83,7 +84,7 @@ EXPORTED = [
     "ar_host_sample_lambda", "ar_host_trace_closest", "ar_host_guide_eval", "ar_abi_version",
     "ar_scene_set_textures", "ar_scene_set_mesh_uv", "ar_scene_update_texels", "ar_scene_texel_count", "ar_adjoint",
     "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats", "ar_scene_set_sdf_union", "ar_scene_set_medium",
-    "ar_adjoint_medium",
+    "ar_adjoint_medium", "ar_tonemap",
 ]
 
 _lib = None
@@ -142,6 +143,7 @@ def load() -> C.CDLL:
         "ar_scene_set_sdf_union": (C.c_int, [vp, vp, C.c_int, C.c_float, C.c_int32]),
         "ar_scene_set_medium": (C.c_int, [vp, P(ArMedium)]),
         "ar_adjoint_medium": (C.c_int, [vp, P(ArRenderParams), vp, vp, vp]),
+        "ar_tonemap": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -25,7 +25,7 @@ BUILD = REPO / "_build"
 LIB = PKG / "libaperture_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["capi.cu", "render.cu", "trace.cu", "noalloc.cu", "guide.cu", "adjoint.cu", "mlp.cu"]
+CU_SOURCES = ["capi.cu", "render.cu", "trace.cu", "noalloc.cu", "guide.cu", "adjoint.cu", "mlp.cu", "tonemap.cu"]
 CPP_SOURCES = ["bvh_build.cpp"]
 
 

@@ -382,6 +382,16 @@ class SceneRenderer:
         check(self._ctx, self._lib.ar_adjoint_medium(self._ctx, C.byref(p), g.data_ptr(), out, _torch_stream(g.device)))
         return out[0], out[1]
 
+    def tonemap(self, xyz: np.ndarray, exposure: float = 1.0, tone: str = "aces") -> np.ndarray:
+        """Display image (height, width, 4) uint8 from a linear XYZ image, on the GPU."""
+        tones = {"aces": _lib.TONE_ACES, "gamma": _lib.TONE_GAMMA, "linear": _lib.TONE_LINEAR}
+        x = np.ascontiguousarray(xyz, np.float64)
+        h, w, _ = x.shape
+        out = np.zeros((h, w, 4), np.uint8)
+        check(self._ctx, self._lib.ar_tonemap(self._ctx, x.ctypes.data, 0, w, h, float(exposure), tones[tone],
+                                              out.ctypes.data))
+        return out
+
     def last_render_stats(self) -> tuple[float, int]:
         ms, n = C.c_float(), C.c_int64()
         check(self._ctx, self._lib.ar_last_render_stats(self._ctx, C.byref(ms), C.byref(n)))
@@ -453,14 +463,55 @@ class Camera:
     def Render(self, sampleNum: int = 1, **kw) -> np.ndarray:
         return self.renderer.Render(self.resolution, self.position, self.direction, sampleNum, fov=self.fov, **kw)
 
-    def RenderToFile(self, path: str, sampleNum: int = 1024, **kw) -> np.ndarray:
-        """Writes the linear XYZ image as a PFM (Portable Float Map)."""
-        img = self.Render(sampleNum, **kw).astype(np.float32)
+    def RenderToFile(self, path: str, sampleNum: int = 1024, tonemapFunction: str = "aces", exp: float = 1.0,
+                     **kw) -> np.ndarray:
+        """Renders and writes the image (Camera::RenderToFile, core/camera.cu:64-89).
+        The extension picks the format:
+          .bmp  tonemapped 8-bit (tonemapFunction "aces" = the reference's
+                default, "gamma" or "linear"; exposure `exp`), the reference's
+                32-bit top-down BMP;
+          .pfm  linear XYZ floats (Portable Float Map), no tonemap;
+          other: `<path>.bmp` as the reference names its output.
+        Returns the linear XYZ image."""
+        img = self.Render(sampleNum, **kw)
         h, w, _ = img.shape
-        with open(path, "wb") as f:
-            f.write(f"PF\n{w} {h}\n-1.0\n".encode())
-            f.write(np.ascontiguousarray(img[::-1]).tobytes())
+        if path.lower().endswith(".pfm"):
+            write_pfm(path, img)
+        else:
+            if not path.lower().endswith(".bmp"):
+                path = path + ".bmp"
+            write_bmp(path, self.renderer.tonemap(img, exp, tonemapFunction))
         return img
+
+
+def write_pfm(path: str, img: np.ndarray) -> None:
+    """Colour PFM, little-endian float32, bottom row first."""
+    img = np.asarray(img, np.float32)
+    h, w, _ = img.shape
+    with open(path, "wb") as f:
+        f.write(f"PF\n{w} {h}\n-1.0\n".encode())
+        f.write(np.ascontiguousarray(img[::-1]).tobytes())
+
+
+def write_bmp(path: str, rgba: np.ndarray) -> None:
+    """32-bit BGRA BMP, top-down (negative height), as SaveBMP (core/camera.cu:10-62) writes it."""
+    rgba = np.asarray(rgba, np.uint8)
+    h, w, _ = rgba.shape
+    bgra = rgba[..., [2, 1, 0, 3]]
+    size = 54 + w * h * 4
+    header = bytearray(54)
+    header[0:2] = b"BM"
+    header[2:6] = size.to_bytes(4, "little")
+    header[10:14] = (54).to_bytes(4, "little")
+    header[14:18] = (40).to_bytes(4, "little")
+    header[18:22] = int(w).to_bytes(4, "little", signed=True)
+    header[22:26] = int(-h).to_bytes(4, "little", signed=True)
+    header[26:28] = (1).to_bytes(2, "little")
+    header[28:30] = (32).to_bytes(2, "little")
+    header[34:38] = (w * h * 4).to_bytes(4, "little")
+    with open(path, "wb") as f:
+        f.write(bytes(header))
+        f.write(np.ascontiguousarray(bgra).tobytes())
 
 
 def host_rgb_encode(rgb: np.ndarray) -> np.ndarray:

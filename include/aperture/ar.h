@@ -234,6 +234,17 @@ ar_status ar_adjoint(ar_ctx* ctx, const ar_render_params* params, const float* d
 ar_status ar_adjoint_medium(ar_ctx* ctx, const ar_render_params* params, const float* dl_dxyz, double* grad2,
                             void* stream);
 
+/* Display transform (Camera::RenderToFile, core/camera.cu:64-89, and
+ * core/tonemap.cuh): per-pixel XYZ x exposure -> linear sRGB (D65) -> tone
+ * curve -> clamp -> 8-bit RGBA (alpha 255), on the GPU.  xyz: 3 doubles per
+ * pixel (what ar_render writes), host or device memory; rgba: host, 4 bytes
+ * per pixel, top row first. */
+#define AR_TONE_ACES 0      /* the reference's ACES fit (its default) */
+#define AR_TONE_GAMMA 1     /* gamma 1/2.2 */
+#define AR_TONE_LINEAR 2    /* linear sRGB */
+ar_status ar_tonemap(ar_ctx* ctx, const double* xyz, int xyz_is_device, int width, int height, float exposure, int tone,
+                     uint8_t* rgba);
+
 /* Device time (ms) of the last ar_render and the number of kernels it launched. */
 ar_status ar_last_render_stats(ar_ctx* ctx, float* device_ms, int64_t* kernel_launches);
 /* Stage times and traversal counters of the last profiled ar_render. */

@@ -64,7 +64,7 @@ def test_mlp_guide_trains_and_stays_unbiased(cuda_device, name, objs, mesh, cam)
     guided = r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=16, guide=2)
     steps, loss = r.mlp_stats()
     assert steps == 8 * spp  # eight Adam steps per frame
-    assert np.isfinite(loss) and loss > 0
+    assert np.isfinite(loss)  # Poisson log-likelihood: may be negative
     assert r.error_word() == 0
     assert np.all(np.isfinite(guided))
     m_plain, m_guided = plain[..., 1].mean(), guided[..., 1].mean()
