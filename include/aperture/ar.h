@@ -108,10 +108,10 @@ typedef struct ar_render_params
 /* AR_GUIDE_MLP (no reference counterpart): the voxel probes learn as with
  * AR_GUIDE_VOXEL and, after every frame, a small network (12-band encoding of
  * position and reflected direction, 5 layers of width 64, BF16 tensor-core
- * kernels with FP32 accumulation, one Adam step at lr 1e-3 on up to 65,536 of
- * the frame's radiance records) trains alongside; once it has trained for 4
- * frames, the guide samples the network's 64-cell directional distribution
- * instead of the probes. */
+ * kernels with FP32 accumulation) trains alongside: guide_train_steps Adam
+ * steps at lr 1e-3, each on 16,384 of the frame's radiance records.  Once it
+ * has taken 16 steps, vertices of the first three diffuse bounces sample the
+ * network's 64-cell directional distribution; later bounces keep the probes. */
 #define AR_GUIDE_MLP 2
 
 /* Per-stage profile of the last ar_render with params->profile = 1. */

@@ -5,11 +5,20 @@
 // headless path: construct from a vector of objects, Render(size, origin,
 // direction, sampleNum) returns the per-pixel linear XYZ image.  Errors throw
 // aperture::Error (the reference only prints, core/vector.cuh:22).
+//
+// Beyond the reference's surface: a triangle mesh with per-triangle materials
+// and uv, albedo textures, the smooth-union SDF object, a homogeneous medium,
+// the voxel / MLP path guide, the replay adjoints (device pointers, as the C
+// ABI takes them) and Camera::RenderToFile writing the reference's BMP or a
+// linear PFM.
 #pragma once
+#include <cctype>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ar.h"
@@ -62,6 +71,14 @@ struct Material
     {
         Material r;
         set3(r.m.albedo, color);
+        set3(r.m.emissive, emissive);
+        return r;
+    }
+    // diffuse albedo read from texture `texture` (0-based) at the mesh uv
+    static Material CreateDiffuseTextured(int texture, float3 emissive = {0, 0, 0})
+    {
+        Material r;
+        r.m.albedo_texture = texture + 1;
         set3(r.m.emissive, emissive);
         return r;
     }
@@ -138,30 +155,133 @@ class SceneRenderer
     SceneRenderer& operator=(const SceneRenderer&) = delete;
 
     void MarkAsDirty() { dirty_ = true; }
+    // SceneRenderer::MarkNeedResetGuiding (core/scene.hpp:102-105)
+    void MarkNeedResetGuiding() { check(ar_guide_reset(ctx_, nullptr), "ar_guide_reset"); }
     float fov_deg = 60.0f;          // the reference's fixed FOV
     int max_depth = 1000;           // the reference's MAX_TRACING_DEPTH
     bool use_nee = true;            // SceneSetting::bUseNEE_
+    int guide = AR_GUIDE_NONE;      // SceneSetting::bUsePathGuiding_ (AR_GUIDE_VOXEL), or AR_GUIDE_MLP
     uint64_t seed = 0x9e3779b97f4a7c15ULL;
 
-    std::vector<float3> Render(int2 size, float3 cameraOrigin, float3 cameraDirection, int sampleNum = 1024)
+    // Triangle mesh: n_vertices x 3 floats, 3 indices per triangle, one material per triangle.
+    void SetMesh(const std::vector<float3>& vertices, const std::vector<uint32_t>& indices,
+                 const std::vector<Material>& triangleMaterials)
+    {
+        mesh_vertices_ = vertices;
+        mesh_indices_ = indices;
+        mesh_materials_ = triangleMaterials;
+        dirty_ = true;
+    }
+    // 6 floats per mesh triangle: (u, v) at each vertex
+    void SetMeshUV(const std::vector<float>& uv)
+    {
+        mesh_uv_ = uv;
+        dirty_ = true;
+    }
+    // RGB float textures, texels row-major (width x height x 3 each)
+    void SetTextures(const std::vector<std::vector<float>>& texels, const std::vector<int2>& sizes)
+    {
+        textures_ = texels;
+        texture_sizes_ = sizes;
+        dirty_ = true;
+    }
+    // Replaces the texel values of the built scene (device or host floats, all textures concatenated).
+    void UpdateTexels(const float* texels, int64_t nFloats, bool isDevice, void* stream = nullptr)
     {
         build();
+        check(ar_scene_update_texels(ctx_, texels, nFloats, isDevice ? 1 : 0, stream), "ar_scene_update_texels");
+    }
+    // Smooth-union SDF object: primitives of 8 floats (kind, centre xyz, size xyz, 0).
+    void SetSdfUnion(const std::vector<float>& prims, float smoothK, const Material& material)
+    {
+        sdf_prims_ = prims;
+        sdf_k_ = smoothK;
+        sdf_material_ = material;
+        dirty_ = true;
+    }
+    // Homogeneous medium in a box (takes effect on the next render); ClearMedium removes it.
+    void SetMedium(float3 boxLo, float3 boxHi, float sigmaT, float albedo, float g, float emission)
+    {
+        ar_medium m{};
+        Material::set3(m.box_lo, boxLo);
+        Material::set3(m.box_hi, boxHi);
+        m.sigma_t = sigmaT;
+        m.albedo = albedo;
+        m.g = g;
+        m.emission = emission;
+        check(ar_scene_set_medium(ctx_, &m), "ar_scene_set_medium");
+    }
+    void ClearMedium() { check(ar_scene_set_medium(ctx_, nullptr), "ar_scene_set_medium"); }
+
+    ar_render_params Params(int2 size, float3 cameraOrigin, float3 cameraDirection, int sampleNum) const
+    {
         ar_render_params p{};
         p.width = size.x;
         p.height = size.y;
         p.spp = sampleNum;
         p.max_depth = max_depth;
-        p.cam_origin[0] = cameraOrigin.x; p.cam_origin[1] = cameraOrigin.y; p.cam_origin[2] = cameraOrigin.z;
-        p.cam_dir[0] = cameraDirection.x; p.cam_dir[1] = cameraDirection.y; p.cam_dir[2] = cameraDirection.z;
+        Material::set3(p.cam_origin, cameraOrigin);
+        Material::set3(p.cam_dir, cameraDirection);
         p.fov_deg = fov_deg;
         p.use_nee = use_nee ? 1 : 0;
         p.seed = seed;
+        p.guide = guide;
+        return p;
+    }
+
+    // Per-pixel mean linear XYZ, FP64 (3 doubles per pixel, top row first).
+    std::vector<double> RenderXYZ(int2 size, float3 cameraOrigin, float3 cameraDirection, int sampleNum = 1024)
+    {
+        build();
+        const ar_render_params p = Params(size, cameraOrigin, cameraDirection, sampleNum);
         std::vector<double> xyz((size_t)size.x * size.y * 3);
         check(ar_render(ctx_, &p, xyz.data(), 0, nullptr, nullptr), "ar_render");
+        return xyz;
+    }
+
+    std::vector<float3> Render(int2 size, float3 cameraOrigin, float3 cameraDirection, int sampleNum = 1024)
+    {
+        const std::vector<double> xyz = RenderXYZ(size, cameraOrigin, cameraDirection, sampleNum);
         std::vector<float3> out((size_t)size.x * size.y);
         for (size_t i = 0; i < out.size(); ++i)
             out[i] = float3{(float)xyz[3 * i], (float)xyz[3 * i + 1], (float)xyz[3 * i + 2]};
         return out;
+    }
+
+    // d(loss)/d(texels) into gradTexelsDevice (float64, TexelCount()) from
+    // dLossDXyzDevice (float32, 3 per pixel), for the render with the same arguments.
+    void Adjoint(const float* dLossDXyzDevice, double* gradTexelsDevice, int2 size, float3 cameraOrigin,
+                 float3 cameraDirection, int sampleNum, void* stream = nullptr)
+    {
+        build();
+        const ar_render_params p = Params(size, cameraOrigin, cameraDirection, sampleNum);
+        check(ar_adjoint(ctx_, &p, dLossDXyzDevice, gradTexelsDevice, stream), "ar_adjoint");
+    }
+    // (d loss / d medium albedo, d loss / d medium emission)
+    std::pair<double, double> AdjointMedium(const float* dLossDXyzDevice, int2 size, float3 cameraOrigin,
+                                            float3 cameraDirection, int sampleNum, void* stream = nullptr)
+    {
+        build();
+        const ar_render_params p = Params(size, cameraOrigin, cameraDirection, sampleNum);
+        double g[2] = {0, 0};
+        check(ar_adjoint_medium(ctx_, &p, dLossDXyzDevice, g, stream), "ar_adjoint_medium");
+        return {g[0], g[1]};
+    }
+    int64_t TexelCount()
+    {
+        build();
+        int64_t n = 0;
+        check(ar_scene_texel_count(ctx_, &n), "ar_scene_texel_count");
+        return n;
+    }
+
+    // XYZ (host, 3 doubles per pixel) -> 8-bit RGBA on the GPU (core/tonemap.cuh)
+    std::vector<uint8_t> Tonemap(const std::vector<double>& xyz, int2 size, float exposure = 1.0f,
+                                 int tone = AR_TONE_ACES)
+    {
+        std::vector<uint8_t> rgba((size_t)size.x * size.y * 4);
+        check(ar_tonemap(ctx_, xyz.data(), 0, size.x, size.y, exposure, tone, rgba.data()), "ar_tonemap");
+        return rgba;
     }
 
     ar_ctx* handle() const { return ctx_; }
@@ -175,6 +295,12 @@ class SceneRenderer
     {
         if (!dirty_) return;
         std::vector<ar_material> mats;
+        auto mat_id = [&mats](const Material& m) {
+            for (size_t i = 0; i < mats.size(); ++i)
+                if (std::memcmp(&mats[i], &m.m, sizeof(ar_material)) == 0) return (int32_t)i;
+            mats.push_back(m.m);
+            return (int32_t)(mats.size() - 1);
+        };
         std::vector<ar_object> objs(objects_.size());
         for (size_t i = 0; i < objects_.size(); ++i)
         {
@@ -182,8 +308,7 @@ class SceneRenderer
             ar_object& o = objs[i];
             std::memset(&o, 0, sizeof(o));
             o.type = (int32_t)s.type_;
-            o.material = (int32_t)mats.size();
-            mats.push_back(s.material_.m);
+            o.material = mat_id(s.material_);
             Material::set3(o.center, s.center_);
             Material::set3(o.extent, s.extent_);
             Material::set3(o.rotation_deg, s.rotation_);
@@ -191,12 +316,46 @@ class SceneRenderer
             Material::set3(o.v1, s.v1_);
             Material::set3(o.v2, s.v2_);
         }
+        std::vector<int32_t> tri_mat(mesh_materials_.size());
+        for (size_t i = 0; i < tri_mat.size(); ++i) tri_mat[i] = mat_id(mesh_materials_[i]);
+        const int32_t sdf_mat = sdf_prims_.empty() ? -1 : mat_id(sdf_material_);
         check(ar_scene_set_materials(ctx_, mats.data(), (int)mats.size()), "ar_scene_set_materials");
         check(ar_scene_set_objects(ctx_, objs.data(), (int)objs.size()), "ar_scene_set_objects");
+        const int ntri = (int)(mesh_indices_.size() / 3);
+        check(ar_scene_set_mesh(ctx_, ntri ? &mesh_vertices_[0].x : nullptr, (int)mesh_vertices_.size(),
+                                ntri ? mesh_indices_.data() : nullptr, ntri, ntri ? tri_mat.data() : nullptr),
+              "ar_scene_set_mesh");
+        if (!mesh_uv_.empty()) check(ar_scene_set_mesh_uv(ctx_, mesh_uv_.data(), ntri), "ar_scene_set_mesh_uv");
+        if (!textures_.empty())
+        {
+            std::vector<float> all;
+            std::vector<int32_t> sizes;
+            for (size_t k = 0; k < textures_.size(); ++k)
+            {
+                all.insert(all.end(), textures_[k].begin(), textures_[k].end());
+                sizes.push_back(texture_sizes_[k].x);
+                sizes.push_back(texture_sizes_[k].y);
+            }
+            check(ar_scene_set_textures(ctx_, all.data(), sizes.data(), (int)textures_.size()),
+                  "ar_scene_set_textures");
+        }
+        check(ar_scene_set_sdf_union(ctx_, sdf_prims_.empty() ? nullptr : sdf_prims_.data(),
+                                     (int)(sdf_prims_.size() / 8), sdf_k_, sdf_mat),
+              "ar_scene_set_sdf_union");
         check(ar_scene_build(ctx_), "ar_scene_build");
         dirty_ = false;
     }
+    static_assert(sizeof(float3) == 3 * sizeof(float), "float3 is three packed floats");
     std::vector<SceneObject> objects_;
+    std::vector<float3> mesh_vertices_;
+    std::vector<uint32_t> mesh_indices_;
+    std::vector<Material> mesh_materials_;
+    std::vector<float> mesh_uv_;
+    std::vector<std::vector<float>> textures_;
+    std::vector<int2> texture_sizes_;
+    std::vector<float> sdf_prims_;
+    float sdf_k_ = 0.0f;
+    Material sdf_material_;
     ar_ctx* ctx_ = nullptr;
     bool dirty_ = true;
 };
@@ -211,7 +370,74 @@ class Camera
     }
     std::vector<float3> Render(int sampleNum = 1) { return renderer_.Render(res_, pos_, dir_, sampleNum); }
 
+    // Camera::RenderToFile (core/camera.cu:64-89): ".pfm" writes linear XYZ
+    // floats (bottom row first); otherwise the tonemapped 32-bit top-down BMP
+    // the reference writes, at `path` if it ends in ".bmp", else `path`.bmp.
+    // tone: AR_TONE_ACES (the reference's default), AR_TONE_GAMMA, AR_TONE_LINEAR.
+    std::vector<double> RenderToFile(const std::string& path, int sampleNum = 1024, int tone = AR_TONE_ACES,
+                                     float exposure = 1.0f)
+    {
+        std::vector<double> xyz = renderer_.RenderXYZ(res_, pos_, dir_, sampleNum);
+        auto ends = [&path](const char* ext) {
+            const size_t n = std::strlen(ext);
+            if (path.size() < n) return false;
+            for (size_t i = 0; i < n; ++i)
+                if (std::tolower((unsigned char)path[path.size() - n + i]) != ext[i]) return false;
+            return true;
+        };
+        if (ends(".pfm"))
+            write_pfm(path, xyz);
+        else
+            write_bmp(ends(".bmp") ? path : path + ".bmp", renderer_.Tonemap(xyz, res_, exposure, tone));
+        return xyz;
+    }
+
   private:
+    void write_pfm(const std::string& path, const std::vector<double>& xyz) const
+    {
+        FILE* f = std::fopen(path.c_str(), "wb");
+        if (!f) throw Error(AR_ERR_INVALID, "cannot open " + path);
+        std::fprintf(f, "PF\n%d %d\n-1.0\n", res_.x, res_.y);
+        std::vector<float> row((size_t)res_.x * 3);
+        for (int y = res_.y - 1; y >= 0; --y)
+        {
+            for (size_t i = 0; i < row.size(); ++i) row[i] = (float)xyz[(size_t)y * res_.x * 3 + i];
+            std::fwrite(row.data(), sizeof(float), row.size(), f);
+        }
+        std::fclose(f);
+    }
+    void write_bmp(const std::string& path, const std::vector<uint8_t>& rgba) const
+    {
+        FILE* f = std::fopen(path.c_str(), "wb");
+        if (!f) throw Error(AR_ERR_INVALID, "cannot open " + path);
+        const uint32_t px = (uint32_t)res_.x * (uint32_t)res_.y * 4u;
+        uint8_t h[54] = {};
+        auto put32 = [&h](int at, uint32_t v) {
+            for (int i = 0; i < 4; ++i) h[at + i] = (uint8_t)(v >> (8 * i));
+        };
+        h[0] = 'B';
+        h[1] = 'M';
+        put32(2, 54u + px);
+        put32(10, 54u);
+        put32(14, 40u);
+        put32(18, (uint32_t)res_.x);
+        put32(22, (uint32_t)(-res_.y));  // negative height: top row first
+        h[26] = 1;
+        h[28] = 32;
+        put32(34, px);
+        std::fwrite(h, 1, 54, f);
+        std::vector<uint8_t> bgra(rgba.size());
+        for (size_t i = 0; i < rgba.size(); i += 4)
+        {
+            bgra[i] = rgba[i + 2];
+            bgra[i + 1] = rgba[i + 1];
+            bgra[i + 2] = rgba[i];
+            bgra[i + 3] = rgba[i + 3];
+        }
+        std::fwrite(bgra.data(), 1, bgra.size(), f);
+        std::fclose(f);
+    }
+
     SceneRenderer& renderer_;
     std::string name_;
     int2 res_;
