@@ -9,6 +9,8 @@ from __future__ import annotations
 import ctypes as C
 from pathlib import Path
 
+import numpy as _np
+
 LIB_PATH = Path(__file__).resolve().parent / "libaperture_gb300.so"
 
 AR_OK = 0
@@ -54,7 +56,7 @@ class ArRenderParams(C.Structure):
                 ("cam_origin", F3), ("cam_dir", F3), ("fov_deg", C.c_float), ("use_nee", C.c_int32),
                 ("seed", C.c_uint64), ("first_frame", C.c_int32), ("wave_paths", C.c_int32),
                 ("profile", C.c_int32), ("guide", C.c_int32), ("guide_unit", C.c_float),
-                ("guide_train_steps", C.c_int32)]
+                ("guide_train_steps", C.c_int32), ("denoise_record", C.c_int32)]
 
 
 GUIDE_NONE = 0
@@ -62,6 +64,10 @@ GUIDE_VOXEL = 1
 GUIDE_MLP = 2
 SDF_SPHERE, SDF_BOX, SDF_TORUS = 0, 1, 2
 TONE_ACES, TONE_GAMMA, TONE_LINEAR = 0, 1, 2
+
+# denoiser records (ar_denoise_read / ar_denoise_write), 40 bytes per pixel each
+DENOISE_GBUF_DTYPE = _np.dtype([("h", "<u2", 14), ("depth", "<f4"), ("valid", "<u4"), ("frames", "<u4")])
+DENOISE_STAT_DTYPE = _np.dtype([("num", "<u4"), ("mean", "<f4", 3), ("m2n", "<f4", 3), ("m3n", "<f4", 3)])
 
 
 class ArRenderProfile(C.Structure):
@@ -84,7 +90,7 @@ EXPORTED = [
     "ar_host_sample_lambda", "ar_host_trace_closest", "ar_host_guide_eval", "ar_abi_version",
     "ar_scene_set_textures", "ar_scene_set_mesh_uv", "ar_scene_update_texels", "ar_scene_texel_count", "ar_adjoint",
     "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats", "ar_scene_set_sdf_union", "ar_scene_set_medium",
-    "ar_adjoint_medium", "ar_tonemap",
+    "ar_adjoint_medium", "ar_tonemap", "ar_denoise", "ar_denoise_read", "ar_denoise_write",
 ]
 
 _lib = None
@@ -144,6 +150,9 @@ def load() -> C.CDLL:
         "ar_scene_set_medium": (C.c_int, [vp, P(ArMedium)]),
         "ar_adjoint_medium": (C.c_int, [vp, P(ArRenderParams), vp, vp, vp]),
         "ar_tonemap": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, vp]),
+        "ar_denoise": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, vp]),
+        "ar_denoise_read": (C.c_int, [vp, P(C.c_int32), P(C.c_int32), vp, vp]),
+        "ar_denoise_write": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

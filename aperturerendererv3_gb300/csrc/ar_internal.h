@@ -10,6 +10,7 @@
 #include "ar_bvh_build.h"
 #include "ar_guide.h"
 #include "ar_mlp.h"
+#include "ar_denoise.h"
 #include "ar_shade.h"
 #include "ar_traverse.cuh"
 
@@ -187,6 +188,7 @@ struct RenderLaunch
     float* grad;  // replay pass: float32 texel gradients
     int mlp_ready;  // guide 2: sample from the network instead of the voxel probes
     double* grad_medium;  // replay pass of ar_adjoint_medium: d loss / d (albedo, emission)
+    int denoise;  // record the denoiser's G-buffer and sample moments
 };
 
 struct Ctx
@@ -287,6 +289,15 @@ struct Ctx
     int mlp_path_cap = 0;
     int* d_mlp_list = nullptr;    // compacted queue of the paths the network is queried for
     MlpBox mlp_box{};
+    // denoiser records (denoise.cu)
+    DnGBuf* d_dn_gb = nullptr;    // per pixel
+    DnStat* d_dn_st = nullptr;    // per pixel
+    float4* d_dn_rec = nullptr;   // per path in flight: first-hit record (2 float4)
+    int dn_w = 0, dn_h = 0;       // image the records belong to (0: none)
+    int dn_rec_cap = 0;
+    float* d_dn_img = nullptr;    // filter input / output staging (float XYZ)
+    double* d_dn_io = nullptr;    // host-image staging (double XYZ)
+    long long dn_img_cap = 0;
 };
 
 // MLP guide (mlp.cu)
@@ -347,4 +358,9 @@ cudaError_t launch_accumulate(Ctx& c, const RenderLaunch& rl, long long first_pa
 cudaError_t launch_adjoint_seed(Ctx& c, const RenderLaunch& rl, int n_paths, const float* dl_dxyz,
                                 long long* launches);
 cudaError_t launch_grad_fold(Ctx& c, double* grad64, long long n, long long* launches);
+// denoiser (denoise.cu): fold one wave's first-hit records and sample XYZ into
+// the per-pixel records, in sample order
+cudaError_t launch_denoise_record(Ctx& c, const RenderLaunch& rl, long long first_path, int n_paths, long long* launches);
+cudaError_t ensure_denoise(Ctx& c, int width, int height, int first_frame);
+void free_denoise(Ctx& c);
 } // namespace ar

@@ -565,7 +565,7 @@ ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch&
 
 extern "C" {
 
-int ar_abi_version(void) { return 2; }
+int ar_abi_version(void) { return 3; }
 
 ar_status ar_create(ar_ctx** out, int device)
 {
@@ -613,6 +613,7 @@ ar_status ar_destroy(ar_ctx* ctx)
     free_scene(c);
     free_guide(c);
     free_mlp(c);
+    free_denoise(c);
     free_waves(c);
     free_dev(c.d_lut_rgb);
     free_dev(c.d_lut_lambda);
@@ -1045,6 +1046,10 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
         st = ensure_mlp(ctx);
         if (st != AR_OK) return st;
     }
+    if (prm->denoise_record != 0 && prm->denoise_record != 1)
+        return fail(ctx, AR_ERR_INVALID, "render: denoise_record must be 0 or 1");
+    rl.denoise = prm->denoise_record;
+    if (rl.denoise) AR_CUDA(ctx, ensure_denoise(c, rl.width, rl.height, rl.first_frame));
     c.mlp_steps_per_frame = prm->guide_train_steps > 0 ? prm->guide_train_steps : AR_MLP_STEPS_PER_FRAME;
     rl.mlp_ready = (rl.guide == 2 && c.mlp_step >= AR_MLP_WARMUP_STEPS) ? 1 : 0;
     if (c.accum_pixels < (size_t)npix)
@@ -1070,6 +1075,7 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
         const int n = (int)n_ll;
         e = launch_render_wave(c, rl, first, n, d_samples, &launches);
         if (e == cudaSuccess) e = launch_accumulate(c, rl, first, n, c.d_accum, &launches);
+        if (e == cudaSuccess && rl.denoise) e = launch_denoise_record(c, rl, first, n, &launches);
         if (e == cudaSuccess && per_sample_xyz)
             e = cudaMemcpyAsync(per_sample_xyz + 3 * first, d_samples, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, c.stream);
         first += n;

@@ -100,9 +100,9 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
                        std::to_string(kMaxPaths) + " paths (" + std::to_string(AR_NOALLOC_SCRATCH_BYTES) + " bytes)";
         return AR_ERR_INVALID;
     }
-    if (prm->profile || prm->guide)
+    if (prm->profile || prm->guide || prm->denoise_record)
     {
-        c.last_error = "render_noalloc: profiling and path guiding need allocations; use ar_render";
+        c.last_error = "render_noalloc: profiling, path guiding and denoiser records need allocations; use ar_render";
         return AR_ERR_INVALID;
     }
     cudaError_t e = cudaSetDevice(c.device);

@@ -306,6 +306,7 @@ struct ShadeParams
     float* grad;  // replay adjoint: float32 texel gradients (3 per texel), or null
     int mlp_ready;  // MLP guide: the network has trained long enough to replace the voxel probes
     double* grad_medium;  // replay adjoint: d loss / d (medium albedo, medium emission), or null
+    float4* gbuf;         // denoiser: first-hit record per path (2 float4), or null
 };
 
 // CollectRadiance (core/render/render.cuh:353-432) on the path's collection
@@ -493,6 +494,19 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                 S.pdf = 1.0f;
                 S.emissive = sky_lighting(rayD);
                 S.media.inside = false;
+            }
+            // denoiser G-buffer of the camera ray's hit (RecordScreenGBuffer at
+            // depth 0, core/render/render.cuh:640-643): albedo (texel when
+            // textured), material index (-1: no surface), normal, distance
+            if constexpr (!ADJ)
+            {
+                if (prm.gbuf && depth == 0)
+                {
+                    const int mid = h.hit ? sc.prim_material[h.obj] : -1;
+                    const V3 alb = h.hit ? mat.albedo : v3(0.0f, 0.0f, 0.0f);
+                    prm.gbuf[2 * (size_t)p] = make_float4(alb.x, alb.y, alb.z, __int_as_float(mid));
+                    prm.gbuf[2 * (size_t)p + 1] = make_float4(h.nrm.x, h.nrm.y, h.nrm.z, h.dist);
+                }
             }
             {
                 const float offsetEPS = eps * fmaxf(1.0f, length(h.pos));
@@ -1057,6 +1071,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     prm.grad = rl.grad;
     prm.grad_medium = rl.grad_medium;
     prm.mlp_ready = rl.mlp_ready;
+    prm.gbuf = rl.denoise ? c.d_dn_rec : nullptr;
     MlpDev net;
     net.wbf = c.d_mlp_wbf;
     net.w32 = c.d_mlp_w32;
@@ -1140,6 +1155,7 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     prm.grad = nullptr;
     prm.grad_medium = nullptr;
     prm.mlp_ready = 0;
+    prm.gbuf = nullptr;
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;

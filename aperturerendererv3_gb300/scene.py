@@ -283,7 +283,7 @@ class SceneRenderer:
 
     def params(self, size, cameraOrigin, cameraDirection, sampleNum, fov=60.0, max_depth=1000, use_nee=True,
                seed=GLOBAL_SEED, first_frame=0, wave_paths=0, profile=False, guide=0,
-               guide_unit=0.0, guide_train_steps=0) -> ArRenderParams:
+               guide_unit=0.0, guide_train_steps=0, denoise_record=False) -> ArRenderParams:
         p = ArRenderParams()
         p.width, p.height = int(size[0]), int(size[1])
         p.spp = int(sampleNum)
@@ -299,12 +299,13 @@ class SceneRenderer:
         p.guide = int(guide)
         p.guide_unit = float(guide_unit)
         p.guide_train_steps = int(guide_train_steps)
+        p.denoise_record = 1 if denoise_record else 0
         return p
 
     def Render(self, size, cameraOrigin, cameraDirection, sampleNum: int = 1024, *, fov: float = 60.0,
                max_depth: int = 1000, use_nee: bool = True, seed: int = GLOBAL_SEED, first_frame: int = 0,
                per_sample: bool = False, wave_paths: int = 0, profile: bool = False, guide: int = 0,
-               guide_unit: float = 0.0, guide_train_steps: int = 0):
+               guide_unit: float = 0.0, guide_train_steps: int = 0, denoise: bool = False):
         """Mean linear XYZ per pixel, shape (height, width, 3), float64.
 
         With per_sample=True also returns every sample's XYZ, shape
@@ -312,17 +313,66 @@ class SceneRenderer:
         path guide: frames render one sample per pixel each and the probes learn
         after every frame (and persist across calls until MarkNeedResetGuiding);
         guide=2 adds the tensor-core MLP guide, trained online on the same
-        records and sampled instead of the probes once it has trained."""
+        records and sampled instead of the probes once it has trained.
+        denoise=True (SceneSetting::bDenoise_) records the denoiser's G-buffer
+        and sample moments during the render (starting over at first_frame 0)
+        and returns the filtered image instead of the raw mean."""
         self._build()
         p = self.params(size, cameraOrigin, cameraDirection, sampleNum, fov, max_depth, use_nee, seed, first_frame,
-                        wave_paths, profile, guide, guide_unit, guide_train_steps)
+                        wave_paths, profile, guide, guide_unit, guide_train_steps, denoise)
         w, h = p.width, p.height
         out = np.zeros((h, w, 3), np.float64)
         ps = np.zeros((p.spp, h, w, 3), np.float32) if per_sample else None
         code = self._lib.ar_render(self._ctx, C.byref(p), out.ctypes.data, 0,
                                    ps.ctypes.data if ps is not None else None, None)
         check(self._ctx, code)
+        if denoise:
+            out = self.denoise(out)
         return (out, ps) if per_sample else out
+
+    # ---- denoiser (core/denoise/*) ----------------------------------------
+    def denoise(self, xyz):
+        """Bilateral-filters an image of the recorded size with the recorded
+        G-buffer and sample moments.  xyz: (height, width, 3) float64 numpy
+        array (returns a new array) or CUDA float64 tensor (returns a new tensor)."""
+        if hasattr(xyz, "data_ptr"):
+            import torch
+            x = xyz.detach().to(torch.float64).contiguous()
+            out = torch.empty_like(x)
+            check(self._ctx, self._lib.ar_denoise(self._ctx, x.data_ptr(), 1, out.data_ptr(), 1,
+                                                  _torch_stream(x.device)))
+            return out
+        a = np.ascontiguousarray(xyz, np.float64)
+        w, h = self.denoise_size()
+        if a.shape != (h, w, 3):
+            raise ValueError(f"image must be ({h}, {w}, 3) to match the recorded buffers")
+        out = np.empty_like(a)
+        check(self._ctx, self._lib.ar_denoise(self._ctx, a.ctypes.data, 0, out.ctypes.data, 0, None))
+        return out
+
+    def denoise_size(self) -> tuple[int, int]:
+        """(width, height) of the recorded denoiser buffers, (0, 0) when none."""
+        w, h = C.c_int32(), C.c_int32()
+        check(self._ctx, self._lib.ar_denoise_read(self._ctx, C.byref(w), C.byref(h), None, None))
+        return w.value, h.value
+
+    def denoise_records(self):
+        """(gbuffer, moments): structured arrays of shape (height, width) with
+        the layouts DENOISE_GBUF_DTYPE / DENOISE_STAT_DTYPE."""
+        w, h = self.denoise_size()
+        g = np.zeros((h, w), _lib.DENOISE_GBUF_DTYPE)
+        m = np.zeros((h, w), _lib.DENOISE_STAT_DTYPE)
+        check(self._ctx, self._lib.ar_denoise_read(self._ctx, None, None, g.ctypes.data, m.ctypes.data))
+        return g, m
+
+    def set_denoise_records(self, gbuffer, moments) -> None:
+        """Replaces the recorded buffers (arrays as denoise_records returns them)."""
+        g = np.ascontiguousarray(gbuffer, _lib.DENOISE_GBUF_DTYPE)
+        m = np.ascontiguousarray(moments, _lib.DENOISE_STAT_DTYPE)
+        if g.shape != m.shape or g.ndim != 2:
+            raise ValueError("gbuffer and moments must be (height, width) arrays of the same shape")
+        h, w = g.shape
+        check(self._ctx, self._lib.ar_denoise_write(self._ctx, w, h, g.ctypes.data, m.ctypes.data))
 
     # ---- device-side rendering and the replay adjoint (torch tensors) -----
     def texel_count(self) -> int:

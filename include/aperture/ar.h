@@ -97,6 +97,7 @@ typedef struct ar_render_params
     int32_t guide;           /* AR_GUIDE_NONE, AR_GUIDE_VOXEL (SceneSetting::bUsePathGuiding_) or AR_GUIDE_MLP */
     float guide_unit;        /* voxel size of the guide (0 = 0.05, PATH_GUIDING_RESOLUTION_UNIT) */
     int32_t guide_train_steps; /* AR_GUIDE_MLP: Adam steps after each frame (0 = 8) */
+    int32_t denoise_record;  /* 1: record the denoiser's per-pixel G-buffer and sample moments (ar_denoise) */
 } ar_render_params;
 
 /* Path guiding modes.  With AR_GUIDE_VOXEL, ar_render renders one frame (one
@@ -244,6 +245,33 @@ ar_status ar_adjoint_medium(ar_ctx* ctx, const ar_render_params* params, const f
 #define AR_TONE_LINEAR 2    /* linear sRGB */
 ar_status ar_tonemap(ar_ctx* ctx, const double* xyz, int xyz_is_device, int width, int height, float exposure, int tone,
                      uint8_t* rgba);
+
+/* Denoiser (SceneRenderer::Render with SceneSetting::bDenoise_,
+ * core/scene.cu:324-348; core/denoise/denoise.cuh).  An ar_render with
+ * params->denoise_record = 1 records, for every sample in sample order, the
+ * camera ray's first hit into per-pixel running means (albedo, normal,
+ * metallic, roughness as halves; hit distance; shading-model histogram) and
+ * the moments of BoxCox(sample XYZ); the records start over when
+ * params->first_frame is 0 or the image size changes, and accumulate across
+ * calls otherwise.  ar_denoise then filters an image of that size (3 doubles
+ * per pixel, as ar_render writes it, read as float) with the reference's
+ * bilateral filter: radius 7, weights from the G-buffer differences, a
+ * Gaussian in pixel distance, and a per-pair Welch t-test (0.5 % two-sided) on
+ * the sample moments; filtering happens on log(1 + XYZ).  Output: 3 doubles
+ * per pixel.  Host or device buffers; ordered on `stream`. */
+ar_status ar_denoise(ar_ctx* ctx, const double* xyz_in, int in_is_device, double* xyz_out, int out_is_device,
+                     void* stream);
+/* The recorded buffers (host copies): 40 bytes per pixel each.
+ * gbuffer: uint16 halves[14] (albedo xyz, normal xyz, metallic, roughness,
+ * shading-model histogram [diffuse, light, glass, GGX, no hit], pad), float
+ * distance, uint32 samples that hit, uint32 samples.  moments: uint32 count,
+ * float mean[3], M2/n[3], M3/n[3] of BoxCox(XYZ) = 2 (sqrt(XYZ) - 1).
+ * width / height (optional) receive the image size (0 when nothing is
+ * recorded); pass NULL buffers to query it. */
+ar_status ar_denoise_read(ar_ctx* ctx, int32_t* width, int32_t* height, void* gbuffer, void* moments);
+/* Replaces the recorded buffers (same layout), e.g. to filter with records
+ * made elsewhere. */
+ar_status ar_denoise_write(ar_ctx* ctx, int32_t width, int32_t height, const void* gbuffer, const void* moments);
 
 /* Device time (ms) of the last ar_render and the number of kernels it launched. */
 ar_status ar_last_render_stats(ar_ctx* ctx, float* device_ms, int64_t* kernel_launches);

@@ -175,6 +175,39 @@ def patch_tree() -> None:
          "const int currentNodeIndex = stack[--sp]; REF_NODE_VISIT_HOOK;", count=1)
     shutil.copy(HERE / "ref_glue.cuh", CORE / "render" / "ref_glue.cuh")
 
+    # (8) denoiser: the device code subtracts two halves in half precision
+    # (core/denoise/denoise.cuh:213-235, the __CUDA_ARCH__ branches); the host
+    # branches subtract in float.  Keep the device arithmetic on the host too.
+    den = CORE / "denoise" / "denoise.cuh"
+    text = den.read_text()
+    text, n = re.subn(r"#ifdef __CUDA_ARCH__\n([^\n]*static_cast<float>\(a\.[^\n]* - b\.[^\n]*\n)#else\n[^\n]*\n#endif\n",
+                      r"\1", text)
+    if n != 3:
+        raise RuntimeError(f"denoise.cuh: expected 3 half-subtraction branches, found {n}")
+    den.write_text(text)
+    # the t-quantile table compiles into the driver's single translation unit:
+    # the (never executed) device copy becomes a local zero table and its
+    # separate definition goes; the host table T005QuantilesHost is unchanged
+    _sub(CORE / "denoise" / "t_quantile.cuh", r"extern __device__ __constant__ float T005QuantilesDev\[T_QUANTILE_LUT_SIZE\];",
+         "static __device__ __constant__ float T005QuantilesDev[T_QUANTILE_LUT_SIZE] = {};")
+    _sub(CORE / "denoise" / "t_quantile.cu", r"__device__ __constant__ float T005QuantilesDev\[T_QUANTILE_LUT_SIZE\] = T005_LUT_INIT;",
+         "")
+    (CORE / PATCH_STAMP).write_text(PATCH_VERSION)
+
+
+# bump when patch_tree() changes, so an existing patched copy is redone
+PATCH_VERSION = "3"
+PATCH_STAMP = ".ar_patch_version"
+
+
+def needs_prepare() -> bool:
+    """True when the reference checkout is present and the patched copy is
+    missing or was made by an older patch_tree()."""
+    if not (REF_ROOT / "core").is_dir():
+        return False
+    stamp = CORE / PATCH_STAMP
+    return not stamp.exists() or stamp.read_text().strip() != PATCH_VERSION
+
 
 def prepare() -> Path:
     copy_tree()
@@ -194,7 +227,8 @@ def build_ref(jobs_hint: int = 0) -> Path:
     if not CORE.is_dir():
         prepare()
     exe = OUT / "ref_cpu"
-    srcs = [HERE / "ref_driver.cu", HERE / "ref_glue.cuh", CSRC / "ar_detmath.h", CSRC / "ar_rng.h", CSRC / "ar_geom.h"]
+    srcs = [HERE / "ref_driver.cu", HERE / "ref_glue.cuh", CSRC / "ar_detmath.h", CSRC / "ar_rng.h", CSRC / "ar_geom.h",
+            CORE / PATCH_STAMP]
     if exe.exists() and all(exe.stat().st_mtime > s.stat().st_mtime for s in srcs if s.exists()):
         return exe
     cmd = [nvcc(), "-std=c++17", "-O3", "-DNDEBUG", "-DLINUX=1",

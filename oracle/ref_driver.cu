@@ -13,7 +13,12 @@
 //           or brute force
 //   render  CalculateRadiance<true, NEE, false> per pixel sample
 //           (core/render/render.cuh:460-999) behind the camera model of
-//           RenderCamera (core/scene.cu:135-189), OpenMP over pixels.
+//           RenderCamera (core/scene.cu:135-189), OpenMP over pixels;
+//           optionally with the denoiser's per-pixel records
+//           (denoise::RecordScreenGBuffer / RecordScreenStatisticBuffer)
+//   denoise the loop of denoise::Bilateral16x16<7> (core/denoise/denoise.cuh:
+//           360-443) per output pixel, calling the reference's weight,
+//           t-test and sample transforms
 // The scene / light-table setup mirrors SceneRenderer::UpdateSceneToDeviceIfDirty
 // (core/scene.cu:656-732) on host memory.
 #include <cfloat>
@@ -30,6 +35,9 @@
 #include "scene.hpp"
 #include "render/render.cuh"
 #include "spectrum/spectrum_lut.cuh"
+#include "denoise/denoise.cuh"
+// the t-quantile table the denoiser's t-test reads
+#include "denoise/t_quantile.cu"
 // explicit SDF instantiations the intersection dispatch links against
 #include "object/sdf/sdf_base.cu"
 
@@ -227,10 +235,76 @@ struct RenderParams
     int32_t use_nee;
     uint64_t seed;
     int32_t first_frame, per_sample_frames;
+    int32_t denoise;  // 1: record the denoiser's G-buffer and sample moments and append them
+};
+// Plain per-pixel layouts of the denoiser records (40 bytes each), shared with
+// the GPU library's ar_denoise_read / ar_denoise_write.
+struct PlainGBuf
+{
+    uint16_t h[14];  // albedo xyz, normal xyz, metallic, roughness, shading model[5], pad
+    float depth;
+    uint32_t valid, frames;
+};
+struct PlainStat
+{
+    uint32_t num;
+    float mean[3], m2n[3], m3n[3];
 };
 #pragma pack(pop)
 
 static float3 f3(const float* v) { return float3{v[0], v[1], v[2]}; }
+
+static uint16_t half_bits(const half& h)
+{
+    uint16_t u;
+    memcpy(&u, &h, 2);
+    return u;
+}
+static half bits_half(uint16_t u)
+{
+    half h;
+    memcpy(&h, &u, 2);
+    return h;
+}
+
+static void to_plain(const denoise::ScreenGBuffer& g, const denoise::ScreenStatisticsBuffer& s, PlainGBuf* pg,
+                     PlainStat* ps)
+{
+    const half hs[8] = {g.albedoX_, g.albedoY_, g.albedoZ_, g.normalX_, g.normalY_, g.normalZ_, g.metallic_, g.roughness_};
+    for (int i = 0; i < 8; ++i) pg->h[i] = half_bits(hs[i]);
+    for (int i = 0; i < 5; ++i) pg->h[8 + i] = half_bits(g.shadingModel_[i]);
+    pg->h[13] = 0;
+    pg->depth = g.depth_;
+    pg->valid = (uint32_t)g.validFrameIndex_;
+    pg->frames = (uint32_t)g.frameIndex_;
+    ps->num = s.num_;
+    const float3 v[3] = {s.mean_, s.M2DivNum_, s.M3DivNum_};
+    float* dst[3] = {ps->mean, ps->m2n, ps->m3n};
+    for (int k = 0; k < 3; ++k)
+    {
+        dst[k][0] = v[k].x;
+        dst[k][1] = v[k].y;
+        dst[k][2] = v[k].z;
+    }
+}
+
+static void from_plain(const PlainGBuf& pg, const PlainStat& ps, denoise::ScreenGBuffer* g,
+                       denoise::ScreenStatisticsBuffer* s)
+{
+    memset(static_cast<void*>(g), 0, sizeof(*g));
+    memset(static_cast<void*>(s), 0, sizeof(*s));
+    half* hs[8] = {&g->albedoX_, &g->albedoY_, &g->albedoZ_, &g->normalX_, &g->normalY_, &g->normalZ_, &g->metallic_,
+                   &g->roughness_};
+    for (int i = 0; i < 8; ++i) *hs[i] = bits_half(pg.h[i]);
+    for (int i = 0; i < 5; ++i) g->shadingModel_[i] = bits_half(pg.h[8 + i]);
+    g->depth_ = pg.depth;
+    g->validFrameIndex_ = pg.valid;
+    g->frameIndex_ = pg.frames;
+    s->num_ = ps.num;
+    s->mean_ = float3{ps.mean[0], ps.mean[1], ps.mean[2]};
+    s->M2DivNum_ = float3{ps.m2n[0], ps.m2n[1], ps.m2n[2]};
+    s->M3DivNum_ = float3{ps.m3n[0], ps.m3n[1], ps.m3n[2]};
+}
 
 static Material make_material(const FileObject& o)
 {
@@ -392,6 +466,14 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
     const float3 right = normalize(cross(camD, float3{0.0, 1.0, 0.0}));
     const float3 up = normalize(cross(camD, right));
 
+    // the reference zeroes its device-side records (ResetScreenGBuffer, core/GUI.hpp:202-230)
+    std::vector<denoise::ScreenGBuffer> gbuf(prm.denoise ? npix : 0);
+    std::vector<denoise::ScreenStatisticsBuffer> stats(prm.denoise ? npix : 0);
+    if (prm.denoise)
+    {
+        memset(static_cast<void*>(gbuf.data()), 0, npix * sizeof(denoise::ScreenGBuffer));
+        memset(static_cast<void*>(stats.data()), 0, npix * sizeof(denoise::ScreenStatisticsBuffer));
+    }
     auto t0 = std::chrono::steady_clock::now();
     for (int s = 0; s < prm.spp; ++s)
     {
@@ -410,8 +492,10 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
             const float sy = ndc.y * tanHalfY;
             const float3 rayDirection = normalize(camD + right * sx + up * sy);
             float4 r;
-            if (prm.use_nee) r = CalculateRadiance<true, true, false>(&seed, camO, rayDirection);
-            else r = CalculateRadiance<true, false, false>(&seed, camO, rayDirection);
+            denoise::ScreenGBuffer* gbp = prm.denoise ? &gbuf[p] : nullptr;
+            denoise::ScreenStatisticsBuffer* stp = prm.denoise ? &stats[p] : nullptr;
+            if (prm.use_nee) r = CalculateRadiance<true, true, false>(&seed, camO, rayDirection, nullptr, gbp, stp);
+            else r = CalculateRadiance<true, false, false>(&seed, camO, rayDirection, nullptr, gbp, stp);
             float3 result = make_f3(r);
             result = max(float3{0}, result);
             sums[3 * p + 0] += (double)result.x;
@@ -429,10 +513,77 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
     auto t1 = std::chrono::steady_clock::now();
     write_file(out_path, sums.data(), sums.size() * 8);
     if (prm.per_sample_frames) write_file(out_path, per_sample.data(), per_sample.size() * 4, true);
+    if (prm.denoise)
+    {
+        std::vector<PlainGBuf> pg(npix);
+        std::vector<PlainStat> ps(npix);
+        for (size_t i = 0; i < npix; ++i) to_plain(gbuf[i], stats[i], &pg[i], &ps[i]);
+        write_file(out_path, pg.data(), pg.size() * sizeof(PlainGBuf), true);
+        write_file(out_path, ps.data(), ps.size() * sizeof(PlainStat), true);
+    }
     free(lut);
     const double secs = std::chrono::duration<double>(t1 - t0).count();
     printf("{\"render_s\": %.6f, \"samples\": %llu, \"msamples_per_s\": %.6f, \"threads\": %d, \"bvh_nodes\": %zu}\n",
            secs, (unsigned long long)npix * prm.spp, (double)npix * prm.spp / secs / 1e6, omp_get_max_threads(), bvh.nodes_.size());
+    return 0;
+}
+
+// ---------------------------------------------------------------- denoise
+// in: int32 width, height; float XYZ image (3 per pixel); PlainGBuf and
+// PlainStat per pixel.  out: float XYZ (3 per pixel).  Per output pixel the
+// loop of Bilateral16x16<7>: neighbours at clamped image coordinates, centre
+// term with weight 1e-6, weights ComputeSVGFWeight x spatial Gaussian x
+// ComputeTStatisticFinal, SeparateSample before and CompositeSample after.
+static int cmd_denoise(const char* in_path, const char* out_path)
+{
+    std::vector<char> buf = read_file(in_path);
+    if (buf.size() < 8) die("bad denoise input");
+    const int W = *reinterpret_cast<const int32_t*>(buf.data());
+    const int H = *reinterpret_cast<const int32_t*>(buf.data() + 4);
+    const size_t npix = (size_t)W * H;
+    if (W <= 0 || H <= 0 || buf.size() != 8 + npix * (12 + sizeof(PlainGBuf) + sizeof(PlainStat))) die("bad denoise input size");
+    const float* img = reinterpret_cast<const float*>(buf.data() + 8);
+    const PlainGBuf* pg = reinterpret_cast<const PlainGBuf*>(buf.data() + 8 + npix * 12);
+    const PlainStat* pst = reinterpret_cast<const PlainStat*>(buf.data() + 8 + npix * (12 + sizeof(PlainGBuf)));
+    std::vector<denoise::ScreenGBuffer> g(npix);
+    std::vector<denoise::ScreenStatisticsBuffer> st(npix);
+    for (size_t i = 0; i < npix; ++i) from_plain(pg[i], pst[i], &g[i], &st[i]);
+    std::vector<float> out(npix * 3);
+    constexpr int R = 7;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int oy = 0; oy < H; ++oy)
+    {
+        for (int ox = 0; ox < W; ++ox)
+        {
+            const size_t c = (size_t)oy * W + ox;
+            const float3 cc{img[3 * c], img[3 * c + 1], img[3 * c + 2]};
+            float3 acc = make_float3(0, 0, 0);
+            float accW = 0.0f;
+            constexpr float CENTER_PIXEL_EPS = 1.0e-6f;
+            acc = acc + denoise::SeparateSample(g[c], cc) * CENTER_PIXEL_EPS;
+            accW = accW + CENTER_PIXEL_EPS;
+            for (int j = -R; j <= R; ++j)
+            {
+                const int ny = clampi(oy + j, 0, H - 1);
+                for (int i = -R; i <= R; ++i)
+                {
+                    const int nx = clampi(ox + i, 0, W - 1);
+                    const size_t q = (size_t)ny * W + nx;
+                    const float3 qc{img[3 * q], img[3 * q + 1], img[3 * q + 2]};
+                    const float weight = denoise::ComputeSVGFWeight(g[c], g[q]) *
+                                         arm_expf(-(i * i + j * j) * denoise::FilterParams::inv2Sigma2Spatial_) *
+                                         denoise::ComputeTStatisticFinal(st[c], st[q]);
+                    acc = acc + denoise::SeparateSample(g[q], qc) * weight;
+                    accW = accW + weight;
+                }
+            }
+            const float3 r = denoise::CompositeSample(g[c], acc / accW);
+            out[3 * c] = r.x;
+            out[3 * c + 1] = r.y;
+            out[3 * c + 2] = r.z;
+        }
+    }
+    write_file(out_path, out.data(), out.size() * 4);
     return 0;
 }
 
@@ -504,6 +655,7 @@ int main(int argc, char** argv)
     if ((cmd == "trace" || cmd == "brute") && argc == 5) return cmd_trace(argv[2], argv[3], argv[4], cmd == "brute");
     if (cmd == "render" && argc == 5) return cmd_render(argv[2], argv[3], argv[4]);
     if (cmd == "guide" && argc == 4) return cmd_guide(argv[2], argv[3]);
+    if (cmd == "denoise" && argc == 4) return cmd_denoise(argv[2], argv[3]);
     die("bad arguments");
     return 2;
 }

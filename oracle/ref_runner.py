@@ -22,7 +22,10 @@ OBJ_DTYPE = np.dtype([("type", "<i4"), ("shading", "<i4"), ("center", "<f4", 3),
                       ("specular", "<f4"), ("ior", "<f4"), ("sigma_a", "<f4"), ("abbe", "<f4"), ("tilt", "<f4")])
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("max_depth", "<i4"),
                          ("cam_origin", "<f4", 3), ("cam_dir", "<f4", 3), ("fov", "<f4"), ("use_nee", "<i4"),
-                         ("seed", "<u8"), ("first_frame", "<i4"), ("per_sample", "<i4")])
+                         ("seed", "<u8"), ("first_frame", "<i4"), ("per_sample", "<i4"), ("denoise", "<i4")])
+# denoiser records in the driver's plain layout (the GPU library's ar_denoise_read layout)
+GBUF_DTYPE = np.dtype([("h", "<u2", 14), ("depth", "<f4"), ("valid", "<u4"), ("frames", "<u4")])
+STAT_DTYPE = np.dtype([("num", "<u4"), ("mean", "<f4", 3), ("m2n", "<f4", 3), ("m3n", "<f4", 3)])
 
 
 def available() -> bool:
@@ -68,12 +71,15 @@ def scene_bytes(objects, mesh=None) -> bytes:
 
 
 def render(objects, size, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
-           seed=0x9E3779B97F4A7C15, first_frame=0, per_sample_frames=0, mesh=None, threads=None):
-    """Returns (mean XYZ (H, W, 3) float64, per-sample XYZ or None, stats dict)."""
+           seed=0x9E3779B97F4A7C15, first_frame=0, per_sample_frames=0, mesh=None, threads=None, denoise=False):
+    """Returns (mean XYZ (H, W, 3) float64, per-sample XYZ or None, stats dict); with
+    denoise=True the stats dict also holds the denoiser records under "gbuffer" and
+    "moments" ((H, W) arrays of GBUF_DTYPE / STAT_DTYPE)."""
     exe = ensure_built()
     w, h = int(size[0]), int(size[1])
     prm = np.zeros(1, PARAMS_DTYPE)
-    prm[0] = (w, h, spp, max_depth, origin, direction, fov, 1 if use_nee else 0, seed, first_frame, per_sample_frames)
+    prm[0] = (w, h, spp, max_depth, origin, direction, fov, 1 if use_nee else 0, seed, first_frame, per_sample_frames,
+              1 if denoise else 0)
     with tempfile.TemporaryDirectory() as td:
         td = Path(td)
         (td / "scene.bin").write_bytes(scene_bytes(objects, mesh))
@@ -90,10 +96,37 @@ def render(objects, size, origin, direction, spp, *, fov=60.0, max_depth=1000, u
         raw = (td / "out.bin").read_bytes()
     npix = w * h
     sums = np.frombuffer(raw[: npix * 24], np.float64).reshape(h, w, 3)
+    at = npix * 24
     per = None
     if per_sample_frames:
-        per = np.frombuffer(raw[npix * 24:], np.float32).reshape(per_sample_frames, h, w, 3)
+        per = np.frombuffer(raw[at: at + npix * 12 * per_sample_frames], np.float32).reshape(per_sample_frames, h, w, 3)
+        at += npix * 12 * per_sample_frames
+    if denoise:
+        stats["gbuffer"] = np.frombuffer(raw[at: at + npix * GBUF_DTYPE.itemsize], GBUF_DTYPE).reshape(h, w).copy()
+        at += npix * GBUF_DTYPE.itemsize
+        stats["moments"] = np.frombuffer(raw[at: at + npix * STAT_DTYPE.itemsize], STAT_DTYPE).reshape(h, w).copy()
     return sums / spp, per, stats
+
+
+def denoise(image, gbuffer, moments, threads=None) -> np.ndarray:
+    """The reference's bilateral denoiser on the host: image (H, W, 3) read as
+    float32, records as GBUF_DTYPE / STAT_DTYPE (H, W) arrays; returns float32 (H, W, 3)."""
+    exe = ensure_built()
+    img = np.ascontiguousarray(image, np.float32)
+    h, w, _ = img.shape
+    g = np.ascontiguousarray(gbuffer, GBUF_DTYPE).reshape(h, w)
+    m = np.ascontiguousarray(moments, STAT_DTYPE).reshape(h, w)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "in.bin").write_bytes(np.array([w, h], np.int32).tobytes() + img.tobytes() + g.tobytes() + m.tobytes())
+        env = dict(os.environ)
+        if threads:
+            env["OMP_NUM_THREADS"] = str(threads)
+        r = subprocess.run([str(exe), "denoise", str(td / "in.bin"), str(td / "out.bin")], capture_output=True,
+                           text=True, env=env)
+        if r.returncode != 0:
+            raise RuntimeError("reference oracle failed: " + r.stderr)
+        return np.frombuffer((td / "out.bin").read_bytes(), np.float32).reshape(h, w, 3).copy()
 
 
 def trace(tris: np.ndarray, rays: np.ndarray, brute: bool = False, threads=None):

@@ -101,7 +101,7 @@ def test_cpp_layer_equals_python_layer(tmp_path, cuda_device):
         write_pfm
     exe = compile_program(tmp_path, FULL_PROGRAM)
     out = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, check=True).stdout
-    assert out.startswith("texels 16"), out
+    assert out.startswith("texels 48"), out   # floats: 16 texels x RGB
     light = SceneObject((0, 0.49, 0), (0.1, 0.005, 0.1), Material.CreateLight((17, 12, 4)), (0, 0, 0), OBJECT_CUBE)
     v = np.array([[-0.5, -0.5, -0.5], [0.5, -0.5, -0.5], [0.5, -0.5, 0.5], [-0.5, -0.5, 0.5], [-0.5, 0.5, -0.5],
                   [0.5, 0.5, -0.5]], np.float32)
