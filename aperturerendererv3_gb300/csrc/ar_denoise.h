@@ -21,8 +21,6 @@
 #include "ar_vec.h"
 
 #define AR_DN_RADIUS 7                   // Bilateral16x16<7> (core/scene.cu:341)
-#define AR_DN_TILE 16                    // output tile edge
-#define AR_DN_SPAN (AR_DN_TILE + 2 * AR_DN_RADIUS)
 #define AR_DN_MODELS 5                   // diffuse, light, glass, GGX, no hit (EShadingModel::MAT_MAX)
 #define AR_DN_NO_HIT 4
 #define AR_DN_TQ_SIZE 1024               // T_QUANTILE_LUT_SIZE (core/denoise/t_quantile.cuh:6)
@@ -68,8 +66,14 @@ __device__ __forceinline__ void dn_record_model(DnGBuf& g, int model)
     const uint64_t f = g.frames;
     const float affix = 1.0f / (float)(f + 1ull);
     const float pre = (float)f / (float)(f + 1ull);
-    for (int i = 0; i < AR_DN_MODELS; ++i) g.h[8 + i] = __float2half_rn(__half2float(g.h[8 + i]) * pre);
-    g.h[8 + model] = __float2half_rn(__half2float(g.h[8 + model]) + affix);
+#pragma unroll
+    for (int i = 0; i < AR_DN_MODELS; ++i)
+    {
+        const __half scaled = __float2half_rn(__half2float(g.h[8 + i]) * pre);
+        // the bin of this sample's model gains affix (a select, not an indexed
+        // store, so the record stays in registers)
+        g.h[8 + i] = (i == model) ? __float2half_rn(__half2float(scaled) + affix) : scaled;
+    }
 }
 
 // RecordScreenGBuffer (core/denoise/denoise.cuh:106-158) for one sample.

@@ -362,5 +362,7 @@ cudaError_t launch_grad_fold(Ctx& c, double* grad64, long long n, long long* lau
 // the per-pixel records, in sample order
 cudaError_t launch_denoise_record(Ctx& c, const RenderLaunch& rl, long long first_path, int n_paths, long long* launches);
 cudaError_t ensure_denoise(Ctx& c, int width, int height, int first_frame);
+// v[i] *= inv for n doubles on stream s
+cudaError_t launch_scale_means(double* v, long long n, double inv, cudaStream_t s);
 void free_denoise(Ctx& c);
 } // namespace ar

@@ -1111,13 +1111,13 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
         e = cudaMemcpy(c.stats, c.d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
     c.profile = 0;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
-    // mean over samples
-    std::vector<double> sums((size_t)npix * 3);
-    AR_CUDA(ctx, cudaMemcpy(sums.data(), c.d_accum, sums.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    const double inv = 1.0 / (double)rl.spp;
-    for (auto& s : sums) s *= inv;
-    if (out_is_device) AR_CUDA(ctx, cudaMemcpy(out_xyz, sums.data(), sums.size() * sizeof(double), cudaMemcpyHostToDevice));
-    else std::memcpy(out_xyz, sums.data(), sums.size() * sizeof(double));
+    // mean over samples, scaled on the device and copied once
+    const size_t out_bytes = (size_t)npix * 3 * sizeof(double);
+    AR_CUDA(ctx, launch_scale_means(c.d_accum, npix * 3, 1.0 / (double)rl.spp, c.stream));
+    c.last_launches += 1;
+    AR_CUDA(ctx, cudaMemcpyAsync(out_xyz, c.d_accum, out_bytes,
+                                 out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c.stream));
+    AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
     unsigned int word = 0;
     AR_CUDA(ctx, cudaMemcpy(&word, c.d_err, sizeof(word), cudaMemcpyDeviceToHost));
     if (word) return fail(ctx, AR_ERR_DEVICE, "device error word set: " + std::to_string(word));

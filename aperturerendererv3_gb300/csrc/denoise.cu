@@ -8,11 +8,12 @@
 // thread per frame).
 //
 // Filtering: k_bilateral is the reference's Bilateral16x16<7>
-// (core/denoise/denoise.cuh:360-443) restructured for the SM: a 32 x 8 output
-// tile stages the 46 x 22 pixels it reads as per-pixel keys (dn_make_key) in
-// shared memory, planar, so a warp reads 32 consecutive words per field; the
-// t-test of a pair is evaluated first and the G-buffer weight only for pairs
-// that pass (a failing pair contributes weight 0 in the reference as well).
+// (core/denoise/denoise.cuh:360-443) restructured for the SM: one 1024-thread
+// block per 32 x 32 output tile stages the 46 x 46 pixels it reads as
+// per-pixel keys (dn_make_key, 96 B each, 203 KB per block) in shared memory,
+// planar, so a warp reads 32 consecutive words per field; the t-test of a pair
+// is evaluated first and the G-buffer weight only for pairs that pass (a
+// failing pair contributes weight 0 in the reference as well).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,25 +27,24 @@ namespace ar
 {
 namespace
 {
-constexpr int TX = 32, TY = 8;                       // output tile
+constexpr int TX = 32, TY = 32;                      // output tile
 constexpr int SX = TX + 2 * AR_DN_RADIUS;            // 46
-constexpr int SY = TY + 2 * AR_DN_RADIUS;            // 22
+constexpr int SY = TY + 2 * AR_DN_RADIUS;            // 46
 constexpr int SPAN = SX * SY;                        // staged pixels per tile
 constexpr int TAPS = (2 * AR_DN_RADIUS + 1) * (2 * AR_DN_RADIUS + 1);
 // planes of the staged keys (one float or one 32-bit word per pixel each)
 enum
 {
     P_COL = 0,
-    P_ALB = 3,
-    P_NRM = 6,
-    P_DEP = 9,
-    P_MR = 10,
-    P_MOD = 11,   // 3 words: 6 halves
-    P_TH = 14,
-    P_VTH = 17,
-    P_UP = 20,
-    P_LO = 23,
-    P_COUNT = 26
+    P_NRM = 3,
+    P_DEP = 6,
+    P_H = 7,      // 5 words of half pairs: (albedo x, y), (albedo z, metallic), (roughness, model 0),
+                  // (model 1, model 2), (model 3, model 4)
+    P_TH = 12,
+    P_VTH = 15,
+    P_UP = 18,
+    P_LO = 21,
+    P_COUNT = 24
 };
 constexpr size_t SMEM_BYTES = ((size_t)P_COUNT * SPAN + AR_DN_TQ_SIZE + TAPS) * sizeof(float);
 } // namespace
@@ -93,7 +93,7 @@ __device__ __forceinline__ __half half_hi(uint32_t w) { return __ushort_as_half(
 // subtraction (rounded to half), then widened
 __device__ __forceinline__ float hdiff(__half a, __half b) { return __half2float(__hsub(a, b)); }
 
-__global__ void __launch_bounds__(TX * TY, 2) k_bilateral(const double* __restrict__ in_xyz, double* __restrict__ out_xyz,
+__global__ void __launch_bounds__(TX * TY, 1) k_bilateral(const double* __restrict__ in_xyz, double* __restrict__ out_xyz,
                                                          const DnGBuf* __restrict__ gb, const DnStat* __restrict__ st,
                                                          const float* __restrict__ tq_global, int W, int H)
 {
@@ -120,7 +120,6 @@ __global__ void __launch_bounds__(TX * TY, 2) k_bilateral(const double* __restri
         for (int ch = 0; ch < 3; ++ch)
         {
             sm[(P_COL + ch) * SPAN + e] = k.col[ch];
-            sm[(P_ALB + ch) * SPAN + e] = k.alb[ch];
             sm[(P_NRM + ch) * SPAN + e] = k.nrm[ch];
             sm[(P_TH + ch) * SPAN + e] = k.theta[ch];
             sm[(P_VTH + ch) * SPAN + e] = k.vth[ch];
@@ -128,8 +127,11 @@ __global__ void __launch_bounds__(TX * TY, 2) k_bilateral(const double* __restri
             sm[(P_LO + ch) * SPAN + e] = k.lo[ch];
         }
         sm[P_DEP * SPAN + e] = k.depth;
-        smu[P_MR * SPAN + e] = half2_bits(k.mr[0], k.mr[1]);
-        for (int w = 0; w < 3; ++w) smu[(P_MOD + w) * SPAN + e] = half2_bits(k.model[2 * w], k.model[2 * w + 1]);
+        smu[P_H * SPAN + e] = half2_bits(__float2half_rn(k.alb[0]), __float2half_rn(k.alb[1]));
+        smu[(P_H + 1) * SPAN + e] = half2_bits(__float2half_rn(k.alb[2]), k.mr[0]);
+        smu[(P_H + 2) * SPAN + e] = half2_bits(k.mr[1], k.model[0]);
+        smu[(P_H + 3) * SPAN + e] = half2_bits(k.model[1], k.model[2]);
+        smu[(P_H + 4) * SPAN + e] = half2_bits(k.model[3], k.model[4]);
     }
     __syncthreads();
     const int ox = blockIdx.x * TX + threadIdx.x, oy = blockIdx.y * TY + threadIdx.y;
@@ -137,11 +139,10 @@ __global__ void __launch_bounds__(TX * TY, 2) k_bilateral(const double* __restri
 
     // centre key
     const int ce = (threadIdx.y + AR_DN_RADIUS) * SX + threadIdx.x + AR_DN_RADIUS;
-    float cCol[3], cAlb[3], cNrm[3], cTh[3], cVth[3], cUp[3], cLo[3];
+    float cCol[3], cNrm[3], cTh[3], cVth[3], cUp[3], cLo[3];
     for (int ch = 0; ch < 3; ++ch)
     {
         cCol[ch] = sm[(P_COL + ch) * SPAN + ce];
-        cAlb[ch] = sm[(P_ALB + ch) * SPAN + ce];
         cNrm[ch] = sm[(P_NRM + ch) * SPAN + ce];
         cTh[ch] = sm[(P_TH + ch) * SPAN + ce];
         cVth[ch] = sm[(P_VTH + ch) * SPAN + ce];
@@ -149,8 +150,10 @@ __global__ void __launch_bounds__(TX * TY, 2) k_bilateral(const double* __restri
         cLo[ch] = sm[(P_LO + ch) * SPAN + ce];
     }
     const float cDep = sm[P_DEP * SPAN + ce];
-    const uint32_t cMR = smu[P_MR * SPAN + ce];
-    const uint32_t cM0 = smu[P_MOD * SPAN + ce], cM1 = smu[(P_MOD + 1) * SPAN + ce], cM2 = smu[(P_MOD + 2) * SPAN + ce];
+    const uint32_t cH0 = smu[P_H * SPAN + ce], cH1 = smu[(P_H + 1) * SPAN + ce], cH2 = smu[(P_H + 2) * SPAN + ce],
+                   cH3 = smu[(P_H + 3) * SPAN + ce], cH4 = smu[(P_H + 4) * SPAN + ce];
+    const float cAlb0 = __half2float(half_lo(cH0)), cAlb1 = __half2float(half_hi(cH0)),
+                cAlb2 = __half2float(half_lo(cH1));
 
     constexpr float CENTER_EPS = 1.0e-6f;
     float acc0 = cCol[0] * CENTER_EPS, acc1 = cCol[1] * CENTER_EPS, acc2 = cCol[2] * CENTER_EPS;
@@ -164,9 +167,12 @@ __global__ void __launch_bounds__(TX * TY, 2) k_bilateral(const double* __restri
             const int e = row + ii;
             // ComputeTStatisticFinal (core/denoise/denoise.cuh:309-321): all three
             // channels below their Welch-t threshold
+            // (a channel that fails decides the pair; the rest need not be evaluated)
             bool pass = true;
+#pragma unroll
             for (int ch = 0; ch < 3; ++ch)
             {
+                if (!pass) break;
                 const float t = cTh[ch] - sm[(P_TH + ch) * SPAN + e];
                 const float t2 = t * t;
                 const float vB = sm[(P_VTH + ch) * SPAN + e];
@@ -174,17 +180,18 @@ __global__ void __launch_bounds__(TX * TY, 2) k_bilateral(const double* __restri
                 const float T = sqrtf(0.5f / (1.0f - wAsym) - 1.0f);
                 const float u = cUp[ch] + sm[(P_UP + ch) * SPAN + e];
                 const float nu = u * u / (cLo[ch] + sm[(P_LO + ch) * SPAN + e]);
-                pass = pass && (T < dn_t_quantile(s_tq, nu));
+                pass = T < dn_t_quantile(s_tq, nu);
             }
             float weight = 0.0f;
             if (pass)
             {
                 // ComputeSVGFWeight (core/denoise/denoise.cuh:178-242)
                 float wTerm = 0.0f;
+                const uint32_t b0 = smu[P_H * SPAN + e], b1 = smu[(P_H + 1) * SPAN + e];
                 {
-                    const float d0 = cAlb[0] - sm[P_ALB * SPAN + e];
-                    const float d1 = cAlb[1] - sm[(P_ALB + 1) * SPAN + e];
-                    const float d2 = cAlb[2] - sm[(P_ALB + 2) * SPAN + e];
+                    const float d0 = cAlb0 - __half2float(half_lo(b0));
+                    const float d1 = cAlb1 - __half2float(half_hi(b0));
+                    const float d2 = cAlb2 - __half2float(half_lo(b1));
                     wTerm += (d0 * d0 + d1 * d1 + d2 * d2) * DnSigma::kAlbedo;
                 }
                 {
@@ -199,24 +206,23 @@ __global__ void __launch_bounds__(TX * TY, 2) k_bilateral(const double* __restri
                     const float d = (cDep - b) / denom;
                     wTerm += d * d * DnSigma::kDepth;
                 }
-                const uint32_t bMR = smu[P_MR * SPAN + e];
+                const uint32_t b2 = smu[(P_H + 2) * SPAN + e];
                 {
-                    const float dm = hdiff(half_lo(cMR), half_lo(bMR));
+                    const float dm = hdiff(half_hi(cH1), half_hi(b1));
                     wTerm += dm * dm * DnSigma::kMetallic;
                 }
                 {
-                    const float dr = hdiff(half_hi(cMR), half_hi(bMR));
+                    const float dr = hdiff(half_lo(cH2), half_lo(b2));
                     wTerm += dr * dr * DnSigma::kRough;
                 }
                 {
-                    const uint32_t b0 = smu[P_MOD * SPAN + e], b1 = smu[(P_MOD + 1) * SPAN + e],
-                                   b2 = smu[(P_MOD + 2) * SPAN + e];
+                    const uint32_t b3 = smu[(P_H + 3) * SPAN + e], b4 = smu[(P_H + 4) * SPAN + e];
                     float l1 = 0.0f;
-                    l1 += fabsf(hdiff(half_lo(cM0), half_lo(b0)));
-                    l1 += fabsf(hdiff(half_hi(cM0), half_hi(b0)));
-                    l1 += fabsf(hdiff(half_lo(cM1), half_lo(b1)));
-                    l1 += fabsf(hdiff(half_hi(cM1), half_hi(b1)));
-                    l1 += fabsf(hdiff(half_lo(cM2), half_lo(b2)));
+                    l1 += fabsf(hdiff(half_hi(cH2), half_hi(b2)));
+                    l1 += fabsf(hdiff(half_lo(cH3), half_lo(b3)));
+                    l1 += fabsf(hdiff(half_hi(cH3), half_hi(b3)));
+                    l1 += fabsf(hdiff(half_lo(cH4), half_lo(b4)));
+                    l1 += fabsf(hdiff(half_hi(cH4), half_hi(b4)));
                     const float tv = 0.5f * l1;
                     wTerm += tv * tv * DnSigma::kModel;
                 }

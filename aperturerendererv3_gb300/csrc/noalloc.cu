@@ -73,11 +73,6 @@ T* carve(unsigned char*& cur, size_t n)
     return p;
 }
 
-__global__ void k_scale_means(double* v, long long n, double inv)
-{
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) v[i] *= inv;
-}
 } // namespace
 
 extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz_device, void* stream)
@@ -189,7 +184,7 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
     if (e == cudaSuccess)
     {
         const long long nv = npix * 3;
-        k_scale_means<<<(int)((nv + 255) / 256), 256, 0, wb.stream>>>(out_xyz_device, nv, 1.0 / (double)rl.spp);
+        launch_scale_means(out_xyz_device, nv, 1.0 / (double)rl.spp, wb.stream);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess)

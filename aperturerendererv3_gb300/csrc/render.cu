@@ -1173,6 +1173,20 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     return cudaGetLastError();
 }
 
+// per-pixel sums -> means (one double multiply each, as the host would do it)
+__global__ void k_scale_means(double* v, long long n, double inv)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) v[i] *= inv;
+}
+
+cudaError_t launch_scale_means(double* v, long long n, double inv, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    k_scale_means<<<(int)((n + 255) / 256), 256, 0, s>>>(v, n, inv);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_accumulate(Ctx& c, const RenderLaunch& rl, long long first_path, int n, double* accum, long long* launches)
 {
     const long long npix = (long long)rl.width * rl.height;

@@ -306,6 +306,55 @@ def combined_extra(device: int, spp: int = 16) -> dict:
     return out
 
 
+def denoise_extra(r, w, cam, spp: int = 8, steps: int = 5) -> dict:
+    """The denoiser on the headline workload's image: a render with and without
+    the per-sample G-buffer / moment records (device time of ar_render), the
+    bilateral filter of the 1920x1080 result (CUDA events on the launching
+    stream, mean over `steps` launches) and the reference's own filter loop on
+    the host over a 256 x 256 crop of the same image and records."""
+    import torch
+    size, kw = w["size"], dict(fov=cam["fov"], max_depth=w["depth"])
+    r.Render(size, cam["origin"], cam["direction"], spp, **kw)
+    plain_ms = r.last_render_stats()[0]
+    img = r.Render(size, cam["origin"], cam["direction"], spp, **kw)
+    r.Render(size, cam["origin"], cam["direction"], spp, denoise=True, **kw)
+    rec_ms = r.last_render_stats()[0]
+    dev = torch.device("cuda", r.device)
+    t = torch.as_tensor(img, device=dev)
+    for _ in range(2):
+        r.denoise(t)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(steps):
+        r.denoise(t)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    filt_ms = e0.elapsed_time(e1) / steps
+    npix = size[0] * size[1]
+    out = {"width": size[0], "height": size[1], "spp": spp, "render_ms": plain_ms, "render_with_records_ms": rec_ms,
+           "record_overhead": rec_ms / plain_ms - 1.0, "filter_ms": filt_ms,
+           "filter_mpix_per_s": npix / (filt_ms / 1e3) / 1e6,
+           "filter_pairs_per_s": npix * 225 / (filt_ms / 1e3), "taps": 225}
+    try:
+        import time
+        from oracle import ref_runner as rr
+        if rr.available():
+            g, m = r.denoise_records()
+            y0, x0, n = size[1] // 2 - 128, size[0] // 2 - 128, 256
+            crop = (slice(y0, y0 + n), slice(x0, x0 + n))
+            t0 = time.perf_counter()
+            rr.denoise(img[crop], g[crop], m[crop])
+            cpu_s = time.perf_counter() - t0
+            out["cpu_reference"] = {"mpix_per_s": n * n / cpu_s / 1e6, "cores": os.cpu_count() or 1,
+                                    "sample": "256 x 256 crop of the same image and records",
+                                    "kind": "reference"}
+    except Exception as e:  # the CPU comparison never hides the GPU numbers
+        out["cpu_reference"] = {"error": str(e)}
+    return out
+
+
 def bvh_stress_extra(device: int, steps: int) -> dict:
     """BVH stress workload: 1M random triangles (centroids U[0,1]^3, vertices
     +N(0, 0.005^2)), 1920x1080 primary rays plus one cosine-hemisphere bounce ray
@@ -485,7 +534,8 @@ def main() -> None:
                          ("adjoint", lambda: adjoint_extra(local, 3)),
                          ("combined", lambda: combined_extra(local) if args.workload != "combined" else
                           {"note": "the headline is the combined workload"}),
-                         ("bvh_stress", lambda: bvh_stress_extra(local, 5))):
+                         ("bvh_stress", lambda: bvh_stress_extra(local, 5)),
+                         ("denoise", lambda: denoise_extra(r, w, cam))):
             try:
                 extras[name] = fn()
             except Exception as e:  # an extra never hides the headline
