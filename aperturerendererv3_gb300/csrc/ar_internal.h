@@ -130,6 +130,9 @@ struct StageEvent
 };
 
 // Per-path state of the wavefront integrator (structure of arrays).
+// ints in a render wave's counter array (layout: AR_CNT_* in render.cu)
+#define AR_CNT_COUNT 8
+
 struct PathState
 {
     uint64_t* rng;

@@ -98,23 +98,54 @@ AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3
 #define AR_DEVERR_STACK 1u
 #define AR_DEVERR_QUEUE 2u
 
+// Traversal of one ray as a resumable state: init() sets it up, each step()
+// visits one node (box tests of its children, the primitives of the hit
+// leaves, the next node from the children or the stack) and returns false once
+// the traversal is over.  The persistent wavefront kernels interleave steps of
+// many rays per lane (refilling lanes whose ray finished); traverse() runs one
+// ray to completion.  Either way a ray performs the same operations in the
+// same order.
 template <bool AnyHit>
-AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,
-                                                    unsigned int* err, uint32_t& n_visits, uint32_t& n_tests)
+struct TravState
 {
+    V3 o, d, inv;
+    RayShear sh;
+    uint32_t oct;
+    float tmin, tmax;
     TravResult res;
-    res.t = tmax;
-    res.slot = -1;
-    res.id = -1;
-    if (sc.node_count <= 0) return res;
-    const RayShear sh = make_shear(d);
-    const V3 inv = v3(inv_safe(d.x), inv_safe(d.y), inv_safe(d.z));
-    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    int node;
+    int sp;
+    uint32_t n_visits, n_tests;
     uint2 stack[AR_TRAV_STACK];
-    int sp = 0;
-    int node = 0;
-    while (true)
+
+    AR_HD void init(const TravScene& sc, V3 o_, V3 d_, float tmin_, float tmax_)
     {
+        o = o_;
+        d = d_;
+        tmin = tmin_;
+        tmax = tmax_;
+        res.t = tmax_;
+        res.slot = -1;
+        res.id = -1;
+        sh = make_shear(d_);
+        inv = v3(inv_safe(d_.x), inv_safe(d_.y), inv_safe(d_.z));
+        oct = (d_.x < 0.0f ? 1u : 0u) | (d_.y < 0.0f ? 2u : 0u) | (d_.z < 0.0f ? 4u : 0u);
+        sp = 0;
+        node = sc.node_count > 0 ? 0 : -2;  // -2: nothing to traverse
+        n_visits = 0;
+        n_tests = 0;
+    }
+
+    AR_HD TravResult result() const
+    {
+        TravResult r = res;
+        if (r.slot < 0) r.t = tmax;
+        return r;
+    }
+
+    AR_HD bool step(const TravScene& sc, unsigned int* err)
+    {
+        if (node == -2) return false;
         if (node >= 0)
         {
             ++n_visits;
@@ -176,7 +207,8 @@ AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, floa
                             res.t = t;
                             res.slot = first + k;
                             res.id = id;
-                            return res;
+                            node = -2;
+                            return false;
                         }
                     }
                     else if (t < res.t || (t == res.t && res.id >= 0 && id < res.id))
@@ -199,11 +231,15 @@ AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, floa
                     if (sp < AR_TRAV_STACK) stack[sp++] = make_uint2(child_base, hit_int | (imask << 8));
                     else if (err) AR_ATOMIC_OR(err, AR_DEVERR_STACK);
                 }
-                continue;
+                return true;
             }
         }
-        if (sp == 0) break;
-        uint2 e = stack[--sp];
+        if (sp == 0)
+        {
+            node = -2;
+            return false;
+        }
+        const uint2 e = stack[--sp];
         uint32_t m = e.y & 0xffu;
         const uint32_t im = e.y >> 8;
         const uint32_t i = AR_FFS(m) - 1;
@@ -211,9 +247,22 @@ AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, floa
         const uint32_t s = i ^ oct;
         node = (int)(e.x + AR_POPC(im & ((1u << s) - 1u)));
         if (m) stack[sp++] = make_uint2(e.x, m | (im << 8));
+        return true;
     }
-    if (res.slot < 0) res.t = tmax;
-    return res;
+};
+
+template <bool AnyHit>
+AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,
+                                                    unsigned int* err, uint32_t& n_visits, uint32_t& n_tests)
+{
+    TravState<AnyHit> st;
+    st.init(sc, o, d, tmin, tmax);
+    while (st.step(sc, err))
+    {
+    }
+    n_visits = st.n_visits;
+    n_tests = st.n_tests;
+    return st.result();
 }
 
 // stats (optional): [0] += node visits, [1] += primitive tests

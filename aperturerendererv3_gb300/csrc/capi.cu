@@ -581,7 +581,7 @@ ar_status ar_create(ar_ctx** out, int device)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_err, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(c.d_err, 0, sizeof(unsigned int));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_counters, 8 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_counters, AR_CNT_COUNT * sizeof(int));
     // spectral tables: CIE CMFs, D65, lambda LUT (built on the host: 840 encoder runs)
     if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_cie, sizeof(AR_TAB_CMF));
     if (e == cudaSuccess) e = cudaMemcpy(c.d_cie, AR_TAB_CMF, sizeof(AR_TAB_CMF), cudaMemcpyHostToDevice);

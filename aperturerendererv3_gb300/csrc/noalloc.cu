@@ -135,7 +135,7 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
     wb.sq.valid_unocc = carve<uint8_t>(cur, n);
     wb.queue[0] = carve<int>(cur, n);
     wb.queue[1] = carve<int>(cur, n);
-    wb.counters = carve<int>(cur, 4);
+    wb.counters = carve<int>(cur, AR_CNT_COUNT);
     if ((size_t)(cur - base) > AR_NOALLOC_SCRATCH_BYTES)
     {
         c.last_error = "render_noalloc: scratch layout exceeds the array";

@@ -160,6 +160,13 @@ __device__ __forceinline__ int albedo_texel(const DevScene& sc, int tex, int slo
     return ti.x + y * ti.y + x;
 }
 
+// counters of a render wave (c.d_counters / the allocation-free scratch)
+#define AR_CNT_Q0 0          // queue 0 length
+#define AR_CNT_Q1 1          // queue 1 length
+#define AR_CNT_SHADOW 2
+#define AR_CNT_MLP 3
+#define AR_CNT_FETCH 4       // k_extend, k_shadow fetch counters
+
 // ---------------------------------------------------------------- raygen
 struct CamParams
 {
@@ -207,54 +214,118 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
 }
 
 // ---------------------------------------------------------------- extend
+// The traversal kernels are persistent over the queue: a warp's lanes take
+// rays from a global fetch counter, step their traversals, and whenever at
+// least a threshold of lanes have finished, the warp fetches that many new rays
+// (one atomic per warp), so lanes do not idle behind the warp's longest ray.
+#ifndef AR_EXT_REFILL_MIN
+#define AR_EXT_REFILL_MIN 4      // closest hit: idle lanes that trigger a refill
+#endif
+#ifndef AR_EXT_STEPS
+#define AR_EXT_STEPS 8           // closest hit: node visits between refill checks
+#endif
+#ifndef AR_SHD_REFILL_MIN
+#define AR_SHD_REFILL_MIN 8      // shadow rays
+#endif
+#ifndef AR_SHD_STEPS
+#define AR_SHD_STEPS 16
+#endif
+
+// Warp-wide fetch of rays for the idle lanes: true and *q = the lane's queue
+// index when it got one; *exhausted (warp-uniform) once the queue is used up.
+template <int MinIdle>
+__device__ __forceinline__ bool warp_refill(int* fetch, int n, bool active, bool* exhausted, int* q)
+{
+    const unsigned idle = __ballot_sync(0xffffffffu, !active);
+    if (*exhausted || __popc(idle) < MinIdle) return false;
+    const int need = __popc(idle);
+    const int leader = __ffs(idle) - 1;
+    int base = 0;
+    if (lane_id() == leader) base = atomicAdd(fetch, need);
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (base + need >= n) *exhausted = true;
+    if (active) return false;
+    *q = base + __popc(idle & ((1u << lane_id()) - 1u));
+    return *q < n;
+}
+
+// closest hit of a finished traversal: the SDF object is marched up to the
+// BVH hit (it has the largest primitive id: a BVH hit at equal t wins)
+__device__ __forceinline__ void extend_finish(const DevScene& sc, const PathState& ps, int p,
+                                              const TravState<false>& st)
+{
+    const TravResult r = st.result();
+    float t = r.t;
+    int slot = r.slot;
+    if (sc.trav.sdf.count > 0)
+    {
+        const float ts = sdf_march(sc.trav.sdf, st.o, st.d, sdf_eps(st.tmin), slot < 0 ? 3.0e38f : t);
+        if (ts >= st.tmin && (slot < 0 || ts < t))
+        {
+            t = ts;
+            slot = AR_SLOT_SDF;
+        }
+    }
+    if (sc.stats)
+    {
+        atomicAdd(&sc.stats[0], (unsigned long long)st.n_visits);
+        atomicAdd(&sc.stats[1], (unsigned long long)st.n_tests);
+        atomicAdd(&sc.stats[4], 1ull);
+    }
+    ps.hit_t[p] = t;
+    ps.hit_slot[p] = slot;
+}
+
 __global__ void __launch_bounds__(AR_BLOCK) k_extend(DevScene sc, PathState ps, const int* __restrict__ queue,
-                                                   const int* __restrict__ counter, unsigned int* err)
+                                                   const int* __restrict__ counter, int* fetch, unsigned int* err)
 {
     const int n = *counter;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    TravState<false> st;
+    int p = 0;
+    bool active = false, exhausted = false;
+    while (true)
     {
-        const int p = queue[q];
-        const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
-        const V3 o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
-        const uint32_t dep = ps.depths[p];
-        const int ndd = (int)(dep >> 16);
-        const float tmin = intersect_eps(ndd);
-        const uint32_t fl = ps.flags[p];
-        const int mobj = __float_as_int(ps.media_v[p].w);
-        float t = 0.0f;
-        int slot = -1;
-        if ((fl & 1u) && mobj >= 0)
+        int q;
+        if (warp_refill<AR_EXT_REFILL_MIN>(fetch, n, active, &exhausted, &q))
         {
-            // inside a medium: intersect only the enclosing object (render.cuh:89-92)
-            const int s = sc.prim_slot[mobj];
-            int id;
-            const float th = prim_hit(sc.trav, s, make_shear(d), o, d, &id, tmin);
-            if (th >= tmin)
+            p = queue[q];
+            const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
+            const V3 o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
+            const float tmin = intersect_eps((int)(ps.depths[p] >> 16));
+            const int mobj = __float_as_int(ps.media_v[p].w);
+            if ((ps.flags[p] & 1u) && mobj >= 0)
             {
-                t = th;
-                slot = s;
+                // inside a medium: intersect only the enclosing object (render.cuh:89-92)
+                const int s = sc.prim_slot[mobj];
+                int id;
+                const float th = prim_hit(sc.trav, s, make_shear(d), o, d, &id, tmin);
+                ps.hit_t[p] = th >= tmin ? th : 0.0f;
+                ps.hit_slot[p] = th >= tmin ? s : -1;
+                if (sc.stats) atomicAdd(&sc.stats[4], 1ull);
+            }
+            else
+            {
+                st.init(sc.trav, o, d, tmin, __int_as_float(0x7f800000));
+                active = true;
             }
         }
-        else
+        if (__ballot_sync(0xffffffffu, active) == 0)
         {
-            const TravResult r = traverse<false>(sc.trav, o, d, tmin, __int_as_float(0x7f800000), err,
-                                                 sc.stats ? sc.stats + 0 : nullptr);
-            t = r.t;
-            slot = r.slot;
-            if (sc.trav.sdf.count > 0)
+            if (exhausted) break;
+            continue;
+        }
+        if (active)
+        {
+            for (int it = 0; it < AR_EXT_STEPS; ++it)
             {
-                // the SDF object has the largest primitive id: a BVH hit at equal t wins
-                const float ts = sdf_march(sc.trav.sdf, o, d, sdf_eps(tmin), slot < 0 ? 3.0e38f : t);
-                if (ts >= tmin && (slot < 0 || ts < t))
+                if (!st.step(sc.trav, err))
                 {
-                    t = ts;
-                    slot = AR_SLOT_SDF;
+                    extend_finish(sc, ps, p, st);
+                    active = false;
+                    break;
                 }
             }
         }
-        if (sc.stats) atomicAdd(&sc.stats[4], 1ull);
-        ps.hit_t[p] = t;
-        ps.hit_slot[p] = slot;
     }
 }
 
@@ -877,26 +948,61 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
 }
 
 // ---------------------------------------------------------------- shadow
+__device__ __forceinline__ void shadow_finish(const DevScene& sc, const PathState& ps, const ShadowQueue& sq, int i,
+                                              int p, const TravState<true>& st)
+{
+    bool occluded = st.result().slot >= 0;
+    if (!occluded && sc.trav.sdf.count > 0)
+    {
+        const float ts = sdf_march(sc.trav.sdf, st.o, st.d, sdf_eps(0.0f), st.tmax);
+        occluded = ts >= 0.0f && ts < st.tmax;
+    }
+    if (sc.stats)
+    {
+        atomicAdd(&sc.stats[2], (unsigned long long)st.n_visits);
+        atomicAdd(&sc.stats[3], (unsigned long long)st.n_tests);
+        atomicAdd(&sc.stats[5], 1ull);
+    }
+    ps.radiance[p] = ps.radiance[p] + (occluded ? sq.v_occ[i] : sq.d[i].w);
+    const bool valid = occluded ? true : (sq.valid_unocc[i] != 0);
+    ps.flags[p] = (ps.flags[p] & ~2u) | (valid ? 2u : 0u);
+}
+
 __global__ void __launch_bounds__(AR_BLOCK) k_shadow(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ counter,
-                                                   unsigned int* err)
+                                                   int* fetch, unsigned int* err)
 {
     const int n = *counter;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    TravState<true> st;
+    int i = 0, p = 0;
+    bool active = false, exhausted = false;
+    while (true)
     {
-        const float4 o = sq.o[i], d = sq.d[i];
-        const int p = sq.path[i];
-        const TravResult r = traverse<true>(sc.trav, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, o.w, err,
-                                            sc.stats ? sc.stats + 2 : nullptr);
-        if (sc.stats) atomicAdd(&sc.stats[5], 1ull);
-        bool occluded = r.slot >= 0;
-        if (!occluded && sc.trav.sdf.count > 0)
+        int q;
+        if (warp_refill<AR_SHD_REFILL_MIN>(fetch, n, active, &exhausted, &q))
         {
-            const float ts = sdf_march(sc.trav.sdf, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), sdf_eps(0.0f), o.w);
-            occluded = ts >= 0.0f && ts < o.w;
+            i = q;
+            p = sq.path[i];
+            const float4 o = sq.o[i], d = sq.d[i];
+            st.init(sc.trav, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, o.w);
+            active = true;
         }
-        ps.radiance[p] = ps.radiance[p] + (occluded ? sq.v_occ[i] : d.w);
-        const bool valid = occluded ? true : (sq.valid_unocc[i] != 0);
-        ps.flags[p] = (ps.flags[p] & ~2u) | (valid ? 2u : 0u);
+        if (__ballot_sync(0xffffffffu, active) == 0)
+        {
+            if (exhausted) break;
+            continue;
+        }
+        if (active)
+        {
+            for (int it = 0; it < AR_SHD_STEPS; ++it)
+            {
+                if (!st.step(sc.trav, err))
+                {
+                    shadow_finish(sc, ps, sq, i, p, st);
+                    active = false;
+                    break;
+                }
+            }
+        }
     }
 }
 
@@ -1055,12 +1161,12 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
     const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
     const int grid_p = sms * 8;
-    int* cnt = c.d_counters;  // [0],[1]: extend queues, [2]: shadow
+    int* cnt = c.d_counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
     {
         StageScope st(c, ST_RAYGEN);
-        k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, c.d_queue[0], &cnt[0], first_path, n, rl.width, rl.height, rl.seed,
-                                             rl.first_frame, cam, c.camera_inside);
+        k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, c.d_queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height,
+                                             rl.seed, rl.first_frame, cam, c.camera_inside);
         if (rl.guide) k_guide_init<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, n);
     }
     long long L = rl.guide ? 2 : 1;
@@ -1079,39 +1185,40 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
-        cudaMemsetAsync(&cnt[nxt], 0, sizeof(int), s);
-        cudaMemsetAsync(&cnt[2], 0, sizeof(int), s);
+        int* qn = &cnt[AR_CNT_Q0 + cur];
+        cudaMemsetAsync(&cnt[AR_CNT_Q0 + nxt], 0, sizeof(int), s);
+        cudaMemsetAsync(&cnt[AR_CNT_SHADOW], 0, sizeof(int), s);
+        cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, 2 * sizeof(int), s);  // fetch counters of k_extend / k_shadow
         {
             StageScope st(c, ST_EXTEND);
-            k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], &cnt[cur], c.d_err);
+            k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, &cnt[AR_CNT_FETCH], c.d_err);
         }
         {
             StageScope st(c, ST_SHADE);
             if (rl.guide == 2 && rl.mlp_ready)
             {
                 // network inference for every queued hit (tensor cores), before shading
-                cudaMemsetAsync(&cnt[3], 0, sizeof(int), s);
-                k_mlp_query<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], &cnt[cur], c.d_mlp_list, &cnt[3]);
-                launch_mlp_infer(net, c.ps.q_pos, c.ps.q_wr, c.d_mlp_list, &cnt[3], 0, c.ps.q_dist, nullptr, c.d_err,
+                cudaMemsetAsync(&cnt[AR_CNT_MLP], 0, sizeof(int), s);
+                k_mlp_query<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, c.d_mlp_list, &cnt[AR_CNT_MLP]);
+                launch_mlp_infer(net, c.ps.q_pos, c.ps.q_wr, c.d_mlp_list, &cnt[AR_CNT_MLP], 0, c.ps.q_dist, nullptr, c.d_err,
                                  sms, s);
                 L += 2;
             }
+            int* shc = &cnt[AR_CNT_SHADOW];
+            int* nq = c.d_queue[nxt];
+            int* nn = &cnt[AR_CNT_Q0 + nxt];
             if (rl.guide == 2)
-                k_shade<2, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
-                                                              c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
+                k_shade<2, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
             else if (rl.guide)
-                k_shade<1, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
-                                                              c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
+                k_shade<1, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
             else if (rl.adjoint)
-                k_shade<0, true><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
-                                                                 c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
+                k_shade<0, true><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
             else
-                k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], &cnt[cur],
-                                                                  c.d_queue[nxt], &cnt[nxt], &cnt[2], prm);
+                k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
         }
         {
             StageScope st(c, ST_SHADOW);
-            k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[2], c.d_err);
+            k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], c.d_err);
         }
         L += 3;
     }
@@ -1144,9 +1251,9 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
     const int grid_p = sms * 8;
-    int* cnt = wb.counters;
+    int* cnt = wb.counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
-    k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(wb.ps, wb.queue[0], &cnt[0], first_path, n, rl.width, rl.height, rl.seed,
+    k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(wb.ps, wb.queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height, rl.seed,
                                          rl.first_frame, cam, camera_inside);
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
@@ -1159,12 +1266,13 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
-        cudaMemsetAsync(&cnt[nxt], 0, sizeof(int), s);
-        cudaMemsetAsync(&cnt[2], 0, sizeof(int), s);
-        k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[cur], err);
-        k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[cur], wb.queue[nxt], &cnt[nxt],
-                                                   &cnt[2], prm);
-        k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[2], err);
+        cudaMemsetAsync(&cnt[AR_CNT_Q0 + nxt], 0, sizeof(int), s);
+        cudaMemsetAsync(&cnt[AR_CNT_SHADOW], 0, sizeof(int), s);
+        cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, 2 * sizeof(int), s);
+        k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur], &cnt[AR_CNT_FETCH], err);
+        k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[AR_CNT_Q0 + cur],
+                                                   wb.queue[nxt], &cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], prm);
+        k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], err);
     }
     k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);
     const long long npix = (long long)rl.width * rl.height;
