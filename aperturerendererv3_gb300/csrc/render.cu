@@ -230,6 +230,9 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
 #ifndef AR_SHD_STEPS
 #define AR_SHD_STEPS 16
 #endif
+#ifndef AR_TRAV_MIN_BLOCKS
+#define AR_TRAV_MIN_BLOCKS 5     // blocks per SM the traversal kernels are compiled for (48 registers)
+#endif
 
 // Warp-wide fetch of rays for the idle lanes: true and *q = the lane's queue
 // index when it got one; *exhausted (warp-uniform) once the queue is used up.
@@ -276,7 +279,7 @@ __device__ __forceinline__ void extend_finish(const DevScene& sc, const PathStat
     ps.hit_slot[p] = slot;
 }
 
-__global__ void __launch_bounds__(AR_BLOCK) k_extend(DevScene sc, PathState ps, const int* __restrict__ queue,
+__global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScene sc, PathState ps, const int* __restrict__ queue,
                                                    const int* __restrict__ counter, int* fetch, unsigned int* err)
 {
     const int n = *counter;
@@ -968,7 +971,7 @@ __device__ __forceinline__ void shadow_finish(const DevScene& sc, const PathStat
     ps.flags[p] = (ps.flags[p] & ~2u) | (valid ? 2u : 0u);
 }
 
-__global__ void __launch_bounds__(AR_BLOCK) k_shadow(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ counter,
+__global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_shadow(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ counter,
                                                    int* fetch, unsigned int* err)
 {
     const int n = *counter;
