@@ -422,6 +422,9 @@ def main() -> None:
     ap.add_argument("--guide", type=int, default=0, choices=[0, 1, 2], help="1: voxel path guide, 2: MLP guide")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the guided, adjoint and BVH-stress measurements reported beside the headline")
+    ap.add_argument("--extras", default=None,
+                    help="comma-separated subset of the extras to run (guided_voxel, guide_compare, adjoint, combined, "
+                         "bvh_stress, denoise); default: all")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = dict(WORKLOADS[args.workload])
@@ -536,6 +539,8 @@ def main() -> None:
                           {"note": "the headline is the combined workload"}),
                          ("bvh_stress", lambda: bvh_stress_extra(local, 5)),
                          ("denoise", lambda: denoise_extra(r, w, cam))):
+            if args.extras and name not in args.extras.split(","):
+                continue
             try:
                 extras[name] = fn()
             except Exception as e:  # an extra never hides the headline
