@@ -22,6 +22,9 @@ AR_ERR_DEVICE = -5
 
 OBJECT_CUBE = 0
 OBJECT_SPHERE = 1
+OBJECT_SDF = 2
+SDF_OBJECT_TORUS, SDF_OBJECT_VOLUME = 0, 1
+SDF_FN_TORUS, SDF_FN_DIAMOND = 0, 1
 OBJECT_TRIANGLE = 3
 
 SHADING_DIFFUSE = 0
@@ -43,7 +46,8 @@ class ArMaterial(C.Structure):
 
 class ArObject(C.Structure):
     _fields_ = [("type", C.c_int32), ("material", C.c_int32), ("center", F3), ("extent", F3),
-                ("rotation_deg", F3), ("v0", F3), ("v1", F3), ("v2", F3)]
+                ("rotation_deg", F3), ("v0", F3), ("v1", F3), ("v2", F3), ("sdf_type", C.c_int32),
+                ("sdf_params", C.c_float * 4), ("sdf_volume", C.c_int32)]
 
 
 class ArMedium(C.Structure):
@@ -91,6 +95,7 @@ EXPORTED = [
     "ar_scene_set_textures", "ar_scene_set_mesh_uv", "ar_scene_update_texels", "ar_scene_texel_count", "ar_adjoint",
     "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats", "ar_scene_set_sdf_union", "ar_scene_set_medium",
     "ar_adjoint_medium", "ar_tonemap", "ar_denoise", "ar_denoise_read", "ar_denoise_write",
+    "ar_sdf_volume_add", "ar_sdf_volume_add_data", "ar_sdf_volume_read", "ar_sdf_volume_clear",
 ]
 
 _lib = None
@@ -153,6 +158,10 @@ def load() -> C.CDLL:
         "ar_denoise": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, vp]),
         "ar_denoise_read": (C.c_int, [vp, P(C.c_int32), P(C.c_int32), vp, vp]),
         "ar_denoise_write": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp]),
+        "ar_sdf_volume_add": (C.c_int, [vp, C.c_int32, vp, vp, P(C.c_int32)]),
+        "ar_sdf_volume_add_data": (C.c_int, [vp, vp, vp, P(C.c_int32)]),
+        "ar_sdf_volume_read": (C.c_int, [vp, C.c_int32, vp, vp]),
+        "ar_sdf_volume_clear": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -88,10 +88,11 @@ struct GuideSamples
 struct DevScene
 {
     TravScene trav;
+    TravScene sdf_trav;        // the SDF objects' own BVH (node_count 0: none)
     const Material* materials;
     const int* prim_material;  // per primitive id
     const int* prim_light;     // per primitive id, -1 when not a light
-    const int* prim_slot;      // per primitive id: its slot in the BVH leaf array
+    const int* prim_slot;      // per primitive id: its slot in the BVH leaf array (SDF objects: in sdf_trav)
     const Light* lights;
     int light_count;
     const float* lut_rgb;      // RES^3 x 4
@@ -149,6 +150,7 @@ struct PathState
     float4* prev;       // xyz last vertex, w = last BSDF pdf
     float* hit_t;
     int* hit_slot;
+    float4* hit_nrm;    // normal of SDF hits (computed by k_extend), xyz
     float* out_xyz;     // 3 per path
     int capacity;
     // guided rendering only: RGB probe query and the per-vertex radiance
@@ -175,6 +177,7 @@ struct ShadowQueue
     float4* d;      // xyz direction, w = contribution if unoccluded
     float* v_occ;   // contribution if occluded
     uint8_t* valid_unocc;
+    float* sdf_eps; // SDF objects' march tolerance at the shading vertex's depth
 };
 
 struct RenderLaunch
@@ -205,6 +208,19 @@ struct Ctx
     std::vector<int> object_material;
     std::vector<int> object_type;
     std::vector<float> object_tri;       // 9 per object (triangles)
+    std::vector<float4> object_sdf;      // SDF objects: field parameters (one per object)
+    // SDF volume cache (persists across scene builds, like the reference's SDFCacheManager)
+    std::vector<std::vector<float>> vol_host;   // host copies (overlap tests, reads)
+    std::vector<int> vol_dims;                  // 3 per volume
+    std::vector<float*> vol_dev;                // device grids
+    SdfVolume* d_vols = nullptr;                // device table
+    float4* d_sdf_params = nullptr;
+    int sdf_object_count = 0;                   // SDF objects in the scene
+    int* d_pend_list = nullptr;                 // shadow rays left for the SDF pass
+    // the SDF objects' BVH
+    arbvh::WideBVH sdf_bvh;
+    void* d_sdf_nodes = nullptr;
+    void* d_sdf_bvh_slots = nullptr;
     std::vector<float> mesh_v;           // 9 per mesh triangle
     std::vector<int> mesh_material;
     // built scene
@@ -340,8 +356,9 @@ struct WaveBuffers
     PathState ps;
     ShadowQueue sq;
     int* queue[2];
-    int* counters;   // 3 ints
+    int* counters;   // AR_CNT_COUNT ints
     double* accum;   // 3 doubles per pixel
+    int* pend_list;  // shadow rays left for the SDF pass
     cudaStream_t stream;
 };
 cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb, int device, const RenderLaunch& rl,
@@ -368,4 +385,6 @@ cudaError_t ensure_denoise(Ctx& c, int width, int height, int first_frame);
 // v[i] *= inv for n doubles on stream s
 cudaError_t launch_scale_means(double* v, long long n, double inv, cudaStream_t s);
 void free_denoise(Ctx& c);
+// SDF volume cache (sdfvol.cu)
+void free_volumes(Ctx& c);
 } // namespace ar

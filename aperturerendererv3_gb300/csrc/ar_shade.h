@@ -7,6 +7,7 @@
 
 #define AR_OBJ_CUBE 0
 #define AR_OBJ_SPHERE 1
+#define AR_OBJ_SDF 2
 #define AR_OBJ_TRIANGLE 3
 
 #define AR_MAT_DIFFUSE 0

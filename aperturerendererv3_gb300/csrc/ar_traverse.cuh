@@ -14,6 +14,7 @@
 #include "ar_bvh.h"
 #include "ar_geom.h"
 #include "ar_sdf.h"
+#include "ar_sdf_obj.h"
 #include "ar_shade.h"
 
 #define AR_TRAV_STACK 40
@@ -26,6 +27,9 @@ struct TravScene
     const uint4* __restrict__ nodes;       // 5 uint4 per node
     const float4* __restrict__ slots;      // 3 float4 per primitive slot
     const Object* __restrict__ objects;    // analytic object table, indexed by primitive id
+    const float4* __restrict__ sdf_params; // SDF objects: field parameters, indexed by primitive id
+    const SdfVolume* __restrict__ sdf_vols;  // the SDF volume cache
+    int sdf_vol_count;
     int node_count;
     SdfUnion sdf;                          // the smooth-union SDF object (count 0: none); not in the BVH
     int sdf_id;                            // its primitive id
@@ -70,8 +74,24 @@ AR_HD uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, int s)
     return (w >> (8 * (s & 3))) & 0xffu;
 }
 
+// the field of SDF object `id` (Object.pad: kind, volume index)
+AR_HD SdfObjField sdf_obj_field(const TravScene& sc, const Object& ob, int id)
+{
+    SdfObjField f;
+    f.kind = ob.pad[0];
+    f.prm = sc.sdf_params[id];
+    const int vi = ob.pad[1];
+    f.vol = (f.kind == AR_SDF_OBJ_VOLUME && vi >= 0 && vi < sc.sdf_vol_count) ? &sc.sdf_vols[vi] : nullptr;
+    return f;
+}
+
 // Intersects one primitive slot; returns t (or -1 on miss) and the id.
-AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3 d, int* id_out, float tmin = 0.0f)
+// Sdf: the slot may hold an SDF object (the SDF objects' own BVH), marched
+// with tolerance sdf_eps (SDF_EPS of the ray's depth); the main BVH holds no
+// SDF objects, so its traversal is compiled without the march.
+template <bool Sdf = false>
+AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3 d, int* id_out, float tmin,
+                     float sdf_eps = 0.0f)
 {
     const float4 a = AR_LDG(&sc.slots[3 * (size_t)slot + 0]);
     const uint32_t tag = AR_F2U(a.w);
@@ -88,6 +108,11 @@ AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3
     }
     (void)tmin;
     const Object ob = sc.objects[id];
+    if (kind == AR_PRIM_KIND_SDF)
+    {
+        if (!Sdf) return -1.0f;
+        return sdf_obj_hit(sdf_obj_field(sc, ob, id), ob.center, ob.extent, ob.w2o, o, d, sdf_eps, nullptr);
+    }
     Hit h;
     h.hit = false;
     const bool ok = (kind == AR_PRIM_KIND_BOX) ? intersect_box(o, d, ob, &h, false) : intersect_sphere(o, d, ob, &h, false);
@@ -105,7 +130,7 @@ AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3
 // many rays per lane (refilling lanes whose ray finished); traverse() runs one
 // ray to completion.  Either way a ray performs the same operations in the
 // same order.
-template <bool AnyHit>
+template <bool AnyHit, bool Sdf = false>
 struct TravState
 {
     V3 o, d, inv;
@@ -116,6 +141,7 @@ struct TravState
     int node;
     int sp;
     uint32_t n_visits, n_tests;
+    float sdf_eps;                 // Sdf: march tolerance of SDF objects
     uint2 stack[AR_TRAV_STACK];
 
     AR_HD void init(const TravScene& sc, V3 o_, V3 d_, float tmin_, float tmax_)
@@ -134,6 +160,15 @@ struct TravState
         node = sc.node_count > 0 ? 0 : -2;  // -2: nothing to traverse
         n_visits = 0;
         n_tests = 0;
+        sdf_eps = 0.0f;
+    }
+
+    // continues from a result found elsewhere (the main BVH's hit for the SDF
+    // objects' BVH): closer hits or equal t with a smaller id replace it
+    AR_HD void start_from(TravResult r, float sdf_eps_)
+    {
+        res = r;
+        sdf_eps = sdf_eps_;
     }
 
     AR_HD TravResult result() const
@@ -198,7 +233,7 @@ struct TravState
                 {
                     int id;
                     ++n_tests;
-                    const float t = prim_hit(sc, first + k, sh, o, d, &id, tmin);
+                    const float t = prim_hit<Sdf>(sc, first + k, sh, o, d, &id, tmin, sdf_eps);
                     if (!(t >= tmin)) continue;  // also rejects misses (-1)
                     if (AnyHit)
                     {
@@ -250,6 +285,28 @@ struct TravState
         return true;
     }
 };
+
+// Slots of hits outside the main BVH (PathState::hit_slot)
+#define AR_SLOT_SOLO (-3)          // a ray inside an SDF object, resolved by the SDF pass
+#define AR_SLOT_SDFOBJ_BASE (-4)   // SDF object hit: AR_SLOT_SDFOBJ_BASE - (slot in the SDF objects' BVH)
+
+// The SDF objects' BVH from a result found in the main BVH: closest hit
+// (equal t: the smaller id wins, as in one traversal over both) or any hit.
+// Returns the raw result: a different id than `start` means an SDF object won,
+// and res.slot then indexes this BVH's slots.  Out of line: the march lives here.
+template <bool AnyHit>
+AR_SDFOBJ_CALL TravResult sdf_bvh_trace(const TravScene sc, V3 o, V3 d, float tmin, float tmax, float sdf_eps,
+                                        TravResult start)
+{
+    if (sc.node_count <= 0) return start;
+    TravState<AnyHit, true> st;
+    st.init(sc, o, d, tmin, tmax);
+    st.start_from(start, sdf_eps);
+    while (st.step(sc, nullptr))
+    {
+    }
+    return st.res;
+}
 
 template <bool AnyHit>
 AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, float tmax,

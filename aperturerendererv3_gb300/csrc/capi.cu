@@ -32,6 +32,10 @@ DevScene dev_scene(const Ctx& c)
     s.trav.nodes = reinterpret_cast<const uint4*>(c.d_nodes);
     s.trav.slots = reinterpret_cast<const float4*>(c.d_slots);
     s.trav.objects = c.d_objects;
+    s.trav.sdf_params = c.d_sdf_params;
+    s.trav.sdf_vols = c.d_vols;
+    s.trav.sdf_vol_count = (int)c.vol_dev.size();
+
     s.trav.node_count = (int)c.bvh.nodes.size();
     s.materials = c.d_materials;
     s.prim_material = c.d_prim_material;
@@ -48,6 +52,10 @@ DevScene dev_scene(const Ctx& c)
     s.guide = c.guide;
     s.trav.sdf = c.sdf;
     s.trav.sdf_id = c.sdf_id;
+    s.sdf_trav = s.trav;
+    s.sdf_trav.nodes = reinterpret_cast<const uint4*>(c.d_sdf_nodes);
+    s.sdf_trav.slots = reinterpret_cast<const float4*>(c.d_sdf_bvh_slots);
+    s.sdf_trav.node_count = c.d_sdf_nodes ? (int)c.sdf_bvh.nodes.size() : 0;
     s.medium = c.medium;
     s.texels = c.d_texels;
     s.tex_info = c.d_tex_info;
@@ -100,6 +108,10 @@ void free_scene(Ctx& c)
     free_dev(c.d_tex_info);
     free_dev(c.d_prim_uv);
     free_dev(c.d_sdf);
+    free_dev(c.d_sdf_params);
+    free_dev(c.d_sdf_nodes);
+    free_dev(c.d_sdf_bvh_slots);
+    c.sdf_object_count = 0;
     c.sdf = SdfUnion{};
     c.tex_count = 0;
     c.texel_floats = 0;
@@ -111,8 +123,8 @@ void free_waves(Ctx& c)
     PathState& p = c.ps;
     free_dev(p.rng); free_dev(p.pixel); free_dev(p.frame); free_dev(p.ray_o); free_dev(p.ray_d);
     free_dev(p.radiance); free_dev(p.mask); free_dev(p.depths); free_dev(p.flags); free_dev(p.media_v);
-    free_dev(p.media_depth); free_dev(p.prev); free_dev(p.hit_t); free_dev(p.hit_slot); free_dev(p.out_xyz);
-    free_dev(c.sq.path); free_dev(c.sq.o); free_dev(c.sq.d); free_dev(c.sq.v_occ); free_dev(c.sq.valid_unocc);
+    free_dev(p.media_depth); free_dev(p.prev); free_dev(p.hit_t); free_dev(p.hit_slot); free_dev(p.hit_nrm); free_dev(c.d_pend_list); free_dev(p.out_xyz);
+    free_dev(c.sq.path); free_dev(c.sq.o); free_dev(c.sq.d); free_dev(c.sq.v_occ); free_dev(c.sq.valid_unocc); free_dev(c.sq.sdf_eps);
     free_dev(c.d_queue[0]);
     free_dev(c.d_queue[1]);
     c.wave_capacity = 0;
@@ -146,12 +158,15 @@ ar_status ensure_waves(ar_ctx* ctx, int cap)
     AR_CUDA(ctx, alloc_dev(p.prev, n));
     AR_CUDA(ctx, alloc_dev(p.hit_t, n));
     AR_CUDA(ctx, alloc_dev(p.hit_slot, n));
+    AR_CUDA(ctx, alloc_dev(p.hit_nrm, n));
+    AR_CUDA(ctx, alloc_dev(c.d_pend_list, n));
     AR_CUDA(ctx, alloc_dev(p.out_xyz, 3 * n));
     AR_CUDA(ctx, alloc_dev(c.sq.path, n));
     AR_CUDA(ctx, alloc_dev(c.sq.o, n));
     AR_CUDA(ctx, alloc_dev(c.sq.d, n));
     AR_CUDA(ctx, alloc_dev(c.sq.v_occ, n));
     AR_CUDA(ctx, alloc_dev(c.sq.valid_unocc, n));
+    AR_CUDA(ctx, alloc_dev(c.sq.sdf_eps, n));
     AR_CUDA(ctx, alloc_dev(c.d_queue[0], n));
     AR_CUDA(ctx, alloc_dev(c.d_queue[1], n));
     p.capacity = cap;
@@ -459,7 +474,7 @@ float luminance(V3 c) { return dot(c, v3(0.2126f, 0.7152f, 0.0722f)); }
 // SceneObject::GetArea (core/render/object.cuh:240-255)
 float object_area(const Object& o)
 {
-    if (o.type == AR_OBJ_CUBE)
+    if (o.type == AR_OBJ_CUBE || o.type == AR_OBJECT_SDF)  // SceneObject::GetArea (core/render/object.cuh:249-263)
     {
         const float ex = fabsf(o.extent.x), ey = fabsf(o.extent.y), ez = fabsf(o.extent.z);
         return 8.0f * (ex * ey + ex * ez + ey * ez);
@@ -477,7 +492,7 @@ float object_area(const Object& o)
 void object_bounds(const Object& o, float lo[3], float hi[3])
 {
     V3 half;
-    if (o.type == AR_OBJ_CUBE)
+    if (o.type == AR_OBJ_CUBE || o.type == AR_OBJECT_SDF)  // SceneObject::UpdateProxy (core/render/object.cuh:272-289)
     {
         const V3 ax = mul(o.o2w, v3(1, 0, 0)), ay = mul(o.o2w, v3(0, 1, 0)), az = mul(o.o2w, v3(0, 0, 1));
         half.x = fabsf(ax.x) * o.extent.x + fabsf(ay.x) * o.extent.y + fabsf(az.x) * o.extent.z;
@@ -513,6 +528,32 @@ bool cuda_device_ok(int device, std::string* why)
 // Validates the render parameters and fills the launch description; resets
 // the per-render profile state and decides whether the camera starts inside
 // an object (intersection::Overlap, core/render/intersection.cuh:312-327).
+// intersection::Overlap for one object (core/render/intersection.cuh:312-327);
+// SDF objects evaluate their field on the host copy of the volume cache
+// (OverlapSDFObject, core/object/sdf/sdf_base.cuh:165-176)
+bool overlap_any(const Ctx& c, V3 p, int i)
+{
+    const Object& ob = c.objects[i];
+    if (ob.type != AR_OBJECT_SDF) return overlap_object(p, ob);
+    SdfObjField f;
+    f.kind = ob.pad[0];
+    f.prm = c.object_sdf[i];
+    f.vol = nullptr;
+    SdfVolume hv{};
+    const int vi = ob.pad[1];
+    if (f.kind == AR_SDF_OBJ_VOLUME && vi >= 0 && vi < (int)c.vol_host.size())
+    {
+        hv.data = c.vol_host[vi].data();
+        hv.dx = c.vol_dims[3 * vi];
+        hv.dy = c.vol_dims[3 * vi + 1];
+        hv.dz = c.vol_dims[3 * vi + 2];
+        hv.voxel_size_max = sdf_volume_voxel_size_max(hv.dx, hv.dy, hv.dz);
+        f.vol = &hv;
+    }
+    const V3 lp = mul(ob.w2o, p - ob.center);
+    return sdf_obj_eval(f, sdf_to_unit(lp, ob.extent)) <= 0.0f;
+}
+
 ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch& rl)
 {
     Ctx& c = ctx->c;
@@ -552,7 +593,7 @@ ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch&
     {
         const V3 co = v3(rl.cam_o[0], rl.cam_o[1], rl.cam_o[2]);
         for (size_t i = 0; i < c.objects.size(); ++i)
-            if (c.object_type[i] != AR_OBJECT_TRIANGLE && overlap_object(co, c.objects[i]))
+            if (c.object_type[i] != AR_OBJECT_TRIANGLE && overlap_any(c, co, (int)i))
             {
                 c.camera_inside = 1;
                 break;
@@ -565,7 +606,7 @@ ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch&
 
 extern "C" {
 
-int ar_abi_version(void) { return 3; }
+int ar_abi_version(void) { return 4; }
 
 ar_status ar_create(ar_ctx** out, int device)
 {
@@ -614,6 +655,7 @@ ar_status ar_destroy(ar_ctx* ctx)
     free_guide(c);
     free_mlp(c);
     free_denoise(c);
+    free_volumes(c);
     free_waves(c);
     free_dev(c.d_lut_rgb);
     free_dev(c.d_lut_lambda);
@@ -653,14 +695,24 @@ ar_status ar_scene_set_objects(ar_ctx* ctx, const ar_object* o, int n)
     c.object_material.resize(n);
     c.object_type.resize(n);
     c.object_tri.assign((size_t)n * 9, 0.0f);
+    c.object_sdf.assign((size_t)n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (int i = 0; i < n; ++i)
     {
         const ar_object& s = o[i];
-        if (s.type != AR_OBJECT_CUBE && s.type != AR_OBJECT_SPHERE && s.type != AR_OBJECT_TRIANGLE)
+        if (s.type != AR_OBJECT_CUBE && s.type != AR_OBJECT_SPHERE && s.type != AR_OBJECT_TRIANGLE &&
+            s.type != AR_OBJECT_SDF)
             return fail(ctx, AR_ERR_INVALID, "objects: unsupported type " + std::to_string(s.type));
+        if (s.type == AR_OBJECT_SDF && s.sdf_type != AR_SDF_OBJECT_TORUS && s.sdf_type != AR_SDF_OBJECT_VOLUME)
+            return fail(ctx, AR_ERR_INVALID, "objects: SDF objects are a torus or a cached volume");
         Object& ob = c.objects[i];
         std::memset(&ob, 0, sizeof(ob));
         ob.type = s.type;
+        if (s.type == AR_OBJECT_SDF)
+        {
+            ob.pad[0] = s.sdf_type;
+            ob.pad[1] = s.sdf_volume;
+        }
+        c.object_sdf[i] = make_float4(s.sdf_params[0], s.sdf_params[1], s.sdf_params[2], s.sdf_params[3]);
         ob.center = v3(s.center[0], s.center[1], s.center[2]);
         ob.extent = v3(fabsf(s.extent[0]), fabsf(s.extent[1]), fabsf(s.extent[2]));
         object_frame(v3(s.rotation_deg[0], s.rotation_deg[1], s.rotation_deg[2]), &ob.o2w, &ob.w2o);
@@ -863,7 +915,9 @@ ar_status ar_scene_build(ar_ctx* ctx)
             if (c.object_type[i] == AR_OBJECT_TRIANGLE) tv = &c.object_tri[9 * (size_t)i];
             else
             {
-                p.kind = c.object_type[i] == AR_OBJECT_CUBE ? AR_PRIM_KIND_BOX : AR_PRIM_KIND_SPHERE;
+                p.kind = c.object_type[i] == AR_OBJECT_CUBE   ? AR_PRIM_KIND_BOX
+                         : c.object_type[i] == AR_OBJECT_SDF ? AR_PRIM_KIND_SDF
+                                                             : AR_PRIM_KIND_SPHERE;
                 object_bounds(c.objects[i], p.lo, p.hi);
             }
         }
@@ -883,16 +937,34 @@ ar_status ar_scene_build(ar_ctx* ctx)
             }
         }
     }
+    // SDF objects get their own BVH, traversed in a separate pass, so the main
+    // traversal carries no SDF code
+    std::vector<arbvh::PrimInput> sdf_prims;
+    {
+        size_t w = 0;
+        for (size_t i = 0; i < prims.size(); ++i)
+        {
+            if (prims[i].kind == AR_PRIM_KIND_SDF) sdf_prims.push_back(prims[i]);
+            else prims[w++] = prims[i];
+        }
+        prims.resize(w);
+    }
+    const int n_sdf_objects = (int)sdf_prims.size();
     std::string err;
     if (!arbvh::build_wide_bvh(prims, c.bvh, &err)) return fail(ctx, AR_ERR_INVALID, "BVH build: " + err);
     if (c.bvh.depth >= AR_TRAV_STACK) return fail(ctx, AR_ERR_INVALID, "BVH deeper than the traversal stack");
+    c.sdf_bvh = arbvh::WideBVH{};
+    if (!sdf_prims.empty() && !arbvh::build_wide_bvh(sdf_prims, c.sdf_bvh, &err))
+        return fail(ctx, AR_ERR_INVALID, "SDF object BVH build: " + err);
+    if (c.sdf_bvh.depth >= AR_TRAV_STACK) return fail(ctx, AR_ERR_INVALID, "SDF object BVH deeper than the traversal stack");
     std::vector<int> prim_slot((size_t)nprim, -1);
-    for (size_t s = 0; s < c.bvh.slots.size(); ++s)
-    {
-        uint32_t tag;
-        std::memcpy(&tag, &c.bvh.slots[s].a[3], 4);
-        prim_slot[tag & AR_PRIM_ID_MASK] = (int)s;
-    }
+    for (const arbvh::WideBVH* b : {&c.bvh, &c.sdf_bvh})
+        for (size_t s = 0; s < b->slots.size(); ++s)
+        {
+            uint32_t tag;
+            std::memcpy(&tag, &b->slots[s].a[3], 4);
+            prim_slot[tag & AR_PRIM_ID_MASK] = (int)s;  // SDF objects: a slot of the SDF objects' BVH
+        }
 
     // light table (core/scene.cu:677-706): every primitive with a light material
     c.lights.clear();
@@ -925,6 +997,7 @@ ar_status ar_scene_build(ar_ctx* ctx)
     free_scene(c);
     free_guide(c);
     free_mlp(c);
+    c.sdf_object_count = n_sdf_objects;
     std::vector<Object> objs(c.objects);
     if (objs.empty()) objs.resize(1);
     AR_CUDA(ctx, alloc_dev(c.d_nodes, c.bvh.nodes.size() * sizeof(ar_wide_node)));
@@ -933,6 +1006,21 @@ ar_status ar_scene_build(ar_ctx* ctx)
     AR_CUDA(ctx, cudaMemcpy(c.d_slots, c.bvh.slots.data(), c.bvh.slots.size() * sizeof(ar_prim_slot), cudaMemcpyHostToDevice));
     AR_CUDA(ctx, alloc_dev(c.d_objects, objs.size()));
     AR_CUDA(ctx, cudaMemcpy(c.d_objects, objs.data(), objs.size() * sizeof(Object), cudaMemcpyHostToDevice));
+    {
+        std::vector<float4> sp(c.object_sdf);
+        if (sp.empty()) sp.resize(1);
+        AR_CUDA(ctx, alloc_dev(c.d_sdf_params, sp.size()));
+        AR_CUDA(ctx, cudaMemcpy(c.d_sdf_params, sp.data(), sp.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    if (!c.sdf_bvh.nodes.empty())
+    {
+        AR_CUDA(ctx, alloc_dev(c.d_sdf_nodes, c.sdf_bvh.nodes.size() * sizeof(ar_wide_node)));
+        AR_CUDA(ctx, cudaMemcpy(c.d_sdf_nodes, c.sdf_bvh.nodes.data(), c.sdf_bvh.nodes.size() * sizeof(ar_wide_node),
+                                cudaMemcpyHostToDevice));
+        AR_CUDA(ctx, alloc_dev(c.d_sdf_bvh_slots, c.sdf_bvh.slots.size() * sizeof(ar_prim_slot)));
+        AR_CUDA(ctx, cudaMemcpy(c.d_sdf_bvh_slots, c.sdf_bvh.slots.data(), c.sdf_bvh.slots.size() * sizeof(ar_prim_slot),
+                                cudaMemcpyHostToDevice));
+    }
     AR_CUDA(ctx, alloc_dev(c.d_prim_material, (size_t)nprim));
     AR_CUDA(ctx, cudaMemcpy(c.d_prim_material, prim_material.data(), nprim * sizeof(int), cudaMemcpyHostToDevice));
     AR_CUDA(ctx, alloc_dev(c.d_prim_light, (size_t)nprim));
@@ -1361,6 +1449,9 @@ ar_status ar_host_trace_closest(const float* tris, int ntri, const float* rays, 
     sc.nodes = reinterpret_cast<const uint4*>(bvh.nodes.data());
     sc.slots = reinterpret_cast<const float4*>(bvh.slots.data());
     sc.objects = nullptr;
+    sc.sdf_params = nullptr;
+    sc.sdf_vols = nullptr;
+    sc.sdf_vol_count = 0;
     sc.node_count = (int)bvh.nodes.size();
     sc.sdf = SdfUnion{};
     sc.sdf_id = -1;

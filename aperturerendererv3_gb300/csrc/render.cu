@@ -89,8 +89,10 @@ cudaError_t launch_prepare_materials(Material* mats, int n, const float* lut, cu
 }
 
 // ---------------------------------------------------------------- hit reconstruction
-// Full hit record for primitive slot `slot` at distance t (the traversal's t).
-__device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, V3 d, float t, Hit* h)
+// Full hit record for primitive slot `slot` at distance t (the traversal's t);
+// SDF hits (the union and SDF objects) take the normal k_extend stored in *sdf_nrm.
+__device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, V3 d, float t, Hit* h,
+                                            const float4* sdf_nrm)
 {
     if (slot == AR_SLOT_SDF)
     {
@@ -100,11 +102,14 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
         h->light = sc.prim_light[id];
         h->dist = t;
         h->pos = o + d * t;
-        h->nrm = sdf_normal(sc.trav.sdf, h->pos, 1.0e-4f);
+        const float4 n = *sdf_nrm;
+        h->nrm = v3(n.x, n.y, n.z);
         h->local_pos = h->pos;
         return;
     }
-    const float4 a = __ldg(&sc.trav.slots[3 * (size_t)slot + 0]);
+    const bool sdf_obj = slot <= AR_SLOT_SDFOBJ_BASE;
+    const float4 a = sdf_obj ? __ldg(&sc.sdf_trav.slots[3 * (size_t)(AR_SLOT_SDFOBJ_BASE - slot)])
+                             : __ldg(&sc.trav.slots[3 * (size_t)slot + 0]);
     const uint32_t tag = __float_as_uint(a.w);
     const uint32_t kind = tag >> AR_PRIM_KIND_SHIFT;
     const int id = (int)(tag & AR_PRIM_ID_MASK);
@@ -118,6 +123,18 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
         const float4 c = __ldg(&sc.trav.slots[3 * (size_t)slot + 2]);
         tri_frame(o, d, t, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &h->pos, &h->nrm);
         h->local_pos = v3(0.0f, 0.0f, 0.0f);
+    }
+    else if (kind == AR_PRIM_KIND_SDF)
+    {
+        // IntersectSDFObject's hit frame (core/object/sdf/sdf_base.cuh:140-151); slot is in sdf_trav
+        const Object ob = sc.trav.objects[id];
+        const V3 lo = mul(ob.w2o, o - ob.center);
+        const V3 ld = normalize(mul(ob.w2o, d));
+        const V3 lp = lo + ld * t;
+        h->pos = mul(ob.o2w, lp) + ob.center;
+        const float4 n = *sdf_nrm;
+        h->nrm = v3(n.x, n.y, n.z);
+        h->local_pos = lp;
     }
     else
     {
@@ -166,6 +183,7 @@ __device__ __forceinline__ int albedo_texel(const DevScene& sc, int tex, int slo
 #define AR_CNT_SHADOW 2
 #define AR_CNT_MLP 3
 #define AR_CNT_FETCH 4       // k_extend, k_shadow fetch counters
+#define AR_CNT_PEND 6        // pending SDF work of k_extend, k_shadow
 
 // ---------------------------------------------------------------- raygen
 struct CamParams
@@ -252,31 +270,103 @@ __device__ __forceinline__ bool warp_refill(int* fetch, int n, bool active, bool
     return *q < n;
 }
 
-// closest hit of a finished traversal: the SDF object is marched up to the
-// BVH hit (it has the largest primitive id: a BVH hit at equal t wins)
-__device__ __forceinline__ void extend_finish(const DevScene& sc, const PathState& ps, int p,
-                                              const TravState<false>& st)
+// Shadow rays the traversal left unoccluded, for k_sdf_shadow (list ==
+// nullptr when the scene has no SDF geometry).
+struct SdfPending
+{
+    int* list;
+    int* count;
+};
+
+// closest hit of a finished traversal of the main BVH
+__device__ __forceinline__ void extend_finish(const DevScene& sc, const PathState& ps, int p, const TravState<false>& st)
 {
     const TravResult r = st.result();
-    float t = r.t;
-    int slot = r.slot;
-    if (sc.trav.sdf.count > 0)
-    {
-        const float ts = sdf_march(sc.trav.sdf, st.o, st.d, sdf_eps(st.tmin), slot < 0 ? 3.0e38f : t);
-        if (ts >= st.tmin && (slot < 0 || ts < t))
-        {
-            t = ts;
-            slot = AR_SLOT_SDF;
-        }
-    }
     if (sc.stats)
     {
         atomicAdd(&sc.stats[0], (unsigned long long)st.n_visits);
         atomicAdd(&sc.stats[1], (unsigned long long)st.n_tests);
         atomicAdd(&sc.stats[4], 1ull);
     }
-    ps.hit_t[p] = t;
-    ps.hit_slot[p] = slot;
+    ps.hit_t[p] = r.t;
+    ps.hit_slot[p] = r.slot;
+}
+
+// The SDF pass of the closest hits (scenes with SDF geometry only): the SDF
+// objects' BVH from the main BVH's hit, then the smooth union (marched up to
+// the hit so far; it has the largest primitive id, so a hit at equal t wins),
+// and the normal of an SDF hit (central differences of the field), which
+// k_shade reads from hit_nrm.  Rays inside an SDF object test only it.
+__global__ void __launch_bounds__(AR_BLOCK) k_sdf_extend(DevScene sc, PathState ps, const int* __restrict__ queue,
+                                                       const int* __restrict__ counter)
+{
+    const int n = *counter;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    {
+        const int p = queue[q];
+        const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
+        const V3 o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
+        const float tmin = intersect_eps((int)(ps.depths[p] >> 16));
+        const float seps = 0.5f * fmaxf(tmin, 1.0e-3f);
+        int slot = ps.hit_slot[p];
+        float t = ps.hit_t[p];
+        int sdf_obj_slot = -1;  // slot in the SDF objects' BVH of an SDF object hit
+        if (slot == AR_SLOT_SOLO)
+        {
+            const int s = sc.prim_slot[__float_as_int(ps.media_v[p].w)];
+            int id;
+            const float th = prim_hit<true>(sc.sdf_trav, s, make_shear(d), o, d, &id, tmin, seps);
+            slot = -1;
+            t = 0.0f;
+            if (th >= tmin)
+            {
+                sdf_obj_slot = s;
+                t = th;
+            }
+        }
+        else
+        {
+            TravResult r;
+            r.slot = slot;
+            r.t = slot >= 0 ? t : __int_as_float(0x7f800000);
+            r.id = slot >= 0 ? (int)(__float_as_uint(sc.trav.slots[3 * (size_t)slot].w) & AR_PRIM_ID_MASK) : -1;
+            const TravResult r2 = sdf_bvh_trace<false>(sc.sdf_trav, o, d, tmin, __int_as_float(0x7f800000), seps, r);
+            if (r2.id != r.id)
+            {
+                sdf_obj_slot = r2.slot;
+                slot = -1;
+                t = r2.t;
+            }
+            const bool any = slot >= 0 || sdf_obj_slot >= 0;
+            if (sc.trav.sdf.count > 0)
+            {
+                const float ts = sdf_march(sc.trav.sdf, o, d, sdf_eps(tmin), any ? t : 3.0e38f);
+                if (ts >= tmin && (!any || ts < t))
+                {
+                    t = ts;
+                    slot = AR_SLOT_SDF;
+                    sdf_obj_slot = -1;
+                }
+            }
+        }
+        if (slot == AR_SLOT_SDF)
+        {
+            const V3 nn = sdf_normal(sc.trav.sdf, o + d * t, 1.0e-4f);
+            ps.hit_nrm[p] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+        }
+        else if (sdf_obj_slot >= 0)
+        {
+            const int id = (int)(__float_as_uint(sc.sdf_trav.slots[3 * (size_t)sdf_obj_slot].w) & AR_PRIM_ID_MASK);
+            const Object ob = sc.trav.objects[id];
+            const V3 lo = mul(ob.w2o, o - ob.center);
+            const V3 ld = normalize(mul(ob.w2o, d));
+            const V3 nn = sdf_obj_normal(sdf_obj_field(sc.trav, ob, id), ob.extent, ob.o2w, lo + ld * t, seps);
+            ps.hit_nrm[p] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+            slot = AR_SLOT_SDFOBJ_BASE - sdf_obj_slot;
+        }
+        ps.hit_t[p] = t;
+        ps.hit_slot[p] = slot;
+    }
 }
 
 __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScene sc, PathState ps, const int* __restrict__ queue,
@@ -298,12 +388,21 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
             const int mobj = __float_as_int(ps.media_v[p].w);
             if ((ps.flags[p] & 1u) && mobj >= 0)
             {
-                // inside a medium: intersect only the enclosing object (render.cuh:89-92)
-                const int s = sc.prim_slot[mobj];
-                int id;
-                const float th = prim_hit(sc.trav, s, make_shear(d), o, d, &id, tmin);
-                ps.hit_t[p] = th >= tmin ? th : 0.0f;
-                ps.hit_slot[p] = th >= tmin ? s : -1;
+                // inside a medium: intersect only the enclosing object (render.cuh:89-92);
+                // an SDF object is left to the SDF pass
+                if (sc.trav.objects[mobj].type == AR_OBJ_SDF)
+                {
+                    ps.hit_t[p] = 0.0f;
+                    ps.hit_slot[p] = AR_SLOT_SOLO;
+                }
+                else
+                {
+                    const int s = sc.prim_slot[mobj];
+                    int id;
+                    const float th = prim_hit<false>(sc.trav, s, make_shear(d), o, d, &id, tmin);
+                    ps.hit_t[p] = th >= tmin ? th : 0.0f;
+                    ps.hit_slot[p] = th >= tmin ? s : -1;
+                }
                 if (sc.stats) atomicAdd(&sc.stats[4], 1ull);
             }
             else
@@ -356,7 +455,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_mlp_query(DevScene sc, PathState p
             {
                 const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
                 Hit h;
-                hit_context(sc, slot, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), ps.hit_t[p], &h);
+                hit_context(sc, slot, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), ps.hit_t[p], &h, &ps.hit_nrm[p]);
                 const V3 wr = reflect(v3(rd.x, rd.y, rd.z), h.nrm);
                 ps.q_pos[p] = make_float4(h.pos.x, h.pos.y, h.pos.z, 1.0f);
                 ps.q_wr[p] = make_float4(wr.x, wr.y, wr.z, 0.0f);
@@ -372,6 +471,9 @@ __global__ void __launch_bounds__(AR_BLOCK) k_mlp_query(DevScene sc, PathState p
 }
 
 // ---------------------------------------------------------------- shade
+#ifndef AR_SHADE_MIN_BLOCKS
+#define AR_SHADE_MIN_BLOCKS 2    // blocks per SM the unguided / voxel-guided shade kernels are compiled for
+#endif
 struct ShadeParams
 {
     int use_nee;
@@ -434,7 +536,7 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
 }
 
 template <int GUIDE, bool ADJ>
-__global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
+__global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? 1 : AR_SHADE_MIN_BLOCKS) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
                                                   const int* __restrict__ counter, int* next_queue, int* next_counter,
                                                   int* shadow_counter, ShadeParams prm)
 {
@@ -452,7 +554,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
         bool shadow = false;
         int p = 0;
         V3 sh_o = v3(0, 0, 0), sh_d = v3(0, 0, 0);
-        float sh_tmax = 0.0f, sh_vun = 0.0f, sh_vocc = 0.0f;
+        float sh_tmax = 0.0f, sh_vun = 0.0f, sh_vocc = 0.0f, sh_sdf_eps = 0.0f;
         bool sh_valid = false;
         if (active)
         {
@@ -490,7 +592,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
             h.pos = v3(0, 0, 0);
             h.nrm = v3(0, 0, 0);
             h.local_pos = v3(0, 0, 0);
-            if (slot != -1) hit_context(sc, slot, rayO, rayD, ps.hit_t[p], &h);
+            if (slot != -1) hit_context(sc, slot, rayO, rayD, ps.hit_t[p], &h, &ps.hit_nrm[p]);
 
             // ---- participating medium: a free flight sampled in the medium box
             // ends the segment early with probability 1 - transmittance
@@ -858,6 +960,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
                                     sh_o = h.pos;
                                     sh_d = dirS;
                                     sh_tmax = tmax;
+                                    sh_sdf_eps = 0.5f * intersect_eps(depth);  // SDF_EPS of the NEE depth
                                     sh_vun = vUn;
                                     sh_vocc = vZero;
                                     sh_valid = validUn;
@@ -930,6 +1033,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
             sq.d[sqi] = make_float4(sh_d.x, sh_d.y, sh_d.z, sh_vun);
             sq.v_occ[sqi] = sh_vocc;
             sq.valid_unocc[sqi] = sh_valid ? 1 : 0;
+            sq.sdf_eps[sqi] = sh_sdf_eps;
         }
     }
     if constexpr (ADJ)
@@ -951,28 +1055,54 @@ __global__ void __launch_bounds__(AR_BLOCK) k_shade(DevScene sc, PathState ps, S
 }
 
 // ---------------------------------------------------------------- shadow
-__device__ __forceinline__ void shadow_finish(const DevScene& sc, const PathState& ps, const ShadowQueue& sq, int i,
-                                              int p, const TravState<true>& st)
+__device__ __forceinline__ void shadow_apply(const PathState& ps, const ShadowQueue& sq, int i, int p, bool occluded)
 {
-    bool occluded = st.result().slot >= 0;
-    if (!occluded && sc.trav.sdf.count > 0)
-    {
-        const float ts = sdf_march(sc.trav.sdf, st.o, st.d, sdf_eps(0.0f), st.tmax);
-        occluded = ts >= 0.0f && ts < st.tmax;
-    }
+    ps.radiance[p] = ps.radiance[p] + (occluded ? sq.v_occ[i] : sq.d[i].w);
+    const bool valid = occluded ? true : (sq.valid_unocc[i] != 0);
+    ps.flags[p] = (ps.flags[p] & ~2u) | (valid ? 2u : 0u);
+}
+
+__device__ __forceinline__ void shadow_finish(const DevScene& sc, const PathState& ps, const ShadowQueue& sq, int i,
+                                              int p, const TravState<true>& st, const SdfPending& pend)
+{
+    const bool occluded = st.result().slot >= 0;
     if (sc.stats)
     {
         atomicAdd(&sc.stats[2], (unsigned long long)st.n_visits);
         atomicAdd(&sc.stats[3], (unsigned long long)st.n_tests);
         atomicAdd(&sc.stats[5], 1ull);
     }
-    ps.radiance[p] = ps.radiance[p] + (occluded ? sq.v_occ[i] : sq.d[i].w);
-    const bool valid = occluded ? true : (sq.valid_unocc[i] != 0);
-    ps.flags[p] = (ps.flags[p] & ~2u) | (valid ? 2u : 0u);
+    if (!occluded && pend.list) pend.list[atomicAdd(pend.count, 1)] = i;
+    else shadow_apply(ps, sq, i, p, occluded);
+}
+
+// the SDF pass of the shadow rays the main BVH left unoccluded
+__global__ void __launch_bounds__(AR_BLOCK) k_sdf_shadow(DevScene sc, PathState ps, ShadowQueue sq, SdfPending pend)
+{
+    const int n = *pend.count;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    {
+        const int i = pend.list[k];
+        const int p = sq.path[i];
+        const float4 o4 = sq.o[i], d4 = sq.d[i];
+        const V3 o = v3(o4.x, o4.y, o4.z), d = v3(d4.x, d4.y, d4.z);
+        const float tmax = o4.w;
+        TravResult r;
+        r.t = tmax;
+        r.slot = -1;
+        r.id = -1;
+        bool occluded = sdf_bvh_trace<true>(sc.sdf_trav, o, d, 0.0f, tmax, sq.sdf_eps[i], r).slot >= 0;
+        if (!occluded && sc.trav.sdf.count > 0)
+        {
+            const float ts = sdf_march(sc.trav.sdf, o, d, sdf_eps(0.0f), tmax);
+            occluded = ts >= 0.0f && ts < tmax;
+        }
+        shadow_apply(ps, sq, i, p, occluded);
+    }
 }
 
 __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_shadow(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ counter,
-                                                   int* fetch, unsigned int* err)
+                                                   int* fetch, SdfPending pend, unsigned int* err)
 {
     const int n = *counter;
     TravState<true> st;
@@ -1000,7 +1130,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_shadow(DevScen
             {
                 if (!st.step(sc.trav, err))
                 {
-                    shadow_finish(sc, ps, sq, i, p, st);
+                    shadow_finish(sc, ps, sq, i, p, st, pend);
                     active = false;
                     break;
                 }
@@ -1185,16 +1315,24 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     net.wbf = c.d_mlp_wbf;
     net.w32 = c.d_mlp_w32;
     net.box = c.mlp_box;
+    // SDF geometry: its work leaves the traversal kernels for k_sdf_extend / k_sdf_shadow
+    const bool has_sdf = c.sdf_object_count > 0 || c.sdf.count > 0;
+    const SdfPending pend_shd{has_sdf ? c.d_pend_list : nullptr, &cnt[AR_CNT_PEND]};
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
         int* qn = &cnt[AR_CNT_Q0 + cur];
         cudaMemsetAsync(&cnt[AR_CNT_Q0 + nxt], 0, sizeof(int), s);
         cudaMemsetAsync(&cnt[AR_CNT_SHADOW], 0, sizeof(int), s);
-        cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, 2 * sizeof(int), s);  // fetch counters of k_extend / k_shadow
+        cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, (has_sdf ? 3 : 2) * sizeof(int), s);  // fetch (+ pending) counters
         {
             StageScope st(c, ST_EXTEND);
             k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, &cnt[AR_CNT_FETCH], c.d_err);
+            if (has_sdf)
+            {
+                k_sdf_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn);
+                ++L;
+            }
         }
         {
             StageScope st(c, ST_SHADE);
@@ -1221,7 +1359,13 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         }
         {
             StageScope st(c, ST_SHADOW);
-            k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], c.d_err);
+            k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd,
+                                                 c.d_err);
+            if (has_sdf)
+            {
+                k_sdf_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pend_shd);
+                ++L;
+            }
         }
         L += 3;
     }
@@ -1266,16 +1410,20 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     prm.grad_medium = nullptr;
     prm.mlp_ready = 0;
     prm.gbuf = nullptr;
+    const bool has_sdf = sc.sdf_trav.node_count > 0 || sc.trav.sdf.count > 0;
+    const SdfPending pend_shd{has_sdf ? wb.pend_list : nullptr, &cnt[AR_CNT_PEND]};
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
         cudaMemsetAsync(&cnt[AR_CNT_Q0 + nxt], 0, sizeof(int), s);
         cudaMemsetAsync(&cnt[AR_CNT_SHADOW], 0, sizeof(int), s);
-        cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, 2 * sizeof(int), s);
+        cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, 3 * sizeof(int), s);
         k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur], &cnt[AR_CNT_FETCH], err);
+        if (has_sdf) k_sdf_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur]);
         k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[AR_CNT_Q0 + cur],
                                                    wb.queue[nxt], &cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], prm);
-        k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], err);
+        k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd, err);
+        if (has_sdf) k_sdf_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, pend_shd);
     }
     k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);
     const long long npix = (long long)rl.width * rl.height;

@@ -8,8 +8,8 @@
 namespace ar
 {
 template <bool AnyHit>
-__global__ void __launch_bounds__(256) k_trace(TravScene sc, const float4* __restrict__ rays, int n, int* __restrict__ out,
-                                             float* __restrict__ tout, unsigned int* err)
+__global__ void __launch_bounds__(256) k_trace(TravScene sc, TravScene sdf_objects, const float4* __restrict__ rays, int n,
+                                             int* __restrict__ out, float* __restrict__ tout, unsigned int* err)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
@@ -17,11 +17,22 @@ __global__ void __launch_bounds__(256) k_trace(TravScene sc, const float4* __res
         const float4 b = __ldg(&rays[2 * (size_t)i + 1]);
         const V3 o = v3(a.x, a.y, a.z), d = v3(b.x, b.y, b.z);
         TravResult r = traverse<AnyHit>(sc, o, d, a.w, b.w, err);
-        if (sc.sdf.count > 0 && (!AnyHit || r.slot < 0))
+        if (sdf_objects.node_count > 0 && (!AnyHit || r.slot < 0))
         {
-            // the SDF object (largest primitive id: a BVH hit at equal t wins)
-            const float ts = sdf_march(sc.sdf, o, d, sdf_eps(a.w), r.slot < 0 ? b.w : r.t);
-            if (ts >= a.w && ts < b.w && (r.slot < 0 || ts < r.t))
+            // SDF objects (their own BVH), marched with half of max(tmin, 1e-3)
+            const TravResult r2 = sdf_bvh_trace<AnyHit>(sdf_objects, o, d, a.w, b.w, 0.5f * fmaxf(a.w, 1.0e-3f), r);
+            if (r2.id != r.id)
+            {
+                r = r2;
+                r.slot = AR_SLOT_SDFOBJ_BASE - r2.slot;
+            }
+        }
+        const bool hit = r.id >= 0;
+        if (sc.sdf.count > 0 && (!AnyHit || !hit))
+        {
+            // the smooth-union SDF object (largest primitive id: a BVH hit at equal t wins)
+            const float ts = sdf_march(sc.sdf, o, d, sdf_eps(a.w), hit ? r.t : b.w);
+            if (ts >= a.w && ts < b.w && (!hit || ts < r.t))
             {
                 r.t = ts;
                 r.slot = AR_SLOT_SDF;
@@ -49,8 +60,8 @@ cudaError_t launch_trace(const DevScene& sc, const float* rays, int n, int any, 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = (int)std::min<long long>((n + 255) / 256, (long long)sms * 16);
     const float4* r4 = reinterpret_cast<const float4*>(rays);
-    if (any) k_trace<true><<<blocks, 256, 0, s>>>(sc.trav, r4, n, prim_id, nullptr, err);
-    else k_trace<false><<<blocks, 256, 0, s>>>(sc.trav, r4, n, prim_id, t, err);
+    if (any) k_trace<true><<<blocks, 256, 0, s>>>(sc.trav, sc.sdf_trav, r4, n, prim_id, nullptr, err);
+    else k_trace<false><<<blocks, 256, 0, s>>>(sc.trav, sc.sdf_trav, r4, n, prim_id, t, err);
     if (launches) *launches += 1;
     return cudaGetLastError();
 }

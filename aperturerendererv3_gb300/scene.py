@@ -23,8 +23,9 @@ from typing import Iterable, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import (GLOBAL_SEED, OBJECT_CUBE, OBJECT_SPHERE, OBJECT_TRIANGLE, SHADING_DIFFUSE, SHADING_GGX,
-                   SHADING_GLASS, SHADING_LIGHT, ArMaterial, ArMedium, ArObject, ArRenderParams, check)
+from ._lib import (GLOBAL_SEED, OBJECT_CUBE, OBJECT_SDF, OBJECT_SPHERE, OBJECT_TRIANGLE, SDF_FN_DIAMOND, SDF_FN_TORUS,
+                   SDF_OBJECT_TORUS, SDF_OBJECT_VOLUME, SHADING_DIFFUSE, SHADING_GGX, SHADING_GLASS, SHADING_LIGHT,
+                   ArMaterial, ArMedium, ArObject, ArRenderParams, check)
 
 Vec3 = Sequence[float]
 
@@ -95,6 +96,33 @@ class Material:
         return Material(SHADING_DIFFUSE, (1.0, 1.0, 1.0), _f3(emissive), texture=int(texture))
 
 
+@dataclass(frozen=True)
+class AdditionalObjectInfo:
+    """Field of an SDF object (AdditionalObjectInfo, core/render/object.cuh:216-225):
+    sdf_type SDF_OBJECT_TORUS (params = (R, r)) or SDF_OBJECT_VOLUME (volume =
+    index into the renderer's SDF volume cache)."""
+    sdf_type: int = SDF_OBJECT_TORUS
+    params: tuple = (0.0, 0.0, 0.0, 0.0)
+    volume: int = -1
+
+
+class sdf:
+    """The reference's SDF helpers (namespace sdf, core/object/sdf/*)."""
+
+    @staticmethod
+    def CreateTorus(scale: float = 1.0, R: float = 0.375, r: float = 0.125) -> AdditionalObjectInfo:
+        return AdditionalObjectInfo(SDF_OBJECT_TORUS, (R * scale, r * scale, 0.0, 0.0))
+
+    @staticmethod
+    def CreateSDFVolume(volumeIndex: int) -> AdditionalObjectInfo:
+        return AdditionalObjectInfo(SDF_OBJECT_VOLUME, (0.0, 0.0, 0.0, 0.0), int(volumeIndex))
+
+    @staticmethod
+    def CreateDiamond(scale: float = 1.0, d: float = 0.94, bias: float = 0.5, tableZ: float = 0.3) -> tuple:
+        """Parameters of the diamond functor for SceneRenderer.AddVolumeToCacheManager."""
+        return (d, bias, tableZ, scale * 0.5)
+
+
 @dataclass
 class SceneObject:
     center: tuple = (0.0, 0.0, 0.0)
@@ -102,6 +130,7 @@ class SceneObject:
     material: Material = field(default_factory=Material)
     rotation: tuple = (0.0, 0.0, 0.0)  # Euler angles in degrees
     type: int = OBJECT_CUBE
+    additionalObjectInfo: AdditionalObjectInfo | None = None  # OBJECT_SDF
     v0: tuple = (0.0, 0.0, 0.0)
     v1: tuple = (0.0, 0.0, 0.0)
     v2: tuple = (0.0, 0.0, 0.0)
@@ -179,6 +208,10 @@ def flatten(objects: Iterable[SceneObject], mesh: TriangleMesh | None = None):
         a.v0[:] = _f3(o.v0)
         a.v1[:] = _f3(o.v1)
         a.v2[:] = _f3(o.v2)
+        info = o.additionalObjectInfo if o.additionalObjectInfo is not None else AdditionalObjectInfo()
+        a.sdf_type = int(info.sdf_type)
+        a.sdf_params[:] = tuple(float(x) for x in info.params)
+        a.sdf_volume = int(info.volume)
     mesh_ids = None
     if mesh is not None:
         remap = np.array([mid(m) for m in mesh.materials], np.int32)
@@ -329,6 +362,47 @@ class SceneRenderer:
         if denoise:
             out = self.denoise(out)
         return (out, ps) if per_sample else out
+
+    # ---- SDF volume cache (core/object/sdf/sdf_cache_manager.cuh) ----------
+    def AddVolumeToCacheManager(self, dims, pMin=(0.0, 0.0, 0.0), pMax=(1.0, 1.0, 1.0), sdfFunctor="diamond",
+                                sdfInfo=None) -> int:
+        """Adds a dims[0] x dims[1] x dims[2] distance grid over the unit cube
+        (SceneRenderer::AddVolumeToCacheManager, core/scene.hpp:120-127; pMin /
+        pMax are unused there too) and returns its cache index for
+        sdf.CreateSDFVolume.  sdfFunctor: "diamond" or "torus" (filled on the
+        GPU from sdfInfo, the functor's four parameters: see sdf.CreateDiamond /
+        the torus's (R, r)), or a Python callable f(u) evaluated on the host on
+        an (N, 3) array of unit positions in [-0.5, 0.5]^3."""
+        d = np.ascontiguousarray([int(x) for x in dims], np.int32)
+        idx = C.c_int32()
+        if callable(sdfFunctor):
+            xs = [np.linspace(0.0, 1.0, n, dtype=np.float32) if n > 1 else np.zeros(1, np.float32) for n in d]
+            zz, yy, xx = np.meshgrid(xs[2], xs[1], xs[0], indexing="ij")
+            u = np.stack([xx, yy, zz], -1).reshape(-1, 3) - np.float32(0.5)
+            vox = np.ascontiguousarray(np.asarray(sdfFunctor(u), np.float32).reshape(-1))
+            if vox.size != int(np.prod(d)):
+                raise ValueError("the functor must return one distance per position")
+            check(self._ctx, self._lib.ar_sdf_volume_add_data(self._ctx, vox.ctypes.data, d.ctypes.data, C.byref(idx)))
+        else:
+            fn = {"diamond": SDF_FN_DIAMOND, "torus": SDF_FN_TORUS}.get(sdfFunctor, sdfFunctor)
+            prm = np.zeros(4, np.float32)
+            if sdfInfo is not None:
+                vals = sdfInfo.params if isinstance(sdfInfo, AdditionalObjectInfo) else sdfInfo
+                prm[: len(vals)] = vals
+            check(self._ctx, self._lib.ar_sdf_volume_add(self._ctx, int(fn), prm.ctypes.data, d.ctypes.data,
+                                                         C.byref(idx)))
+        return idx.value
+
+    def sdf_volume(self, index: int) -> np.ndarray:
+        """A cached volume as a (dz, dy, dx) float32 array."""
+        dims = np.zeros(3, np.int32)
+        check(self._ctx, self._lib.ar_sdf_volume_read(self._ctx, int(index), None, dims.ctypes.data))
+        out = np.zeros((dims[2], dims[1], dims[0]), np.float32)
+        check(self._ctx, self._lib.ar_sdf_volume_read(self._ctx, int(index), out.ctypes.data, None))
+        return out
+
+    def ClearVolumes(self) -> None:
+        check(self._ctx, self._lib.ar_sdf_volume_clear(self._ctx))
 
     # ---- denoiser (core/denoise/*) ----------------------------------------
     def denoise(self, xyz):

@@ -38,7 +38,12 @@ typedef int ar_status;
 /* object kinds (EObjectType, core/render/object.cuh:29-34, plus triangles) */
 #define AR_OBJECT_CUBE 0
 #define AR_OBJECT_SPHERE 1
+#define AR_OBJECT_SDF 2        /* EObjectType::OBJ_SDF: a signed distance field inside an oriented box */
 #define AR_OBJECT_TRIANGLE 3
+
+/* Fields of SDF objects (ESDFType, core/render/object.cuh:36-42) */
+#define AR_SDF_OBJECT_TORUS 0  /* sdf_params = (R, r) in unit coordinates (sdf::CreateTorus: 0.375, 0.125 x scale) */
+#define AR_SDF_OBJECT_VOLUME 1 /* sdf_volume = index into the SDF volume cache */
 
 /* shading models (EShadingModel, core/render/object.cuh:44-51) */
 #define AR_SHADING_DIFFUSE 0
@@ -69,7 +74,13 @@ typedef struct ar_material
 } ar_material;
 
 /* One SceneObject: an oriented box (centre, half extent, Euler rotation in
- * degrees), a sphere (radius = max extent) or a triangle (v0, v1, v2). */
+ * degrees), a sphere (radius = max extent), a triangle (v0, v1, v2), or an SDF
+ * object: the oriented box's inside mapped to the unit cube [-0.5, 0.5]^3,
+ * where the field (sdf_type, sdf_params / sdf_volume; the reference's
+ * AdditionalObjectInfo) is marched as IntersectSDFObject does
+ * (core/object/sdf/sdf_base.cuh:107-163).  SDF objects with a light material
+ * are in the light table but, as in the reference's NEESampleLight, are never
+ * picked for next-event estimation. */
 typedef struct ar_object
 {
     int32_t type;
@@ -78,6 +89,9 @@ typedef struct ar_object
     float extent[3];
     float rotation_deg[3];
     float v0[3], v1[3], v2[3];
+    int32_t sdf_type;        /* AR_OBJECT_SDF: AR_SDF_OBJECT_TORUS or AR_SDF_OBJECT_VOLUME */
+    float sdf_params[4];     /* SDFInfo::sdfInfo0_ */
+    int32_t sdf_volume;      /* SDFInfo::cachedVolumeIndex_ */
 } ar_object;
 
 /* Parameters of one render call (SceneRenderer::Render). */
@@ -162,6 +176,26 @@ ar_status ar_scene_texel_count(ar_ctx* ctx, int64_t* n_floats);
 #define AR_SDF_TORUS 2
 ar_status ar_scene_set_sdf_union(ar_ctx* ctx, const float* prims, int n, float smooth_k, int32_t material);
 
+/* SDF volume cache (SDFCacheManager, core/object/sdf/sdf_cache_manager.cuh;
+ * SceneRenderer::AddVolumeToCacheManager, core/scene.hpp:120-127).  A volume
+ * is a dims[0] x dims[1] x dims[2] grid of signed distances (x fastest) over
+ * the unit cube, sampled nearest far from the surface and trilinearly near it
+ * (SampleSDFAdaptive01, core/object/sdf/sdf_volume.cuh:138-149).
+ * ar_sdf_volume_add fills it on the GPU from a built-in functor (FillSDFVolume:
+ * voxel (x, y, z) holds f(x / (dx - 1) - 0.5, ...)): AR_SDF_FN_TORUS with
+ * params (R, r), AR_SDF_FN_DIAMOND with params (d, bias, tableZ, scale), zeros
+ * meaning the reference's defaults (sdf::CreateDiamond: 0.94, 0.5, 0.3, 0.5).
+ * ar_sdf_volume_add_data takes caller values (host memory).  *index receives
+ * the cache index for ar_object.sdf_volume.  Volumes persist across scene
+ * builds until ar_sdf_volume_clear.  ar_sdf_volume_read copies a volume out
+ * (voxels may be NULL to query dims). */
+#define AR_SDF_FN_TORUS 0
+#define AR_SDF_FN_DIAMOND 1
+ar_status ar_sdf_volume_add(ar_ctx* ctx, int32_t fn, const float* params, const int32_t* dims, int32_t* index);
+ar_status ar_sdf_volume_add_data(ar_ctx* ctx, const float* voxels, const int32_t* dims, int32_t* index);
+ar_status ar_sdf_volume_read(ar_ctx* ctx, int32_t index, float* voxels, int32_t* dims);
+ar_status ar_sdf_volume_clear(ar_ctx* ctx);
+
 /* Homogeneous participating medium filling an axis-aligned box (no reference
  * counterpart): extinction sigma_t, single-scattering albedo, Henyey-Greenstein
  * g (core/render/sample.cuh:110-145), and an emission radiance released where
@@ -209,7 +243,7 @@ ar_status ar_trace_any(ar_ctx* ctx, const float* rays, int n, int32_t* hit, void
  * the array: calls that overlap on the GPU race, so serialise them.  No
  * cudaMalloc / cudaFree is made; profiling (params->profile) is rejected. */
 #define AR_NOALLOC_SCRATCH_BYTES (8u << 20)
-#define AR_NOALLOC_MAX_PATHS 49408
+#define AR_NOALLOC_MAX_PATHS 43264
 ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* params, double* out_xyz_device, void* stream);
 
 /* Replay adjoint (no counterpart in the reference).  Gradient of a scalar loss

@@ -192,11 +192,22 @@ def patch_tree() -> None:
          "static __device__ __constant__ float T005QuantilesDev[T_QUANTILE_LUT_SIZE] = {};")
     _sub(CORE / "denoise" / "t_quantile.cu", r"__device__ __constant__ float T005QuantilesDev\[T_QUANTILE_LUT_SIZE\] = T005_LUT_INIT;",
          "")
+    # (9) SDF volume cache on the host: the reference looks volumes up only in
+    # device memory (core/object/sdf/sdf_master.cuh:15-39) and returns no volume
+    # on the host; here the host branch reads a host table the driver fills.
+    sdfm = CORE / "object" / "sdf" / "sdf_master.cuh"
+    _sub(sdfm, r"(\s*)FUNCTION_MODIFIER_INLINE SDFVolumeInfo\* GetSDFVolumeInfoPtr\(const int cacheIndex\)",
+         r"\1inline SDFVolumeInfo* REF_HOST_SDF_INFOS = nullptr;\1inline uint32_t REF_HOST_SDF_COUNT = 0;"
+         r"\1FUNCTION_MODIFIER_INLINE SDFVolumeInfo* GetSDFVolumeInfoPtr(const int cacheIndex)", count=1)
+    _sub(sdfm, r"#else\n(\s*)return nullptr;\n#endif",
+         r"#else\n\1if (cacheIndex < 0 || cacheIndex >= (int)REF_HOST_SDF_COUNT) return nullptr;\n"
+         r"\1return &REF_HOST_SDF_INFOS[cacheIndex];\n#endif", count=1)
+    _sub(sdfm, r"#else\n(\s*)return 0u;\n#endif", r"#else\n\1return REF_HOST_SDF_COUNT;\n#endif", count=1)
     (CORE / PATCH_STAMP).write_text(PATCH_VERSION)
 
 
 # bump when patch_tree() changes, so an existing patched copy is redone
-PATCH_VERSION = "3"
+PATCH_VERSION = "4"
 PATCH_STAMP = ".ar_patch_version"
 
 

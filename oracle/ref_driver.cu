@@ -226,6 +226,9 @@ struct FileObject
     float v0[3], v1[3], v2[3];
     float albedo[3], emissive[3];
     float roughness, metallic, specular, ior, sigma_a, abbe, tilt;
+    int32_t sdf_type;       // OBJ_SDF: ESDFType
+    float sdf_params[4];    // SDFInfo::sdfInfo0_
+    int32_t sdf_volume;     // SDFInfo::cachedVolumeIndex_
 };
 struct RenderParams
 {
@@ -250,7 +253,48 @@ struct PlainStat
     uint32_t num;
     float mean[3], m2n[3], m3n[3];
 };
+// one SDF volume of the scene file: fn >= 0 fills from the reference functor
+// (0 torus, 1 diamond) with params; fn < 0 is followed by the voxel values
+struct FileVolume
+{
+    int32_t fn;
+    float params[4];
+    int32_t dims[3];
+};
 #pragma pack(pop)
+
+// FillSDFVolume's loop (core/object/sdf/sdf_cache_manager.cuh:14-36) on the host,
+// calling the reference's functors
+static void fill_volume(int fn, const float* prm, const int32_t* dims, float* out)
+{
+    SDFInfo info{};
+    info.sdfInfo0_ = float4{prm[0], prm[1], prm[2], prm[3]};
+    const int3 d{dims[0], dims[1], dims[2]};
+#pragma omp parallel for
+    for (int z = 0; z < d.z; ++z)
+        for (int y = 0; y < d.y; ++y)
+            for (int x = 0; x < d.x; ++x)
+            {
+                const float nx = (d.x > 1) ? static_cast<float>(x) / static_cast<float>(d.x - 1) : 0.0f;
+                const float ny = (d.y > 1) ? static_cast<float>(y) / static_cast<float>(d.y - 1) : 0.0f;
+                const float nz = (d.z > 1) ? static_cast<float>(z) / static_cast<float>(d.z - 1) : 0.0f;
+                const float3 pos01 = make_float3(nx, ny, nz);
+                const size_t idx = static_cast<size_t>(z) * d.x * d.y + static_cast<size_t>(y) * d.x + x;
+                out[idx] = fn == 1 ? sdf::SDFDiamondFunctor{}(pos01 - 0.5f, info) : sdf::SDFTorusFunctor{}(pos01 - 0.5f, info);
+            }
+}
+
+// sdfvol: one volume as ar_sdf_volume_add fills it.  in: FileVolume; out: floats
+static int cmd_sdfvol(const char* in_path, const char* out_path)
+{
+    std::vector<char> buf = read_file(in_path);
+    if (buf.size() < sizeof(FileVolume)) die("bad sdfvol input");
+    const FileVolume* fv = reinterpret_cast<const FileVolume*>(buf.data());
+    std::vector<float> data((size_t)fv->dims[0] * fv->dims[1] * fv->dims[2]);
+    fill_volume(fv->fn, fv->params, fv->dims, data.data());
+    write_file(out_path, data.data(), data.size() * 4);
+    return 0;
+}
 
 static float3 f3(const float* v) { return float3{v[0], v[1], v[2]}; }
 
@@ -346,9 +390,42 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
 {
     std::vector<char> sb = read_file(scene_path);
     std::vector<char> pb = read_file(params_path);
-    if (sb.size() < 8 || memcmp(sb.data(), "ARS1", 4) != 0) die("bad scene file");
+    if (sb.size() < 8 || memcmp(sb.data(), "ARS2", 4) != 0) die("bad scene file");
     const int nobj = *reinterpret_cast<const int32_t*>(sb.data() + 4);
     const FileObject* fo = reinterpret_cast<const FileObject*>(sb.data() + 8);
+    // SDF volume cache after the objects
+    std::vector<std::vector<float>> vol_data;
+    std::vector<sdf::SDFVolumeInfo> vol_info;
+    {
+        size_t at = 8 + (size_t)nobj * sizeof(FileObject);
+        if (sb.size() < at + 4) die("bad scene file (volumes)");
+        const int nvol = *reinterpret_cast<const int32_t*>(sb.data() + at);
+        at += 4;
+        for (int v = 0; v < nvol; ++v)
+        {
+            const FileVolume* fv = reinterpret_cast<const FileVolume*>(sb.data() + at);
+            at += sizeof(FileVolume);
+            const size_t n = (size_t)fv->dims[0] * fv->dims[1] * fv->dims[2];
+            std::vector<float> data(n);
+            if (fv->fn < 0)
+            {
+                memcpy(data.data(), sb.data() + at, n * sizeof(float));
+                at += n * sizeof(float);
+            }
+            else
+            {
+                fill_volume(fv->fn, fv->params, fv->dims, data.data());
+            }
+            vol_data.push_back(std::move(data));
+            sdf::SDFVolumeInfo info{};
+            info.dim_ = int3{fv->dims[0], fv->dims[1], fv->dims[2]};
+            info.ComputeVoxelSize();
+            vol_info.push_back(info);
+        }
+        for (size_t v = 0; v < vol_info.size(); ++v) vol_info[v].volumePtr_ = vol_data[v].data();
+        sdf::REF_HOST_SDF_INFOS = vol_info.empty() ? nullptr : vol_info.data();
+        sdf::REF_HOST_SDF_COUNT = (uint32_t)vol_info.size();
+    }
     RenderParams prm;
     memcpy(&prm, pb.data(), sizeof(prm));
 
@@ -370,6 +447,14 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
             so.proxy_.boundMax_ = float3{fmaxf(o.v0[0], fmaxf(o.v1[0], o.v2[0])), fmaxf(o.v0[1], fmaxf(o.v1[1], o.v2[1])), fmaxf(o.v0[2], fmaxf(o.v1[2], o.v2[2]))};
             so.proxy_.center_ = (so.proxy_.boundMin_ + so.proxy_.boundMax_) * 0.5f;
             objs.push_back(so);
+        }
+        else if (o.type == 2)
+        {
+            AdditionalObjectInfo info{};
+            info.sdfType_ = static_cast<ESDFType>(o.sdf_type);
+            info.sdfInfo_.sdfInfo0_ = float4{o.sdf_params[0], o.sdf_params[1], o.sdf_params[2], o.sdf_params[3]};
+            info.sdfInfo_.cachedVolumeIndex_ = o.sdf_volume;
+            objs.emplace_back(f3(o.center), f3(o.extent), make_material(o), f3(o.rotation), EObjectType::OBJ_SDF, info);
         }
         else
         {
@@ -656,6 +741,7 @@ int main(int argc, char** argv)
     if (cmd == "render" && argc == 5) return cmd_render(argv[2], argv[3], argv[4]);
     if (cmd == "guide" && argc == 4) return cmd_guide(argv[2], argv[3]);
     if (cmd == "denoise" && argc == 4) return cmd_denoise(argv[2], argv[3]);
+    if (cmd == "sdfvol" && argc == 4) return cmd_sdfvol(argv[2], argv[3]);
     die("bad arguments");
     return 2;
 }

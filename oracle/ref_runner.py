@@ -19,7 +19,10 @@ EXE = HERE / "_ref" / "ref_cpu"
 OBJ_DTYPE = np.dtype([("type", "<i4"), ("shading", "<i4"), ("center", "<f4", 3), ("extent", "<f4", 3),
                       ("rotation", "<f4", 3), ("v0", "<f4", 3), ("v1", "<f4", 3), ("v2", "<f4", 3),
                       ("albedo", "<f4", 3), ("emissive", "<f4", 3), ("roughness", "<f4"), ("metallic", "<f4"),
-                      ("specular", "<f4"), ("ior", "<f4"), ("sigma_a", "<f4"), ("abbe", "<f4"), ("tilt", "<f4")])
+                      ("specular", "<f4"), ("ior", "<f4"), ("sigma_a", "<f4"), ("abbe", "<f4"), ("tilt", "<f4"),
+                      ("sdf_type", "<i4"), ("sdf_params", "<f4", 4), ("sdf_volume", "<i4")])
+# one SDF volume: fn 0 torus / 1 diamond filled by the reference functor, -1: values follow
+VOL_DTYPE = np.dtype([("fn", "<i4"), ("params", "<f4", 4), ("dims", "<i4", 3)])
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("max_depth", "<i4"),
                          ("cam_origin", "<f4", 3), ("cam_dir", "<f4", 3), ("fov", "<f4"), ("use_nee", "<i4"),
                          ("seed", "<u8"), ("first_frame", "<i4"), ("per_sample", "<i4"), ("denoise", "<i4")])
@@ -40,14 +43,18 @@ def ensure_built() -> Path:
     return prepare_ref.build_ref()
 
 
-def scene_bytes(objects, mesh=None) -> bytes:
-    """Objects (and mesh triangles, appended as triangle objects) in the oracle's file format."""
+def scene_bytes(objects, mesh=None, volumes=None) -> bytes:
+    """Objects (and mesh triangles, appended as triangle objects) in the oracle's file format,
+    then the SDF volume cache: volumes is a list of (fn, params, dims) to fill with the
+    reference's functor, or (None, values (dz, dy, dx), None) for given values."""
     n_mesh = 0 if mesh is None else len(mesh.indices)
     rec = np.zeros(len(objects) + n_mesh, OBJ_DTYPE)
     for i, o in enumerate(objects):
         m = o.material
+        info = getattr(o, "additionalObjectInfo", None)
+        st, sp, sv = (info.sdf_type, info.params, info.volume) if info is not None else (0, (0.0,) * 4, -1)
         rec[i] = (o.type, m.shading, o.center, o.extent, o.rotation, o.v0, o.v1, o.v2, m.albedo, m.emissive,
-                  m.roughness, m.metallic, m.specular, m.ior, m.sigma_a, m.abbe, m.tilt)
+                  m.roughness, m.metallic, m.specular, m.ior, m.sigma_a, m.abbe, m.tilt, st, sp, sv)
     if n_mesh:
         tv = mesh.triangle_vertices().reshape(-1, 3, 3)
         base = len(objects)
@@ -67,11 +74,36 @@ def scene_bytes(objects, mesh=None) -> bytes:
             r["sigma_a"][sel] = m.sigma_a
             r["abbe"][sel] = m.abbe
             r["tilt"][sel] = m.tilt
-    return b"ARS1" + np.int32(len(rec)).tobytes() + rec.tobytes()
+    out = [b"ARS2", np.int32(len(rec)).tobytes(), rec.tobytes(), np.int32(len(volumes or [])).tobytes()]
+    for fn, prm, dims in volumes or []:
+        v = np.zeros(1, VOL_DTYPE)
+        if fn is None:
+            vals = np.ascontiguousarray(prm, np.float32)
+            v[0] = (-1, (0.0,) * 4, (vals.shape[2], vals.shape[1], vals.shape[0]))
+            out += [v.tobytes(), vals.tobytes()]
+        else:
+            v[0] = (int(fn), tuple(prm), tuple(dims))
+            out.append(v.tobytes())
+    return b"".join(out)
+
+
+def sdf_volume(fn: int, params, dims) -> np.ndarray:
+    """One volume filled on the host with the reference's functor: (dz, dy, dx) float32."""
+    exe = ensure_built()
+    v = np.zeros(1, VOL_DTYPE)
+    v[0] = (int(fn), tuple(params), tuple(dims))
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "in.bin").write_bytes(v.tobytes())
+        r = subprocess.run([str(exe), "sdfvol", str(td / "in.bin"), str(td / "out.bin")], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference oracle failed: " + r.stderr)
+        return np.frombuffer((td / "out.bin").read_bytes(), np.float32).reshape(dims[2], dims[1], dims[0]).copy()
 
 
 def render(objects, size, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
-           seed=0x9E3779B97F4A7C15, first_frame=0, per_sample_frames=0, mesh=None, threads=None, denoise=False):
+           seed=0x9E3779B97F4A7C15, first_frame=0, per_sample_frames=0, mesh=None, threads=None, denoise=False,
+           volumes=None):
     """Returns (mean XYZ (H, W, 3) float64, per-sample XYZ or None, stats dict); with
     denoise=True the stats dict also holds the denoiser records under "gbuffer" and
     "moments" ((H, W) arrays of GBUF_DTYPE / STAT_DTYPE)."""
@@ -82,7 +114,7 @@ def render(objects, size, origin, direction, spp, *, fov=60.0, max_depth=1000, u
               1 if denoise else 0)
     with tempfile.TemporaryDirectory() as td:
         td = Path(td)
-        (td / "scene.bin").write_bytes(scene_bytes(objects, mesh))
+        (td / "scene.bin").write_bytes(scene_bytes(objects, mesh, volumes))
         (td / "params.bin").write_bytes(prm.tobytes())
         env = dict(os.environ)
         if threads:

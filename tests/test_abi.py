@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_abi_version():
-    assert _lib.load().ar_abi_version() == 3
+    assert _lib.load().ar_abi_version() == 4
 
 
 def test_null_and_bad_arguments_return_errors():

@@ -41,7 +41,7 @@ def test_noalloc_rejects_waves_beyond_the_scratch_limit(cuda_device):
     r.build()
     lib = _lib.load()
     p = r.params((32, 32), cam["origin"], cam["direction"], 1, fov=cam["fov"], max_depth=4,
-                 wave_paths=49408 + 1)
+                 wave_paths=43264 + 1)
     out = torch.zeros((32, 32, 3), dtype=torch.float64, device="cuda")
     assert lib.ar_render_noalloc(r._ctx, C.byref(p), out.data_ptr(), None) == _lib.AR_ERR_INVALID
     assert b"exceeds the scratch limit" in lib.ar_last_error(r._ctx)
