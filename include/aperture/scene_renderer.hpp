@@ -44,8 +44,52 @@ enum class EObjectType
 {
     OBJ_CUBE = AR_OBJECT_CUBE,
     OBJ_SPHERE = AR_OBJECT_SPHERE,
+    OBJ_SDF = AR_OBJECT_SDF,
     OBJ_TRIANGLE = AR_OBJECT_TRIANGLE,
 };
+
+struct int3
+{
+    int x, y, z;
+};
+
+// field of an SDF object (AdditionalObjectInfo, core/render/object.cuh:216-225)
+struct AdditionalObjectInfo
+{
+    int sdfType = AR_SDF_OBJECT_TORUS;
+    float params[4] = {0, 0, 0, 0};  // SDFInfo::sdfInfo0_
+    int volume = -1;                 // SDFInfo::cachedVolumeIndex_
+};
+
+// the reference's SDF helpers (namespace sdf, core/object/sdf/*)
+namespace sdf
+{
+inline AdditionalObjectInfo CreateTorus(float scale = 1.0f, float R = 0.375f, float r = 0.125f)
+{
+    AdditionalObjectInfo a;
+    a.sdfType = AR_SDF_OBJECT_TORUS;
+    a.params[0] = R * scale;
+    a.params[1] = r * scale;
+    return a;
+}
+inline AdditionalObjectInfo CreateSDFVolume(int volumeIndex)
+{
+    AdditionalObjectInfo a;
+    a.sdfType = AR_SDF_OBJECT_VOLUME;
+    a.volume = volumeIndex;
+    return a;
+}
+// parameters of the diamond volume functor (SDFInfo::sdfInfo0_ of sdf::CreateDiamond)
+inline AdditionalObjectInfo CreateDiamond(float scale = 1.0f, float d = 0.94f, float bias = 0.5f, float tableZ = 0.3f)
+{
+    AdditionalObjectInfo a;
+    a.params[0] = d;
+    a.params[1] = bias;
+    a.params[2] = tableZ;
+    a.params[3] = scale * 0.5f;
+    return a;
+}
+} // namespace sdf
 
 enum class EShadingModel
 {
@@ -122,10 +166,12 @@ struct SceneObject
     float3 v0_{0, 0, 0}, v1_{0, 0, 0}, v2_{0, 0, 0};
     Material material_;
     EObjectType type_ = EObjectType::OBJ_CUBE;
+    AdditionalObjectInfo additionalObjectInfo_;
     SceneObject() = default;
     SceneObject(float3 center, float3 extent, const Material& material, float3 rotation,
-                EObjectType type = EObjectType::OBJ_CUBE)
-        : center_(center), extent_(extent), rotation_(rotation), material_(material), type_(type)
+                EObjectType type = EObjectType::OBJ_CUBE, const AdditionalObjectInfo& additionalObjectInfo = {})
+        : center_(center), extent_(extent), rotation_(rotation), material_(material), type_(type),
+          additionalObjectInfo_(additionalObjectInfo)
     {
     }
     static SceneObject Triangle(float3 a, float3 b, float3 c, const Material& material)
@@ -199,6 +245,29 @@ class SceneRenderer
         sdf_material_ = material;
         dirty_ = true;
     }
+    // SDF volume cache (SceneRenderer::AddVolumeToCacheManager, core/scene.hpp:120-127):
+    // a dims grid over the unit cube filled on the GPU from a built-in functor
+    // (AR_SDF_FN_DIAMOND / AR_SDF_FN_TORUS, parameters in sdfInfo.params;
+    // pMin / pMax are unused, as in the reference); returns the cache index.
+    int AddVolumeToCacheManager(int3 dims, float3 pMin, float3 pMax, int functor, const AdditionalObjectInfo& sdfInfo)
+    {
+        (void)pMin;
+        (void)pMax;
+        const int32_t d[3] = {dims.x, dims.y, dims.z};
+        int32_t index = -1;
+        check(ar_sdf_volume_add(ctx_, functor, sdfInfo.params, d, &index), "ar_sdf_volume_add");
+        return index;
+    }
+    // the same with caller values (dims.x fastest)
+    int AddVolumeToCacheManager(int3 dims, const std::vector<float>& distances)
+    {
+        const int32_t d[3] = {dims.x, dims.y, dims.z};
+        if (distances.size() != (size_t)dims.x * dims.y * dims.z) throw Error(AR_ERR_INVALID, "volume size mismatch");
+        int32_t index = -1;
+        check(ar_sdf_volume_add_data(ctx_, distances.data(), d, &index), "ar_sdf_volume_add_data");
+        return index;
+    }
+
     // Homogeneous medium in a box (takes effect on the next render); ClearMedium removes it.
     void SetMedium(float3 boxLo, float3 boxHi, float sigmaT, float albedo, float g, float emission)
     {
@@ -315,6 +384,9 @@ class SceneRenderer
             Material::set3(o.v0, s.v0_);
             Material::set3(o.v1, s.v1_);
             Material::set3(o.v2, s.v2_);
+            o.sdf_type = s.additionalObjectInfo_.sdfType;
+            for (int k = 0; k < 4; ++k) o.sdf_params[k] = s.additionalObjectInfo_.params[k];
+            o.sdf_volume = s.additionalObjectInfo_.volume;
         }
         std::vector<int32_t> tri_mat(mesh_materials_.size());
         for (size_t i = 0; i < tri_mat.size(); ++i) tri_mat[i] = mat_id(mesh_materials_[i]);

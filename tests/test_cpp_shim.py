@@ -60,6 +60,8 @@ int main(int argc, char** argv) {
         r.SetTextures({texels}, {{4, 4}});
         r.SetSdfUnion(prims, 0.05f, Material::CreateDiffusePureColor({0.3f, 0.6f, 0.8f}));
         r.SetMedium({-0.5f, -0.5f, -0.5f}, {0.5f, 0.0f, 0.5f}, 1.0f, 0.8f, 0.2f, 0.05f);
+        int diamond = r.AddVolumeToCacheManager({16, 16, 16}, {0, 0, 0}, {1, 1, 1}, AR_SDF_FN_DIAMOND, sdf::CreateDiamond());
+        (void)diamond;
         Camera cam(r, "cpp", 24, 16, {0, 0, 1.4f}, {0, 0, -1});
         std::vector<double> xyz = cam.RenderToFile(std::string(argv[1]) + "/img.bmp", 4, AR_TONE_ACES, 1.5f);
         cam.RenderToFile(std::string(argv[1]) + "/img.pfm", 4);
