@@ -25,6 +25,7 @@ OBJECT_SPHERE = 1
 OBJECT_SDF = 2
 SDF_OBJECT_TORUS, SDF_OBJECT_VOLUME = 0, 1
 SDF_FN_TORUS, SDF_FN_DIAMOND = 0, 1
+BUILD_HOST, BUILD_GPU = 0, 1
 OBJECT_TRIANGLE = 3
 
 SHADING_DIFFUSE = 0
@@ -96,6 +97,7 @@ EXPORTED = [
     "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats", "ar_scene_set_sdf_union", "ar_scene_set_medium",
     "ar_adjoint_medium", "ar_tonemap", "ar_denoise", "ar_denoise_read", "ar_denoise_write",
     "ar_sdf_volume_add", "ar_sdf_volume_add_data", "ar_sdf_volume_read", "ar_sdf_volume_clear",
+    "ar_scene_set_build_mode", "ar_scene_build_time",
 ]
 
 _lib = None
@@ -162,6 +164,8 @@ def load() -> C.CDLL:
         "ar_sdf_volume_add_data": (C.c_int, [vp, vp, vp, P(C.c_int32)]),
         "ar_sdf_volume_read": (C.c_int, [vp, C.c_int32, vp, vp]),
         "ar_sdf_volume_clear": (C.c_int, [vp]),
+        "ar_scene_set_build_mode": (C.c_int, [vp, C.c_int32]),
+        "ar_scene_build_time": (C.c_int, [vp, P(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -216,6 +216,8 @@ struct Ctx
     SdfVolume* d_vols = nullptr;                // device table
     float4* d_sdf_params = nullptr;
     int sdf_object_count = 0;                   // SDF objects in the scene
+    int build_mode = 0;                         // AR_BUILD_HOST / AR_BUILD_GPU
+    double last_build_ms = 0.0;                 // wall time of the last BVH build
     int* d_pend_list = nullptr;                 // shadow rays left for the SDF pass
     // the SDF objects' BVH
     arbvh::WideBVH sdf_bvh;
@@ -387,4 +389,6 @@ cudaError_t launch_scale_means(double* v, long long n, double inv, cudaStream_t 
 void free_denoise(Ctx& c);
 // SDF volume cache (sdfvol.cu)
 void free_volumes(Ctx& c);
+// GPU BVH build (bvh_gpu.cu): same format as arbvh::build_wide_bvh; "" on success
+std::string build_wide_bvh_gpu(const std::vector<arbvh::PrimInput>& prims, arbvh::WideBVH& out, cudaStream_t s);
 } // namespace ar

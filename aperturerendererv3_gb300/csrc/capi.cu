@@ -951,7 +951,15 @@ ar_status ar_scene_build(ar_ctx* ctx)
     }
     const int n_sdf_objects = (int)sdf_prims.size();
     std::string err;
-    if (!arbvh::build_wide_bvh(prims, c.bvh, &err)) return fail(ctx, AR_ERR_INVALID, "BVH build: " + err);
+    const auto tb0 = std::chrono::steady_clock::now();
+    if (c.build_mode == AR_BUILD_GPU)
+    {
+        err = build_wide_bvh_gpu(prims, c.bvh, c.stream);
+        if (!err.empty()) return fail(ctx, AR_ERR_CUDA, err);
+    }
+    else if (!arbvh::build_wide_bvh(prims, c.bvh, &err))
+        return fail(ctx, AR_ERR_INVALID, "BVH build: " + err);
+    c.last_build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb0).count();
     if (c.bvh.depth >= AR_TRAV_STACK) return fail(ctx, AR_ERR_INVALID, "BVH deeper than the traversal stack");
     c.sdf_bvh = arbvh::WideBVH{};
     if (!sdf_prims.empty() && !arbvh::build_wide_bvh(sdf_prims, c.sdf_bvh, &err))
@@ -1090,6 +1098,22 @@ ar_status ar_scene_build(ar_ctx* ctx)
         AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
     }
     c.built = true;
+    return AR_OK;
+}
+
+ar_status ar_scene_set_build_mode(ar_ctx* ctx, int32_t mode)
+{
+    if (!ctx) return AR_ERR_INVALID;
+    if (mode != AR_BUILD_HOST && mode != AR_BUILD_GPU) return fail(ctx, AR_ERR_INVALID, "build mode: host or GPU");
+    ctx->c.build_mode = mode;
+    ctx->c.built = false;
+    return AR_OK;
+}
+
+ar_status ar_scene_build_time(ar_ctx* ctx, double* ms)
+{
+    if (!ctx || !ms) return AR_ERR_INVALID;
+    *ms = ctx->c.last_build_ms;
     return AR_OK;
 }
 

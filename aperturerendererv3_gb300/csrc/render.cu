@@ -695,7 +695,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? 1 : AR_SHADE_MIN_BLOCKS
             V3 maskq = v3(1.0f, 1.0f, 1.0f);
             float pgProb = 0.0f;
             bool mlp_on = false;           // GUIDE == 2: this vertex mixes in the network's distribution
-            uint32_t qw[16];               // its 64 quantised cell weights
+            const uint8_t* qcells = nullptr;  // its 64 quantised cell weights (the path's inference record)
             float q_total = 1.0f;
             if constexpr (GUIDE)
             {
@@ -707,16 +707,8 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? 1 : AR_SHADE_MIN_BLOCKS
                 {
                     if (eligible && prm.mlp_ready && ps.q_pos[p].w > 0.0f)
                     {
-                        const uint4* src = reinterpret_cast<const uint4*>(ps.q_dist + 64 * (size_t)p);
-                        for (int k = 0; k < 4; ++k)
-                        {
-                            const uint4 u = src[k];
-                            qw[4 * k] = u.x;
-                            qw[4 * k + 1] = u.y;
-                            qw[4 * k + 2] = u.z;
-                            qw[4 * k + 3] = u.w;
-                        }
-                        const uint8_t* q = reinterpret_cast<const uint8_t*>(qw);
+                        const uint8_t* q = ps.q_dist + 64 * (size_t)p;
+                        qcells = q;
                         q_total = mlp_total(q);
                         mlp_on = true;
                         const float pB = S.pdf;
@@ -936,8 +928,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? 1 : AR_SHADE_MIN_BLOCKS
                                                 pgProb * octahedron_hemisphere_pdf(*probe, L, h.nrm, maskq);
                                     if (mlp_on)
                                         pBsdf = (1.0f - pgProb) * pBsdf +
-                                                pgProb * mlp_hemisphere_pdf(reinterpret_cast<const uint8_t*>(qw),
-                                                                            1.0f / q_total, L, h.nrm);
+                                                pgProb * mlp_hemisphere_pdf(qcells, 1.0f / q_total, L, h.nrm);
                                 }
                                 const float misW = power_heuristic(pLight, pBsdf);
                                 vUn = mask * (contribution * misW) * d65;

@@ -308,6 +308,19 @@ class SceneRenderer:
     def build(self) -> None:
         self._build()
 
+    def set_build_mode(self, mode: str) -> None:
+        """Where the next build makes the BVH: "host" (binned SAH, default) or "gpu"
+        (Morton-code radix tree collapsed on the GPU; same hits)."""
+        code = {"host": _lib.BUILD_HOST, "gpu": _lib.BUILD_GPU}[mode]
+        check(self._ctx, self._lib.ar_scene_set_build_mode(self._ctx, code))
+        self.bDirty = True
+
+    def build_time_ms(self) -> float:
+        """Wall time of the last BVH build."""
+        ms = C.c_double()
+        check(self._ctx, self._lib.ar_scene_build_time(self._ctx, C.byref(ms)))
+        return ms.value
+
     def stats(self) -> dict:
         self._build()
         n, s, d, b = C.c_int64(), C.c_int64(), C.c_int32(), C.c_int64()

@@ -210,6 +210,17 @@ typedef struct ar_medium
 ar_status ar_scene_set_medium(ar_ctx* ctx, const ar_medium* medium);
 /* Builds the BVH, the light table and the spectral LUTs; uploads the scene. */
 ar_status ar_scene_build(ar_ctx* ctx);
+/* Where ar_scene_build builds the main BVH (the reference builds on the host,
+ * BuildBVH, core/bvh/bvh.cuh:142-422): AR_BUILD_HOST (default) is a binned-SAH
+ * build on the host threads; AR_BUILD_GPU sorts the primitives' centroid
+ * Morton codes, builds a binary radix tree (Karras 2012) and collapses it to
+ * the same 8-wide node format on the GPU: much faster for large meshes, a
+ * tree of lower SAH quality, identical hit results.  Takes effect at the next
+ * ar_scene_build; ar_scene_build_time reports the last build's wall time. */
+#define AR_BUILD_HOST 0
+#define AR_BUILD_GPU 1
+ar_status ar_scene_set_build_mode(ar_ctx* ctx, int32_t mode);
+ar_status ar_scene_build_time(ar_ctx* ctx, double* ms);
 /* BVH statistics: nodes, primitive slots, depth, bytes on the device. */
 ar_status ar_scene_stats(ar_ctx* ctx, int64_t* n_nodes, int64_t* n_slots, int32_t* depth, int64_t* device_bytes);
 
