@@ -97,7 +97,7 @@ EXPORTED = [
     "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats", "ar_scene_set_sdf_union", "ar_scene_set_medium",
     "ar_adjoint_medium", "ar_tonemap", "ar_denoise", "ar_denoise_read", "ar_denoise_write",
     "ar_sdf_volume_add", "ar_sdf_volume_add_data", "ar_sdf_volume_read", "ar_sdf_volume_clear",
-    "ar_scene_set_build_mode", "ar_scene_build_time",
+    "ar_scene_set_build_mode", "ar_scene_build_time", "ar_scene_refit_mesh",
 ]
 
 _lib = None
@@ -166,6 +166,7 @@ def load() -> C.CDLL:
         "ar_sdf_volume_clear": (C.c_int, [vp]),
         "ar_scene_set_build_mode": (C.c_int, [vp, C.c_int32]),
         "ar_scene_build_time": (C.c_int, [vp, P(C.c_double)]),
+        "ar_scene_refit_mesh": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -217,6 +217,13 @@ struct Ctx
     float4* d_sdf_params = nullptr;
     int sdf_object_count = 0;                   // SDF objects in the scene
     int build_mode = 0;                         // AR_BUILD_HOST / AR_BUILD_GPU
+    // refit: wide nodes grouped by depth, mesh indices, per-primitive bounds of the rest
+    std::vector<int> refit_level_off;           // depth d: nodes [off[d], off[d+1]) of d_refit_nodes
+    int* d_refit_nodes = nullptr;
+    uint32_t* d_mesh_idx = nullptr;
+    float* d_prim_box = nullptr;                // 6 per primitive id (objects; triangles recomputed)
+    float* d_node_box = nullptr;                // 6 per wide node (refit scratch)
+    float* d_refit_verts = nullptr;
     double last_build_ms = 0.0;                 // wall time of the last BVH build
     int* d_pend_list = nullptr;                 // shadow rays left for the SDF pass
     // the SDF objects' BVH
@@ -224,6 +231,8 @@ struct Ctx
     void* d_sdf_nodes = nullptr;
     void* d_sdf_bvh_slots = nullptr;
     std::vector<float> mesh_v;           // 9 per mesh triangle
+    std::vector<uint32_t> mesh_idx;      // 3 vertex indices per mesh triangle (for refits)
+    int mesh_nv = 0;                     // vertices of the mesh
     std::vector<int> mesh_material;
     // built scene
     arbvh::WideBVH bvh;
@@ -391,4 +400,6 @@ void free_denoise(Ctx& c);
 void free_volumes(Ctx& c);
 // GPU BVH build (bvh_gpu.cu): same format as arbvh::build_wide_bvh; "" on success
 std::string build_wide_bvh_gpu(const std::vector<arbvh::PrimInput>& prims, arbvh::WideBVH& out, cudaStream_t s);
+// refit of the main BVH after mesh vertices moved (bvh_gpu.cu)
+cudaError_t refit_wide_bvh(Ctx& c, const float* verts_dev, cudaStream_t s);
 } // namespace ar

@@ -1,9 +1,11 @@
 // GPU build of the 8-wide compressed BVH (the same node and slot format as the
-// host builder, ar_bvh.h), and its refit after vertices move.  The reference
+// host builder, ar_bvh.h), and its refit after mesh vertices move (the tree is
+// kept; slots take the new vertices, boxes are recomputed from the leaves up).  The reference
 // builds its BVH on the host (BuildBVH, core/bvh/bvh.cuh:142-422); for meshes of
 // millions of triangles the build dominates scene setup, so this path runs it
 // on the GPU:
-//   1. Morton codes of primitive centroids (30 bits) in the centroid bounds;
+//   1. Morton codes of primitive centroids (63 bits) in the centroid bounds,
+//      scaled by the largest extent on every axis (cells stay cubes);
 //   2. a stable LSD radix sort of (code, primitive) pairs, 8-bit digits;
 //   3. the binary radix tree over the sorted codes (Karras, "Maximizing
 //      parallelism in the construction of BVHs, octrees, and k-d trees", HPG
@@ -71,30 +73,37 @@ __global__ void k_centroid_bounds(const arbvh::PrimInput* __restrict__ prims, in
     }
 }
 
-__device__ __forceinline__ unsigned int expand_bits10(unsigned int v)
+// spreads the low 21 bits of v to every third bit
+__device__ __forceinline__ unsigned long long expand_bits21(unsigned long long v)
 {
-    v = (v * 0x00010001u) & 0xFF0000FFu;
-    v = (v * 0x00000101u) & 0x0F00F00Fu;
-    v = (v * 0x00000011u) & 0xC30C30C3u;
-    v = (v * 0x00000005u) & 0x49249249u;
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
     return v;
 }
 
 __global__ void k_morton(const arbvh::PrimInput* __restrict__ prims, int n, const unsigned int* bounds,
-                         unsigned int* keys, unsigned int* vals)
+                         unsigned long long* keys, unsigned int* vals)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    unsigned int code = 0;
+    float lo[3], ext = 0.0f;
     for (int k = 0; k < 3; ++k)
     {
-        const float lo = bits_fmin(bounds[k]), hi = bits_fmin(bounds[3 + k]);
+        lo[k] = bits_fmin(bounds[k]);
+        ext = fmaxf(ext, bits_fmin(bounds[3 + k]) - lo[k]);
+    }
+    unsigned long long code = 0;
+    for (int k = 0; k < 3; ++k)
+    {
         const float c = 0.5f * (prims[i].lo[k] + prims[i].hi[k]);
-        const float ext = hi - lo;
-        float u = ext > 0.0f ? (c - lo) / ext : 0.0f;
+        float u = ext > 0.0f ? (c - lo[k]) / ext : 0.0f;
         u = fminf(fmaxf(u, 0.0f), 1.0f);
-        const unsigned int q = min((unsigned int)(u * 1024.0f), 1023u);
-        code |= expand_bits10(q) << (2 - k);
+        const unsigned long long q = min((unsigned long long)(u * 2097152.0f), 2097151ull);
+        code |= expand_bits21(q) << (2 - k);
     }
     keys[i] = code;
     vals[i] = (unsigned int)i;
@@ -104,7 +113,7 @@ __global__ void k_morton(const arbvh::PrimInput* __restrict__ prims, int n, cons
 // consecutive tiles of kSortBlock keys; pass: histogram per block, exclusive
 // scan over (digit, block), stable scatter (rank within a tile from warp
 // matches and per-warp digit counts, tiles in order).
-__global__ void k_sort_hist(const unsigned int* __restrict__ keys, int n, int shift, unsigned int* hist, int nblocks)
+__global__ void k_sort_hist(const unsigned long long* __restrict__ keys, int n, int shift, unsigned int* hist, int nblocks)
 {
     __shared__ unsigned int h[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
@@ -113,7 +122,7 @@ __global__ void k_sort_hist(const unsigned int* __restrict__ keys, int n, int sh
     for (int t = 0; t < kSortTiles; ++t)
     {
         const long long i = base + (long long)t * kSortBlock + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xffu], 1u);
+        if (i < n) atomicAdd(&h[(unsigned int)(keys[i] >> shift) & 0xffu], 1u);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)d * nblocks + blockIdx.x] = h[d];
@@ -146,10 +155,10 @@ __global__ void k_sort_scan(unsigned int* hist, int total)
     }
 }
 
-__global__ void __launch_bounds__(kSortBlock) k_sort_scatter(const unsigned int* __restrict__ keys,
+__global__ void __launch_bounds__(kSortBlock) k_sort_scatter(const unsigned long long* __restrict__ keys,
                                                            const unsigned int* __restrict__ vals, int n, int shift,
                                                            const unsigned int* __restrict__ hist, int nblocks,
-                                                           unsigned int* __restrict__ okeys,
+                                                           unsigned long long* __restrict__ okeys,
                                                            unsigned int* __restrict__ ovals)
 {
     constexpr int W = kSortBlock / 32;
@@ -164,8 +173,8 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_scatter(const unsigned int*
         __syncthreads();
         const long long i = base + (long long)t * kSortBlock + threadIdx.x;
         const bool valid = i < n;
-        const unsigned int key = valid ? keys[i] : 0u;
-        const unsigned int dig = valid ? ((key >> shift) & 0xffu) : 256u;
+        const unsigned long long key = valid ? keys[i] : 0ull;
+        const unsigned int dig = valid ? ((unsigned int)(key >> shift) & 0xffu) : 256u;
         const unsigned int peers = __match_any_sync(0xffffffffu, dig);
         const unsigned int rank_in_warp = __popc(peers & ((1u << lane) - 1u));
         if (valid && rank_in_warp == 0) wcnt[warp][dig] = __popc(peers);
@@ -193,15 +202,15 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_scatter(const unsigned int*
 
 // ---- radix tree (Karras 2012).  Internal nodes 0..n-2, leaves n-1+k for sorted
 // position k.  first/last: the sorted range a node covers.
-__device__ __forceinline__ int delta(const unsigned int* keys, int n, int i, int j)
+__device__ __forceinline__ int delta(const unsigned long long* keys, int n, int i, int j)
 {
     if (j < 0 || j >= n) return -1;
-    const unsigned int a = keys[i], b = keys[j];
-    if (a != b) return __clz(a ^ b);
-    return 32 + __clz((unsigned int)i ^ (unsigned int)j);
+    const unsigned long long a = keys[i], b = keys[j];
+    if (a != b) return __clzll(a ^ b);
+    return 64 + __clz((unsigned int)i ^ (unsigned int)j);
 }
 
-__global__ void k_radix_tree(const unsigned int* __restrict__ keys, int n, int2* child, int* parent, int2* range)
+__global__ void k_radix_tree(const unsigned long long* __restrict__ keys, int n, int2* child, int* parent, int2* range)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
@@ -487,6 +496,138 @@ __global__ void k_collapse(CollapseArgs a, const int2* __restrict__ queue, int n
 }
 } // namespace lbvh
 
+// ---- refit
+// triangle slots take the moved vertices (slot tag -> triangle id - n_objects)
+__global__ void k_refit_slots(float4* slots, int nslots, const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                              int nobj)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    const uint32_t tag = __float_as_uint(slots[3 * (size_t)s].w);
+    if ((tag >> AR_PRIM_KIND_SHIFT) != AR_PRIM_KIND_TRI) return;
+    const int id = (int)(tag & AR_PRIM_ID_MASK);
+    if (id < nobj) return;  // a triangle object: not part of the mesh
+    const size_t t = (size_t)(id - nobj);
+    for (int j = 0; j < 3; ++j)
+    {
+        const float* v = verts + 3 * (size_t)idx[3 * t + j];
+        float4 w = slots[3 * (size_t)s + j];
+        w.x = v[0];
+        w.y = v[1];
+        w.z = v[2];
+        slots[3 * (size_t)s + j] = w;
+    }
+}
+
+// one depth of wide nodes: child boxes from the leaves' primitives or the
+// deeper level's node boxes, then the node re-quantized as the builders do
+__global__ void k_refit_level(ar_wide_node* nodes, const int* __restrict__ list, int nlist,
+                              const float4* __restrict__ slots, const float* __restrict__ prim_box, float* node_box)
+{
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= nlist) return;
+    const int ni = list[li];
+    ar_wide_node node = nodes[ni];
+    float cb[8][6];
+    float nb[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    int rank = 0;
+    for (int s = 0; s < 8; ++s)
+    {
+        const uint32_t meta = node.meta[s];
+        if (meta == 0u) continue;
+        float b[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+        if (meta & 0x80u)
+        {
+            const float* src = node_box + 6 * (size_t)(node.child_base + rank);
+            for (int k = 0; k < 6; ++k) b[k] = src[k];
+            ++rank;
+        }
+        else
+        {
+            const int cnt = (int)(meta >> 5), first = (int)(node.prim_base + (meta & 31u));
+            for (int j = 0; j < cnt; ++j)
+            {
+                const float4 a = slots[3 * (size_t)(first + j)];
+                const uint32_t tag = __float_as_uint(a.w);
+                if ((tag >> AR_PRIM_KIND_SHIFT) == AR_PRIM_KIND_TRI)
+                {
+                    const float4 bb = slots[3 * (size_t)(first + j) + 1], cc = slots[3 * (size_t)(first + j) + 2];
+                    b[0] = fminf(b[0], fminf(a.x, fminf(bb.x, cc.x)));
+                    b[1] = fminf(b[1], fminf(a.y, fminf(bb.y, cc.y)));
+                    b[2] = fminf(b[2], fminf(a.z, fminf(bb.z, cc.z)));
+                    b[3] = fmaxf(b[3], fmaxf(a.x, fmaxf(bb.x, cc.x)));
+                    b[4] = fmaxf(b[4], fmaxf(a.y, fmaxf(bb.y, cc.y)));
+                    b[5] = fmaxf(b[5], fmaxf(a.z, fmaxf(bb.z, cc.z)));
+                }
+                else
+                {
+                    const float* pb = prim_box + 6 * (size_t)(tag & AR_PRIM_ID_MASK);
+                    for (int k = 0; k < 3; ++k)
+                    {
+                        b[k] = fminf(b[k], pb[k]);
+                        b[3 + k] = fmaxf(b[3 + k], pb[3 + k]);
+                    }
+                }
+            }
+        }
+        for (int k = 0; k < 6; ++k) cb[s][k] = b[k];
+        for (int k = 0; k < 3; ++k)
+        {
+            nb[k] = fminf(nb[k], b[k]);
+            nb[3 + k] = fmaxf(nb[3 + k], b[3 + k]);
+        }
+    }
+    node.px = nb[0];
+    node.py = nb[1];
+    node.pz = nb[2];
+    double scale[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        const double ext = (double)nb[3 + k] - nb[k];
+        int e = -126;
+        if (ext > 0.0)
+        {
+            e = (int)ceil(log2(ext / 255.0));
+            while (ldexp(255.0, e) < ext) ++e;
+            e = max(-126, min(127, e));
+        }
+        node.e[k] = (uint8_t)(e + 127);
+        scale[k] = ldexp(1.0, e);
+    }
+    for (int s = 0; s < 8; ++s)
+    {
+        if (node.meta[s] == 0u) continue;
+        for (int k = 0; k < 3; ++k)
+        {
+            double ql = floor(((double)cb[s][k] - nb[k]) / scale[k]);
+            double qh = ceil(((double)cb[s][3 + k] - nb[k]) / scale[k]);
+            node.qlo[k][s] = (uint8_t)fmin(fmax(ql, 0.0), 255.0);
+            node.qhi[k][s] = (uint8_t)fmin(fmax(qh, 0.0), 255.0);
+        }
+    }
+    nodes[ni] = node;
+    for (int k = 0; k < 6; ++k) node_box[6 * (size_t)ni + k] = nb[k];
+}
+
+cudaError_t refit_wide_bvh(Ctx& c, const float* verts_dev, cudaStream_t s)
+{
+    const int nslots = (int)c.bvh.slots.size();
+    if (nslots == 0) return cudaSuccess;
+    k_refit_slots<<<(nslots + 255) / 256, 256, 0, s>>>(reinterpret_cast<float4*>(c.d_slots), nslots, verts_dev,
+                                                        c.d_mesh_idx, (int)c.objects.size());
+    cudaError_t e = cudaGetLastError();
+    for (int d = (int)c.refit_level_off.size() - 2; d >= 0 && e == cudaSuccess; --d)
+    {
+        const int a = c.refit_level_off[d], b = c.refit_level_off[d + 1];
+        if (b <= a) continue;
+        k_refit_level<<<(b - a + 127) / 128, 128, 0, s>>>(reinterpret_cast<ar_wide_node*>(c.d_nodes), c.d_refit_nodes + a,
+                                                         b - a, reinterpret_cast<const float4*>(c.d_slots), c.d_prim_box,
+                                                         c.d_node_box);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
 // Builds `prims` into out (host copies of nodes and slots, for the scene's
 // bookkeeping) on the GPU; returns the error string or "".
 std::string build_wide_bvh_gpu(const std::vector<arbvh::PrimInput>& prims, arbvh::WideBVH& out, cudaStream_t s)
@@ -511,9 +652,9 @@ std::string build_wide_bvh_gpu(const std::vector<arbvh::PrimInput>& prims, arbvh
     const int node_cap = n;  // wide nodes never outnumber primitives
     auto* dprims = (arbvh::PrimInput*)dalloc(sizeof(arbvh::PrimInput) * n);
     auto* bounds = (unsigned int*)dalloc(6 * sizeof(unsigned int));
-    auto* k0 = (unsigned int*)dalloc(4ull * n);
+    auto* k0 = (unsigned long long*)dalloc(8ull * n);
     auto* v0 = (unsigned int*)dalloc(4ull * n);
-    auto* k1 = (unsigned int*)dalloc(4ull * n);
+    auto* k1 = (unsigned long long*)dalloc(8ull * n);
     auto* v1 = (unsigned int*)dalloc(4ull * n);
     auto* hist = (unsigned int*)dalloc(4ull * 256 * nblocks);
     auto* child = (int2*)dalloc(sizeof(int2) * (size_t)std::max(1, n - 1));
@@ -542,9 +683,10 @@ std::string build_wide_bvh_gpu(const std::vector<arbvh::PrimInput>& prims, arbvh
         k_morton<<<grid, 256, 0, s>>>(dprims, n, bounds, k0, v0);
         e = cudaGetLastError();
     }
-    // 30-bit codes: four 8-bit passes (the last one sees 6 bits)
-    unsigned int *ka = k0, *va = v0, *kb = k1, *vb = v1;
-    for (int pass = 0; pass < 4 && e == cudaSuccess; ++pass)
+    // 63-bit codes: eight 8-bit passes (the last one sees 7 bits)
+    unsigned long long *ka = k0, *kb = k1;
+    unsigned int *va = v0, *vb = v1;
+    for (int pass = 0; pass < 8 && e == cudaSuccess; ++pass)
     {
         const int shift = 8 * pass;
         k_sort_hist<<<nblocks, kSortBlock, 0, s>>>(ka, n, shift, hist, nblocks);

@@ -111,6 +111,12 @@ void free_scene(Ctx& c)
     free_dev(c.d_sdf_params);
     free_dev(c.d_sdf_nodes);
     free_dev(c.d_sdf_bvh_slots);
+    free_dev(c.d_refit_nodes);
+    free_dev(c.d_mesh_idx);
+    free_dev(c.d_prim_box);
+    free_dev(c.d_node_box);
+    free_dev(c.d_refit_verts);
+    c.refit_level_off.clear();
     c.sdf_object_count = 0;
     c.sdf = SdfUnion{};
     c.tex_count = 0;
@@ -739,6 +745,8 @@ ar_status ar_scene_set_mesh(ar_ctx* ctx, const float* v, int nv, const uint32_t*
     Ctx& c = ctx->c;
     c.mesh_v.resize((size_t)nt * 9);
     c.mesh_material.resize(nt);
+    c.mesh_idx.assign(idx ? idx : nullptr, idx ? idx + 3 * (size_t)nt : nullptr);
+    c.mesh_nv = nv;
     for (int t = 0; t < nt; ++t)
     {
         for (int j = 0; j < 3; ++j)
@@ -1012,6 +1020,38 @@ ar_status ar_scene_build(ar_ctx* ctx)
     AR_CUDA(ctx, cudaMemcpy(c.d_nodes, c.bvh.nodes.data(), c.bvh.nodes.size() * sizeof(ar_wide_node), cudaMemcpyHostToDevice));
     AR_CUDA(ctx, alloc_dev(c.d_slots, c.bvh.slots.size() * sizeof(ar_prim_slot)));
     AR_CUDA(ctx, cudaMemcpy(c.d_slots, c.bvh.slots.data(), c.bvh.slots.size() * sizeof(ar_prim_slot), cudaMemcpyHostToDevice));
+    if (nmesh > 0 && !c.bvh.nodes.empty())
+    {
+        // refit tables: wide nodes by depth (children always follow their parent), mesh
+        // indices, the bounds of the non-triangle primitives
+        std::vector<int> level_nodes, cur{0}, next;
+        c.refit_level_off.assign(1, 0);
+        while (!cur.empty())
+        {
+            next.clear();
+            for (int ni : cur)
+            {
+                level_nodes.push_back(ni);
+                const ar_wide_node& nd = c.bvh.nodes[ni];
+                int rank = 0;
+                for (int sl = 0; sl < 8; ++sl)
+                    if (nd.meta[sl] & 0x80u) next.push_back((int)nd.child_base + rank++);
+            }
+            c.refit_level_off.push_back((int)level_nodes.size());
+            cur.swap(next);
+        }
+        std::vector<float> pbox((size_t)std::max(nobj, 1) * 6, 0.0f);
+        for (int i = 0; i < nobj; ++i)
+            if (c.object_type[i] != AR_OBJECT_TRIANGLE && c.object_type[i] != AR_OBJECT_SDF)
+                object_bounds(c.objects[i], &pbox[6 * (size_t)i], &pbox[6 * (size_t)i + 3]);
+        AR_CUDA(ctx, alloc_dev(c.d_refit_nodes, level_nodes.size()));
+        AR_CUDA(ctx, cudaMemcpy(c.d_refit_nodes, level_nodes.data(), level_nodes.size() * sizeof(int), cudaMemcpyHostToDevice));
+        AR_CUDA(ctx, alloc_dev(c.d_mesh_idx, c.mesh_idx.size()));
+        AR_CUDA(ctx, cudaMemcpy(c.d_mesh_idx, c.mesh_idx.data(), c.mesh_idx.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        AR_CUDA(ctx, alloc_dev(c.d_prim_box, pbox.size()));
+        AR_CUDA(ctx, cudaMemcpy(c.d_prim_box, pbox.data(), pbox.size() * sizeof(float), cudaMemcpyHostToDevice));
+        AR_CUDA(ctx, alloc_dev(c.d_node_box, 6 * c.bvh.nodes.size()));
+    }
     AR_CUDA(ctx, alloc_dev(c.d_objects, objs.size()));
     AR_CUDA(ctx, cudaMemcpy(c.d_objects, objs.data(), objs.size() * sizeof(Object), cudaMemcpyHostToDevice));
     {
@@ -1107,6 +1147,39 @@ ar_status ar_scene_set_build_mode(ar_ctx* ctx, int32_t mode)
     if (mode != AR_BUILD_HOST && mode != AR_BUILD_GPU) return fail(ctx, AR_ERR_INVALID, "build mode: host or GPU");
     ctx->c.build_mode = mode;
     ctx->c.built = false;
+    return AR_OK;
+}
+
+ar_status ar_scene_refit_mesh(ar_ctx* ctx, const float* vertices, int n_vertices, int is_device, void* stream)
+{
+    if (!ctx || !vertices) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (!c.built) return fail(ctx, AR_ERR_STATE, "refit before ar_scene_build");
+    if (c.mesh_idx.empty() || !c.d_mesh_idx) return fail(ctx, AR_ERR_STATE, "refit: the scene has no mesh");
+    if (n_vertices != c.mesh_nv) return fail(ctx, AR_ERR_INVALID, "refit: vertex count differs from the mesh's");
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
+    const size_t bytes = (size_t)n_vertices * 3 * sizeof(float);
+    std::vector<float> host((size_t)n_vertices * 3);
+    const float* dv = vertices;
+    if (!c.d_refit_verts) AR_CUDA(ctx, alloc_dev(c.d_refit_verts, (size_t)n_vertices * 3));
+    if (is_device)
+    {
+        AR_CUDA(ctx, cudaMemcpyAsync(host.data(), vertices, bytes, cudaMemcpyDeviceToHost, s));
+    }
+    else
+    {
+        std::memcpy(host.data(), vertices, bytes);
+        AR_CUDA(ctx, cudaMemcpyAsync(c.d_refit_verts, vertices, bytes, cudaMemcpyHostToDevice, s));
+        dv = c.d_refit_verts;
+    }
+    AR_CUDA(ctx, refit_wide_bvh(c, dv, s));
+    AR_CUDA(ctx, cudaStreamSynchronize(s));
+    // the host copy of the mesh follows (light table, later rebuilds)
+    const size_t nt = c.mesh_idx.size() / 3;
+    for (size_t t = 0; t < nt; ++t)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) c.mesh_v[9 * t + 3 * j + k] = host[3 * (size_t)c.mesh_idx[3 * t + j] + k];
     return AR_OK;
 }
 

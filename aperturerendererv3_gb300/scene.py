@@ -315,6 +315,23 @@ class SceneRenderer:
         check(self._ctx, self._lib.ar_scene_set_build_mode(self._ctx, code))
         self.bDirty = True
 
+    def refit_mesh(self, vertices) -> None:
+        """Moves the mesh's vertices (same count) and refits the BVH on the GPU
+        (the tree is kept; hits are exact).  numpy array or CUDA tensor, (nv, 3)."""
+        self._build()
+        if hasattr(vertices, "data_ptr"):
+            import torch
+            v = vertices.detach().to(torch.float32).contiguous()
+            check(self._ctx, self._lib.ar_scene_refit_mesh(self._ctx, v.data_ptr(), v.numel() // 3, 1,
+                                                           _torch_stream(v.device)))
+        else:
+            v = np.ascontiguousarray(vertices, np.float32)
+            check(self._ctx, self._lib.ar_scene_refit_mesh(self._ctx, v.ctypes.data, v.size // 3, 0, None))
+        if self.mesh is not None:
+            self.mesh = TriangleMesh(np.asarray(vertices if not hasattr(vertices, "cpu") else vertices.cpu().numpy(),
+                                                np.float32).reshape(-1, 3), self.mesh.indices, self.mesh.material_ids,
+                                     self.mesh.materials, self.mesh.uv)
+
     def build_time_ms(self) -> float:
         """Wall time of the last BVH build."""
         ms = C.c_double()

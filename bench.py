@@ -306,6 +306,36 @@ def combined_extra(device: int, spp: int = 16) -> dict:
     return out
 
 
+def bvh_build_extra(device: int, spp: int = 4) -> dict:
+    """The terrain's BVH built on the host (binned SAH) and on the GPU (Morton
+    radix tree collapsed to the same 8-wide format): build wall time, node
+    count, extend-ray node visits, and the device time of a 1920x1080 render
+    through each (same image: hits do not depend on the tree)."""
+    from aperturerendererv3_gb300 import SceneRenderer
+    objs, mesh, cam, _ = build_workload("terrain")
+    kw = dict(fov=cam["fov"], max_depth=16)
+    out = {"triangles": int(len(mesh.indices))}
+    imgs = []
+    for mode in ("host", "gpu"):
+        r = SceneRenderer(objs, device=device, mesh=mesh)
+        if mode == "gpu":
+            r.set_build_mode("gpu")
+        r.build()
+        build_ms = r.build_time_ms()
+        r.Render((1920, 1080), cam["origin"], cam["direction"], 1, **kw)
+        imgs.append(r.Render((1920, 1080), cam["origin"], cam["direction"], spp, **kw))
+        ms = r.last_render_stats()[0]
+        r.Render((1920, 1080), cam["origin"], cam["direction"], 1, profile=2, **kw)
+        prof = r.render_profile()
+        out[mode] = {"build_ms": build_ms, "nodes": r.stats()["nodes"], "render_ms": ms,
+                     "msamples_per_s": 1920 * 1080 * spp / (ms / 1e3) / 1e6,
+                     "extend_node_visits_per_ray": prof["extend_node_visits"] / max(1, prof["extend_rays"])}
+        r.close()
+    out["same_image"] = bool(np.array_equal(imgs[0], imgs[1]))
+    out["build_speedup"] = out["host"]["build_ms"] / max(1e-9, out["gpu"]["build_ms"])
+    return out
+
+
 def denoise_extra(r, w, cam, spp: int = 8, steps: int = 5) -> dict:
     """The denoiser on the headline workload's image: a render with and without
     the per-sample G-buffer / moment records (device time of ar_render), the
@@ -424,7 +454,7 @@ def main() -> None:
                     help="skip the guided, adjoint and BVH-stress measurements reported beside the headline")
     ap.add_argument("--extras", default=None,
                     help="comma-separated subset of the extras to run (guided_voxel, guide_compare, adjoint, combined, "
-                         "bvh_stress, denoise); default: all")
+                         "bvh_stress, denoise, bvh_build); default: all")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = dict(WORKLOADS[args.workload])
@@ -538,7 +568,8 @@ def main() -> None:
                          ("combined", lambda: combined_extra(local) if args.workload != "combined" else
                           {"note": "the headline is the combined workload"}),
                          ("bvh_stress", lambda: bvh_stress_extra(local, 5)),
-                         ("denoise", lambda: denoise_extra(r, w, cam))):
+                         ("denoise", lambda: denoise_extra(r, w, cam)),
+                         ("bvh_build", lambda: bvh_build_extra(local))):
             if args.extras and name not in args.extras.split(","):
                 continue
             try:

@@ -221,6 +221,13 @@ ar_status ar_scene_build(ar_ctx* ctx);
 #define AR_BUILD_GPU 1
 ar_status ar_scene_set_build_mode(ar_ctx* ctx, int32_t mode);
 ar_status ar_scene_build_time(ar_ctx* ctx, double* ms);
+/* Refit after the mesh's vertices moved (same triangles, same vertex count as
+ * ar_scene_set_mesh; 3 floats per vertex, host or device memory): the BVH keeps
+ * its tree, triangle slots take the new vertices and every node's quantized
+ * child boxes are recomputed from the leaves up, on the GPU.  Hits are exact
+ * for the moved mesh; traversal cost grows with how far the tree's original
+ * grouping no longer fits (rebuild with ar_scene_build then). */
+ar_status ar_scene_refit_mesh(ar_ctx* ctx, const float* vertices, int n_vertices, int is_device, void* stream);
 /* BVH statistics: nodes, primitive slots, depth, bytes on the device. */
 ar_status ar_scene_stats(ar_ctx* ctx, int64_t* n_nodes, int64_t* n_slots, int32_t* depth, int64_t* device_bytes);
 

@@ -87,3 +87,32 @@ def test_full_terrain_build(cuda_device):
     ia, ta = a.trace_closest(rays)
     ib, tb = b.trace_closest(rays)
     assert torch.equal(ia, ib) and torch.equal(ta, tb)
+
+
+@pytest.mark.parametrize("mode", ["host", "gpu"])
+def test_refit_answers_like_a_rebuild(cuda_device, mode):
+    """Move the terrain's vertices, refit, and compare with a fresh build of the
+    moved mesh: same hits, same render."""
+    import torch
+    from aperturerendererv3_gb300.scene import TriangleMesh
+    objs, mesh = configs.terrain_scene(res=256, n_spheres=16, seed=5)
+    r = SceneRenderer(objs, mesh=mesh)
+    r.set_build_mode(mode)
+    r.build()
+    rng = np.random.default_rng(3)
+    v = np.asarray(mesh.vertices, np.float32).copy()
+    v[:, 1] = v[:, 1] * 1.4 + rng.normal(0.0, 0.003, len(v)).astype(np.float32)
+    r.refit_mesh(v)
+    moved = TriangleMesh(v, mesh.indices, mesh.material_ids, mesh.materials, mesh.uv)
+    fresh = SceneRenderer(objs, mesh=moved)
+    fresh.build()
+    cam = configs.TERRAIN_CAMERA
+    rays = torch.as_tensor(configs.pinhole_rays(320, 180, cam["origin"], cam["direction"], cam["fov"]), device="cuda")
+    ia, ta = r.trace_closest(rays)
+    ib, tb = fresh.trace_closest(rays)
+    assert torch.equal(ia, ib) and torch.equal(ta, tb)
+    kw = dict(fov=cam["fov"], max_depth=6)
+    assert np.array_equal(r.Render((48, 27), cam["origin"], cam["direction"], 2, **kw),
+                          fresh.Render((48, 27), cam["origin"], cam["direction"], 2, **kw))
+    with pytest.raises(Exception):
+        r.refit_mesh(v[:-1])
