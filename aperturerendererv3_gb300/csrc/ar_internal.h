@@ -223,7 +223,8 @@ struct Ctx
     uint32_t* d_mesh_idx = nullptr;
     float* d_prim_box = nullptr;                // 6 per primitive id (objects; triangles recomputed)
     float* d_node_box = nullptr;                // 6 per wide node (refit scratch)
-    float* d_refit_verts = nullptr;
+    float* d_refit_verts = nullptr;             // the latest refit's vertices (3 per mesh vertex)
+    bool mesh_v_stale = false;                  // mesh_v lags d_refit_verts until a build needs it
     double last_build_ms = 0.0;                 // wall time of the last BVH build
     int* d_pend_list = nullptr;                 // shadow rays left for the SDF pass
     // the SDF objects' BVH

@@ -298,6 +298,23 @@ void free_mlp(Ctx& c)
 // Adam moments, per-path query buffers and the records' extra fields.  The
 // position box spans the non-emissive geometry (a distant sun would squeeze
 // everything else into a corner of the encoding).
+// brings the host copy of the mesh up to the last refit's vertices
+cudaError_t sync_mesh_host(Ctx& c)
+{
+    if (!c.mesh_v_stale) return cudaSuccess;
+    std::vector<float> host((size_t)c.mesh_nv * 3);
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(host.data(), c.d_refit_verts, host.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    const size_t nt = c.mesh_idx.size() / 3;
+    for (size_t t = 0; t < nt; ++t)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) c.mesh_v[9 * t + 3 * j + k] = host[3 * (size_t)c.mesh_idx[3 * t + j] + k];
+    c.mesh_v_stale = false;
+    return cudaSuccess;
+}
+
 ar_status ensure_mlp(ar_ctx* ctx)
 {
     Ctx& c = ctx->c;
@@ -333,6 +350,7 @@ ar_status ensure_mlp(ar_ctx* ctx)
         AR_CUDA(ctx, launch_mlp_to_bf16(c.d_mlp_w32, c.d_mlp_wbf, c.stream));
         AR_CUDA(ctx, mlp_prepare_kernels());
         c.mlp_step = 0;
+        AR_CUDA(ctx, sync_mesh_host(c));
         // box of the non-emissive geometry
         float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
         auto grow = [&](const float* a, const float* b) {
@@ -743,6 +761,7 @@ ar_status ar_scene_set_mesh(ar_ctx* ctx, const float* v, int nv, const uint32_t*
     if (!ctx) return AR_ERR_INVALID;
     if (nt < 0 || nv < 0 || (nt > 0 && (!v || !idx || !mat))) return fail(ctx, AR_ERR_INVALID, "mesh: bad pointer or count");
     Ctx& c = ctx->c;
+    c.mesh_v_stale = false;
     c.mesh_v.resize((size_t)nt * 9);
     c.mesh_material.resize(nt);
     c.mesh_idx.assign(idx ? idx : nullptr, idx ? idx + 3 * (size_t)nt : nullptr);
@@ -862,6 +881,7 @@ ar_status ar_scene_build(ar_ctx* ctx)
     if (!ctx) return AR_ERR_INVALID;
     Ctx& c = ctx->c;
     AR_CUDA(ctx, cudaSetDevice(c.device));
+    AR_CUDA(ctx, sync_mesh_host(c));
     const int nobj = (int)c.objects.size();
     const int nmesh = (int)c.mesh_material.size();
     const int nsdf = c.sdf_prims.empty() ? 0 : 1;  // the smooth-union SDF is one primitive, after the mesh
@@ -1160,26 +1180,14 @@ ar_status ar_scene_refit_mesh(ar_ctx* ctx, const float* vertices, int n_vertices
     AR_CUDA(ctx, cudaSetDevice(c.device));
     cudaStream_t s = stream ? (cudaStream_t)stream : c.stream;
     const size_t bytes = (size_t)n_vertices * 3 * sizeof(float);
-    std::vector<float> host((size_t)n_vertices * 3);
-    const float* dv = vertices;
     if (!c.d_refit_verts) AR_CUDA(ctx, alloc_dev(c.d_refit_verts, (size_t)n_vertices * 3));
-    if (is_device)
-    {
-        AR_CUDA(ctx, cudaMemcpyAsync(host.data(), vertices, bytes, cudaMemcpyDeviceToHost, s));
-    }
-    else
-    {
-        std::memcpy(host.data(), vertices, bytes);
-        AR_CUDA(ctx, cudaMemcpyAsync(c.d_refit_verts, vertices, bytes, cudaMemcpyHostToDevice, s));
-        dv = c.d_refit_verts;
-    }
-    AR_CUDA(ctx, refit_wide_bvh(c, dv, s));
+    // the context keeps the vertices on the device; its host copy of the mesh
+    // (rebuilds, the MLP guide's bounds) is brought up to date when next needed
+    AR_CUDA(ctx, cudaMemcpyAsync(c.d_refit_verts, vertices, bytes,
+                                 is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    AR_CUDA(ctx, refit_wide_bvh(c, c.d_refit_verts, s));
     AR_CUDA(ctx, cudaStreamSynchronize(s));
-    // the host copy of the mesh follows (light table, later rebuilds)
-    const size_t nt = c.mesh_idx.size() / 3;
-    for (size_t t = 0; t < nt; ++t)
-        for (int j = 0; j < 3; ++j)
-            for (int k = 0; k < 3; ++k) c.mesh_v[9 * t + 3 * j + k] = host[3 * (size_t)c.mesh_idx[3 * t + j] + k];
+    c.mesh_v_stale = true;
     return AR_OK;
 }
 

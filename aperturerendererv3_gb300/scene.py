@@ -233,7 +233,8 @@ class SceneRenderer:
             raise _lib.ArError(code, f"ar_create(device={device}) failed (no usable CUDA device?)")
         self._ctx = ctx
         self.objects = list(sceneObjects)
-        self.mesh = mesh
+        self._mesh = mesh
+        self._refit_v = None      # vertices of the last refit, folded into `mesh` when it is next read
         self.textures = list(textures) if textures is not None else []
         self.sdf = sdf
         self.medium = medium
@@ -250,6 +251,22 @@ class SceneRenderer:
             self.close()
         except Exception:
             pass
+
+    @property
+    def mesh(self):
+        if self._refit_v is not None:
+            v = self._refit_v
+            v = v.cpu().numpy() if hasattr(v, "cpu") else v
+            m = self._mesh
+            self._mesh = TriangleMesh(np.asarray(v, np.float32).reshape(-1, 3), m.indices, m.material_ids,
+                                      m.materials, m.uv)
+            self._refit_v = None
+        return self._mesh
+
+    @mesh.setter
+    def mesh(self, m) -> None:
+        self._mesh = m
+        self._refit_v = None
 
     def MarkAsDirty(self) -> None:
         self.bDirty = True
@@ -327,10 +344,9 @@ class SceneRenderer:
         else:
             v = np.ascontiguousarray(vertices, np.float32)
             check(self._ctx, self._lib.ar_scene_refit_mesh(self._ctx, v.ctypes.data, v.size // 3, 0, None))
-        if self.mesh is not None:
-            self.mesh = TriangleMesh(np.asarray(vertices if not hasattr(vertices, "cpu") else vertices.cpu().numpy(),
-                                                np.float32).reshape(-1, 3), self.mesh.indices, self.mesh.material_ids,
-                                     self.mesh.materials, self.mesh.uv)
+        if self._mesh is not None:
+            # a private copy (on the device for tensors); the host mesh is made from it only when read
+            self._refit_v = v.clone() if hasattr(v, "clone") else v.copy()
 
     def build_time_ms(self) -> float:
         """Wall time of the last BVH build."""

@@ -330,10 +330,37 @@ def bvh_build_extra(device: int, spp: int = 4) -> dict:
         out[mode] = {"build_ms": build_ms, "nodes": r.stats()["nodes"], "render_ms": ms,
                      "msamples_per_s": 1920 * 1080 * spp / (ms / 1e3) / 1e6,
                      "extend_node_visits_per_ray": prof["extend_node_visits"] / max(1, prof["extend_rays"])}
+        if mode == "host":
+            out["refit"] = refit_measure(r, mesh, cam, kw, spp)
         r.close()
     out["same_image"] = bool(np.array_equal(imgs[0], imgs[1]))
     out["build_speedup"] = out["host"]["build_ms"] / max(1e-9, out["gpu"]["build_ms"])
     return out
+
+
+def refit_measure(r, mesh, cam, kw, spp: int, steps: int = 5) -> dict:
+    """Refit of the built terrain after its heights are scaled by 1.1 (vertices
+    given in device memory): wall time of `refit_mesh` (a device copy of the
+    vertices, triangle slots, node boxes level by level, one synchronize), and
+    the render through the refitted tree."""
+    import torch
+    dev = torch.device("cuda", r.device)
+    v = torch.as_tensor(np.asarray(mesh.vertices, np.float32), device=dev)
+    v[:, 1] *= 1.1
+    r.refit_mesh(v)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r.refit_mesh(v)
+    torch.cuda.synchronize(dev)
+    refit_ms = (time.perf_counter() - t0) * 1e3 / steps
+    r.Render((1920, 1080), cam["origin"], cam["direction"], spp, **kw)
+    ms = r.last_render_stats()[0]
+    r.Render((1920, 1080), cam["origin"], cam["direction"], 1, profile=2, **kw)
+    prof = r.render_profile()
+    return {"vertices": int(v.shape[0]), "refit_ms": refit_ms, "render_ms": ms,
+            "msamples_per_s": 1920 * 1080 * spp / (ms / 1e3) / 1e6,
+            "extend_node_visits_per_ray": prof["extend_node_visits"] / max(1, prof["extend_rays"])}
 
 
 def denoise_extra(r, w, cam, spp: int = 8, steps: int = 5) -> dict:

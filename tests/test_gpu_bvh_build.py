@@ -116,3 +116,31 @@ def test_refit_answers_like_a_rebuild(cuda_device, mode):
                           fresh.Render((48, 27), cam["origin"], cam["direction"], 2, **kw))
     with pytest.raises(Exception):
         r.refit_mesh(v[:-1])
+
+
+@pytest.mark.parametrize("mode", ["host", "gpu"])
+def test_rebuild_after_device_refit_uses_moved_vertices(cuda_device, mode):
+    """A refit from device memory, then a rebuild through the C ABI alone (no
+    new mesh upload): the context's host copy of the mesh follows the refit."""
+    import ctypes as C
+    import torch
+    from aperturerendererv3_gb300 import _lib
+    from aperturerendererv3_gb300.scene import TriangleMesh
+    objs, mesh = configs.terrain_scene(res=128, n_spheres=8, seed=9)
+    r = SceneRenderer(objs, mesh=mesh)
+    r.build()
+    v = np.asarray(mesh.vertices, np.float32).copy()
+    v[:, 1] = v[:, 1] * 0.6 + 0.05
+    r.refit_mesh(torch.as_tensor(v, device="cuda"))
+    code = {"host": _lib.BUILD_HOST, "gpu": _lib.BUILD_GPU}[mode]
+    assert r._lib.ar_scene_set_build_mode(r._ctx, code) == _lib.AR_OK
+    assert r._lib.ar_scene_build(r._ctx) == _lib.AR_OK
+    fresh = SceneRenderer(objs, mesh=TriangleMesh(v, mesh.indices, mesh.material_ids, mesh.materials, mesh.uv))
+    fresh.build()
+    cam = configs.TERRAIN_CAMERA
+    rays = torch.as_tensor(configs.pinhole_rays(160, 90, cam["origin"], cam["direction"], cam["fov"]), device="cuda")
+    ia, ta = r.trace_closest(rays)
+    ib, tb = fresh.trace_closest(rays)
+    assert torch.equal(ia, ib) and torch.equal(ta, tb)
+    # the Python mesh follows too
+    assert np.array_equal(np.asarray(r.mesh.vertices), v)
