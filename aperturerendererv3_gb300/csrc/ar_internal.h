@@ -16,6 +16,30 @@
 
 namespace ar
 {
+// Order of a frame's pixels among the paths of a wave: bands of 4 rows, each
+// cut into chunks 8 pixels wide taken left to right, row by row inside a
+// chunk.  When the width is a multiple of 8, 32 consecutive paths (one warp)
+// cover an 8 x 4 tile of the image, whose camera rays stay closer together
+// through the BVH than a 32 x 1 strip's.  A bijection of [0, W*H); each path's
+// random stream is keyed by its pixel and frame, so results do not depend on
+// this order.
+#define AR_TILE_W 8u
+#define AR_TILE_H 4u
+AR_HD uint32_t slot_pixel(uint32_t u, uint32_t W, uint32_t H)
+{
+    const uint32_t band_px = AR_TILE_H * W;
+    const uint32_t b = u / band_px;
+    uint32_t rem = u - b * band_px;
+    const uint32_t hb = (H - AR_TILE_H * b) < AR_TILE_H ? (H - AR_TILE_H * b) : AR_TILE_H;
+    const uint32_t chunk_px = AR_TILE_W * hb;
+    const uint32_t c = rem / chunk_px;
+    rem -= c * chunk_px;
+    const uint32_t wc = (W - AR_TILE_W * c) < AR_TILE_W ? (W - AR_TILE_W * c) : AR_TILE_W;
+    const uint32_t r = rem / wc;
+    const uint32_t x = rem - r * wc;
+    return (AR_TILE_H * b + r) * W + AR_TILE_W * c + x;
+}
+
 // Voxel guide as the kernels see it: a sparse open-addressing hash from the
 // packed (voxel, face) key to a probe index, and the probe pool.  The
 // reference keeps the same sparse key set as a sorted unique array

@@ -1291,6 +1291,21 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (d_samples) cudaFree(d_samples);
+    if (e == cudaSuccess && per_sample_xyz)
+    {
+        // samples arrive in path-slot order; hand them back frame-major, pixel-minor
+        std::vector<float> frame((size_t)npix * 3);
+        for (long long f = 0; f < rl.spp; ++f)
+        {
+            float* base = per_sample_xyz + 3 * f * npix;
+            std::memcpy(frame.data(), base, frame.size() * sizeof(float));
+            for (long long u = 0; u < npix; ++u)
+            {
+                const size_t px = slot_pixel((uint32_t)u, (uint32_t)rl.width, (uint32_t)rl.height);
+                for (int k = 0; k < 3; ++k) base[3 * px + k] = frame[3 * u + k];
+            }
+        }
+    }
     c.last_launches = launches;
     for (const StageEvent& se : c.stage_events)
     {

@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
     if (k >= n) return;
     const long long npix = (long long)width * height;
     const long long g = first_path + k;
-    const uint32_t pixel = (uint32_t)(g % npix);
+    const uint32_t pixel = slot_pixel((uint32_t)(g % npix), (uint32_t)width, (uint32_t)height);
     const uint32_t frame = (uint32_t)(g / npix) + (uint32_t)first_frame;
     const int i = (int)(pixel % (uint32_t)width), j = (int)(pixel / (uint32_t)width);
     DevRand R;
@@ -1210,13 +1210,18 @@ __global__ void k_guide_emit(DevScene sc, PathState ps, int n, GuideSamples gs)
 }
 
 // per pixel, adds the wave's samples in increasing sample order (deterministic)
-__global__ void k_accumulate(const float* __restrict__ out_xyz, long long first_path, int n, long long npix,
+// one thread per pixel slot u of a frame (slot_pixel(u) is its pixel): the
+// wave's samples of that pixel are added in frame order
+__global__ void k_accumulate(const float* __restrict__ out_xyz, long long first_path, int n, int width, int height,
                              double* __restrict__ accum)
 {
-    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (p >= npix) return;
-    long long g = first_path - (first_path % npix) + p;
+    const long long npix = (long long)width * height;
+    const long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (u >= npix) return;
+    long long g = first_path - (first_path % npix) + u;
     if (g < first_path) g += npix;
+    if (g >= first_path + n) return;
+    const long long p = slot_pixel((uint32_t)u, (uint32_t)width, (uint32_t)height);
     double sx = accum[3 * p], sy = accum[3 * p + 1], sz = accum[3 * p + 2];
     bool any = false;
     for (; g < first_path + n; g += npix)
@@ -1418,8 +1423,8 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     }
     k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);
     const long long npix = (long long)rl.width * rl.height;
-    k_accumulate<<<(int)((npix + AR_BLOCK - 1) / AR_BLOCK), AR_BLOCK, 0, s>>>(wb.ps.out_xyz, first_path, n, npix,
-                                                                             wb.accum);
+    k_accumulate<<<(int)((npix + AR_BLOCK - 1) / AR_BLOCK), AR_BLOCK, 0, s>>>(wb.ps.out_xyz, first_path, n, rl.width,
+                                                                             rl.height, wb.accum);
     return cudaGetLastError();
 }
 
@@ -1441,7 +1446,7 @@ cudaError_t launch_accumulate(Ctx& c, const RenderLaunch& rl, long long first_pa
 {
     const long long npix = (long long)rl.width * rl.height;
     const int grid = (int)((npix + AR_BLOCK - 1) / AR_BLOCK);
-    k_accumulate<<<grid, AR_BLOCK, 0, c.stream>>>(c.ps.out_xyz, first_path, n, npix, accum);
+    k_accumulate<<<grid, AR_BLOCK, 0, c.stream>>>(c.ps.out_xyz, first_path, n, rl.width, rl.height, accum);
     if (launches) *launches += 1;
     return cudaGetLastError();
 }
