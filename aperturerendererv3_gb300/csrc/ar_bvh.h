@@ -7,7 +7,8 @@
 //   w1: child_base (u32) | prim_base (u32) | meta[0..7] (u8)
 //   w2: qlo_x[8], qlo_y[8]      w3: qlo_z[8], qhi_x[8]      w4: qhi_y[8], qhi_z[8]
 // A child box decodes as p + q * 2^(e-127) per axis (exact conservative bounds).
-// meta[i]: 0 = empty slot; 0x80 | r = internal child stored at child_base + r;
+// meta[i]: 0 = empty slot (its box is inverted, qlo 255 and qhi 0: no ray meets it);
+//          0x80 | r = internal child stored at child_base + r;
 //          (n << 5) | off = leaf with n (1..3) primitive slots at prim_base + off.
 // Children sit in slots chosen by the direction of their centroid from the
 // node's centroid (slot bit k set = +axis k), so a ray whose direction-sign

@@ -18,7 +18,6 @@
 #include "ar_shade.h"
 
 #define AR_TRAV_STACK 40
-#define AR_BOX_SLACK 1.0000004f  // >= 1 + 2*gamma_3 (Ize, "Robust BVH Ray Traversal", JCGT 2013)
 
 namespace ar
 {
@@ -197,27 +196,43 @@ struct TravState
             const uint32_t imask = w0.w >> 24;
             const uint32_t child_base = w1.x;
             const uint32_t prim_base = w1.y;
+            // Per axis the plane p + q 2^e is met at t(q) = q A + B with
+            // A = 2^e / d (exact: a power of two times the reciprocal) and
+            // B = (p - o) / d.  Each child plane costs one fused multiply-add;
+            // E = 2^-21 (|B| + 255 |A|) bounds every rounding of B, of the
+            // reciprocal and of the fused evaluation (at most about 5.2 ulp of
+            // |B| + 255 |A|), so near planes move down and far planes up by E
+            // and the test never rejects a box the ray meets.  Overflow gives
+            // NaN or an infinity on the permissive side, which fminf / fmaxf
+            // then ignore.  The near plane of each axis is the low one when
+            // the direction is positive (octant bit clear): no min / max pairs.
+            const float ax = sx * inv.x, ay = sy * inv.y, az = sz * inv.z;
+            const float bx = (px - o.x) * inv.x, by = (py - o.y) * inv.y, bz = (pz - o.z) * inv.z;
+            const float ex = (fabsf(bx) + 255.0f * fabsf(ax)) * 0x1p-21f;
+            const float ey = (fabsf(by) + 255.0f * fabsf(ay)) * 0x1p-21f;
+            const float ez = (fabsf(bz) + 255.0f * fabsf(az)) * 0x1p-21f;
+            const float bnx = bx - ex, bfx = bx + ex, bny = by - ey, bfy = by + ey, bnz = bz - ez, bfz = bz + ez;
+            const bool fx = oct & 1u, fy = oct & 2u, fz = oct & 4u;
+            const uint32_t nx0 = fx ? w3.z : w2.x, nx1 = fx ? w3.w : w2.y, fx0 = fx ? w2.x : w3.z, fx1 = fx ? w2.y : w3.w;
+            const uint32_t ny0 = fy ? w4.x : w2.z, ny1 = fy ? w4.y : w2.w, fy0 = fy ? w2.z : w4.x, fy1 = fy ? w2.w : w4.y;
+            const uint32_t nz0 = fz ? w4.z : w3.x, nz1 = fz ? w4.w : w3.y, fz0 = fz ? w3.x : w4.z, fz1 = fz ? w3.y : w4.w;
+            const float tlim = res.t;
             uint32_t hit_int = 0, hit_leaf = 0;
 #pragma unroll
             for (int s = 0; s < 8; ++s)
             {
-                const uint32_t meta = byte_of(w1.z, w1.w, s);
-                if (meta == 0u) continue;
-                const float lx = fmaf((float)byte_of(w2.x, w2.y, s), sx, px);
-                const float ly = fmaf((float)byte_of(w2.z, w2.w, s), sy, py);
-                const float lz = fmaf((float)byte_of(w3.x, w3.y, s), sz, pz);
-                const float hx = fmaf((float)byte_of(w3.z, w3.w, s), sx, px);
-                const float hy = fmaf((float)byte_of(w4.x, w4.y, s), sy, py);
-                const float hz = fmaf((float)byte_of(w4.z, w4.w, s), sz, pz);
-                const float t0x = (lx - o.x) * inv.x, t1x = (hx - o.x) * inv.x;
-                const float t0y = (ly - o.y) * inv.y, t1y = (hy - o.y) * inv.y;
-                const float t0z = (lz - o.z) * inv.z, t1z = (hz - o.z) * inv.z;
-                const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-                const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z)) * AR_BOX_SLACK;
-                if (tn <= fminf(tf, res.t))
+                const float tnx = fmaf((float)byte_of(nx0, nx1, s), ax, bnx);
+                const float tny = fmaf((float)byte_of(ny0, ny1, s), ay, bny);
+                const float tnz = fmaf((float)byte_of(nz0, nz1, s), az, bnz);
+                const float tfx = fmaf((float)byte_of(fx0, fx1, s), ax, bfx);
+                const float tfy = fmaf((float)byte_of(fy0, fy1, s), ay, bfy);
+                const float tfz = fmaf((float)byte_of(fz0, fz1, s), az, bfz);
+                const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+                const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
+                if (tn <= tf)
                 {
                     const uint32_t bit = 1u << ((uint32_t)s ^ oct);
-                    if (meta & 0x80u) hit_int |= bit;
+                    if (imask & (1u << s)) hit_int |= bit;
                     else hit_leaf |= bit;
                 }
             }

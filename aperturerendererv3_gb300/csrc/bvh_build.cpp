@@ -271,6 +271,8 @@ struct Collapser
         }
         ar_wide_node node;
         std::memset(&node, 0, sizeof(node));
+        // empty slots: an inverted box (low 255, high 0) that no ray meets
+        std::memset(node.qlo, 0xff, sizeof(node.qlo));
         node.px = nb.lo[0];
         node.py = nb.lo[1];
         node.pz = nb.lo[2];

@@ -409,6 +409,7 @@ __global__ void k_collapse(CollapseArgs a, const int2* __restrict__ queue, int n
     }
     ar_wide_node node;
     memset(&node, 0, sizeof(node));
+    memset(node.qlo, 0xff, sizeof(node.qlo));  // empty slots: an inverted box that no ray meets
     node.px = nb.lo[0];
     node.py = nb.lo[1];
     node.pz = nb.lo[2];

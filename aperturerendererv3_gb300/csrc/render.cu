@@ -248,17 +248,22 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
 #ifndef AR_SHD_STEPS
 #define AR_SHD_STEPS 16
 #endif
+#ifndef AR_EXT_REFILL_MIN0
+#define AR_EXT_REFILL_MIN0 32    // camera rays: a warp refills only when all its lanes are idle
+#endif
+#ifndef AR_SHD_REFILL_MIN0
+#define AR_SHD_REFILL_MIN0 32    // shadow rays of the first vertices
+#endif
 #ifndef AR_TRAV_MIN_BLOCKS
 #define AR_TRAV_MIN_BLOCKS 5     // blocks per SM the traversal kernels are compiled for (48 registers)
 #endif
 
 // Warp-wide fetch of rays for the idle lanes: true and *q = the lane's queue
 // index when it got one; *exhausted (warp-uniform) once the queue is used up.
-template <int MinIdle>
-__device__ __forceinline__ bool warp_refill(int* fetch, int n, bool active, bool* exhausted, int* q)
+__device__ __forceinline__ bool warp_refill(int* fetch, int n, bool active, bool* exhausted, int* q, int min_idle)
 {
     const unsigned idle = __ballot_sync(0xffffffffu, !active);
-    if (*exhausted || __popc(idle) < MinIdle) return false;
+    if (*exhausted || __popc(idle) < min_idle) return false;
     const int need = __popc(idle);
     const int leader = __ffs(idle) - 1;
     int base = 0;
@@ -370,7 +375,8 @@ __global__ void __launch_bounds__(AR_BLOCK) k_sdf_extend(DevScene sc, PathState 
 }
 
 __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScene sc, PathState ps, const int* __restrict__ queue,
-                                                   const int* __restrict__ counter, int* fetch, unsigned int* err)
+                                                   const int* __restrict__ counter, int* fetch, unsigned int* err,
+                                                   int min_idle)
 {
     const int n = *counter;
     TravState<false> st;
@@ -379,7 +385,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
     while (true)
     {
         int q;
-        if (warp_refill<AR_EXT_REFILL_MIN>(fetch, n, active, &exhausted, &q))
+        if (warp_refill(fetch, n, active, &exhausted, &q, min_idle))
         {
             p = queue[q];
             const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
@@ -1093,7 +1099,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_sdf_shadow(DevScene sc, PathState 
 }
 
 __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_shadow(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ counter,
-                                                   int* fetch, SdfPending pend, unsigned int* err)
+                                                   int* fetch, SdfPending pend, unsigned int* err, int min_idle)
 {
     const int n = *counter;
     TravState<true> st;
@@ -1102,7 +1108,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_shadow(DevScen
     while (true)
     {
         int q;
-        if (warp_refill<AR_SHD_REFILL_MIN>(fetch, n, active, &exhausted, &q))
+        if (warp_refill(fetch, n, active, &exhausted, &q, min_idle))
         {
             i = q;
             p = sq.path[i];
@@ -1323,7 +1329,8 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, (has_sdf ? 3 : 2) * sizeof(int), s);  // fetch (+ pending) counters
         {
             StageScope st(c, ST_EXTEND);
-            k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, &cnt[AR_CNT_FETCH], c.d_err);
+            k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, &cnt[AR_CNT_FETCH], c.d_err,
+                                                 b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN);
             if (has_sdf)
             {
                 k_sdf_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn);
@@ -1356,7 +1363,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         {
             StageScope st(c, ST_SHADOW);
             k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd,
-                                                 c.d_err);
+                                                 c.d_err, b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN);
             if (has_sdf)
             {
                 k_sdf_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pend_shd);
@@ -1414,11 +1421,13 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
         cudaMemsetAsync(&cnt[AR_CNT_Q0 + nxt], 0, sizeof(int), s);
         cudaMemsetAsync(&cnt[AR_CNT_SHADOW], 0, sizeof(int), s);
         cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, 3 * sizeof(int), s);
-        k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur], &cnt[AR_CNT_FETCH], err);
+        k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur], &cnt[AR_CNT_FETCH], err,
+                                             b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN);
         if (has_sdf) k_sdf_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur]);
         k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[AR_CNT_Q0 + cur],
                                                    wb.queue[nxt], &cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], prm);
-        k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd, err);
+        k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd, err,
+                                             b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN);
         if (has_sdf) k_sdf_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, pend_shd);
     }
     k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);
