@@ -289,14 +289,16 @@ struct TravState
             node = -2;
             return false;
         }
-        const uint2 e = stack[--sp];
+        // the top group gives its nearest child; the group stays while children remain
+        const uint2 e = stack[sp - 1];
         uint32_t m = e.y & 0xffu;
         const uint32_t im = e.y >> 8;
         const uint32_t i = AR_FFS(m) - 1;
         m &= m - 1;
         const uint32_t s = i ^ oct;
         node = (int)(e.x + AR_POPC(im & ((1u << s) - 1u)));
-        if (m) stack[sp++] = make_uint2(e.x, m | (im << 8));
+        if (m) stack[sp - 1].y = m | (im << 8);
+        else --sp;
         return true;
     }
 };

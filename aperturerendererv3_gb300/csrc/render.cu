@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
 #define AR_SHD_REFILL_MIN0 32    // shadow rays of the first vertices
 #endif
 #ifndef AR_TRAV_MIN_BLOCKS
-#define AR_TRAV_MIN_BLOCKS 5     // blocks per SM the traversal kernels are compiled for (48 registers)
+#define AR_TRAV_MIN_BLOCKS 4     // blocks per SM the traversal kernels are compiled for (64 registers)
 #endif
 
 // Warp-wide fetch of rays for the idle lanes: true and *q = the lane's queue
