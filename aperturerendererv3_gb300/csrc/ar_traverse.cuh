@@ -141,10 +141,12 @@ struct TravState
     int sp;
     uint32_t n_visits, n_tests;
     float sdf_eps;                 // Sdf: march tolerance of SDF objects
-    uint2 stack[AR_TRAV_STACK];
+    uint2* stack;                  // AR_TRAV_STACK node groups, owned by the caller: kept out of
+                                   // the struct so its scalars stay in registers
 
-    AR_HD void init(const TravScene& sc, V3 o_, V3 d_, float tmin_, float tmax_)
+    AR_HD void init(const TravScene& sc, V3 o_, V3 d_, float tmin_, float tmax_, uint2* stack_)
     {
+        stack = stack_;
         o = o_;
         d = d_;
         tmin = tmin_;
@@ -317,7 +319,8 @@ AR_SDFOBJ_CALL TravResult sdf_bvh_trace(const TravScene sc, V3 o, V3 d, float tm
 {
     if (sc.node_count <= 0) return start;
     TravState<AnyHit, true> st;
-    st.init(sc, o, d, tmin, tmax);
+    uint2 stk[AR_TRAV_STACK];
+    st.init(sc, o, d, tmin, tmax, stk);
     st.start_from(start, sdf_eps);
     while (st.step(sc, nullptr))
     {
@@ -330,7 +333,8 @@ AR_HD TravResult traverse_impl(const TravScene& sc, V3 o, V3 d, float tmin, floa
                                                     unsigned int* err, uint32_t& n_visits, uint32_t& n_tests)
 {
     TravState<AnyHit> st;
-    st.init(sc, o, d, tmin, tmax);
+    uint2 stk[AR_TRAV_STACK];
+    st.init(sc, o, d, tmin, tmax, stk);
     while (st.step(sc, err))
     {
     }

@@ -380,6 +380,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
 {
     const int n = *counter;
     TravState<false> st;
+    uint2 stk[AR_TRAV_STACK];
     int p = 0;
     bool active = false, exhausted = false;
     while (true)
@@ -413,7 +414,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
             }
             else
             {
-                st.init(sc.trav, o, d, tmin, __int_as_float(0x7f800000));
+                st.init(sc.trav, o, d, tmin, __int_as_float(0x7f800000), stk);
                 active = true;
             }
         }
@@ -1103,6 +1104,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_shadow(DevScen
 {
     const int n = *counter;
     TravState<true> st;
+    uint2 stk[AR_TRAV_STACK];
     int i = 0, p = 0;
     bool active = false, exhausted = false;
     while (true)
@@ -1113,7 +1115,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_shadow(DevScen
             i = q;
             p = sq.path[i];
             const float4 o = sq.o[i], d = sq.d[i];
-            st.init(sc.trav, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, o.w);
+            st.init(sc.trav, v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), 0.0f, o.w, stk);
             active = true;
         }
         if (__ballot_sync(0xffffffffu, active) == 0)
