@@ -83,6 +83,44 @@ ARR_FN ar_pcg ar_pcg_init(uint64_t seed, uint64_t pixel, uint64_t frame)
     return g;
 }
 
+// The jump of ar_pcg_advance is affine in the state and linear in the
+// increment: advancing by delta maps state to mult * state + inc * plus1
+// (mod 2^64), where mult and plus1 depend on delta alone (plus1 is the
+// additive term ar_pcg_advance builds for inc = 1).  A kernel computes the
+// pair once per frame and applies it per stream, with the same result as
+// ar_pcg_init.
+ARR_FN void ar_pcg_jump(uint64_t delta, uint64_t* mult, uint64_t* plus1)
+{
+    uint64_t cur_mult = AR_PCG_MULT, cur_plus = 1u;
+    uint64_t acc_mult = 1u, acc_plus = 0u;
+    while (delta > 0)
+    {
+        if (delta & 1u)
+        {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1u) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1u;
+    }
+    *mult = acc_mult;
+    *plus1 = acc_plus;
+}
+
+// ar_pcg_init with the frame's jump given as (mult, plus1) = ar_pcg_jump(frame << 32)
+ARR_FN ar_pcg ar_pcg_init_jumped(uint64_t seed, uint64_t pixel, uint64_t frame, uint64_t mult, uint64_t plus1)
+{
+    ar_pcg g;
+    g.state = 0u;
+    g.inc = ar_pcg_increment(pixel);
+    ar_pcg_next(&g);
+    g.state += seed;
+    ar_pcg_next(&g);
+    if (frame) g.state = mult * g.state + g.inc * plus1;
+    return g;
+}
+
 // Uniform in (0, 1]: 24 random bits, +1, scaled exactly.
 ARR_FN float ar_rand1(ar_pcg* g)
 {

@@ -198,14 +198,34 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) *counter = n;
-    if (k >= n) return;
     const long long npix = (long long)width * height;
+    // stream jumps of the first and last frame this block covers, computed once
+    __shared__ uint64_t s_jump[2][2];
+    const long long g_first = first_path + (long long)blockIdx.x * blockDim.x;
+    const long long g_last = first_path + min((long long)(blockIdx.x + 1) * blockDim.x, (long long)n) - 1;
+    const uint32_t f_first = (uint32_t)(g_first / npix) + (uint32_t)first_frame;
+    const uint32_t f_last = (uint32_t)(g_last / npix) + (uint32_t)first_frame;
+    if (threadIdx.x < 2)
+    {
+        uint64_t m, c;
+        ar_pcg_jump((uint64_t)(threadIdx.x ? f_last : f_first) << 32, &m, &c);
+        s_jump[threadIdx.x][0] = m;
+        s_jump[threadIdx.x][1] = c;
+    }
+    __syncthreads();
+    if (k >= n) return;
     const long long g = first_path + k;
     const uint32_t pixel = slot_pixel((uint32_t)(g % npix), (uint32_t)width, (uint32_t)height);
     const uint32_t frame = (uint32_t)(g / npix) + (uint32_t)first_frame;
     const int i = (int)(pixel % (uint32_t)width), j = (int)(pixel / (uint32_t)width);
     DevRand R;
-    R.g = ar_pcg_init(seed, pixel, frame);
+    if (frame == f_first || frame == f_last)
+    {
+        const int w = frame == f_first ? 0 : 1;
+        R.g = ar_pcg_init_jumped(seed, pixel, frame, s_jump[w][0], s_jump[w][1]);
+    }
+    else
+        R.g = ar_pcg_init(seed, pixel, frame);  // blocks spanning more than two frames (images under 256 pixels)
     const float u = (i + R()) / static_cast<float>(width);
     const float v = (j + R()) / static_cast<float>(height);
     const float nx = u * 2.f - 1.f;
