@@ -194,10 +194,14 @@ struct CamParams
 
 __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, int* counter, long long first_path, int n,
                                                    int width, int height, uint64_t seed, int first_frame, CamParams cam,
-                                                   int camera_inside)
+                                                   int camera_inside, int* fetch_reset)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) *counter = n;
+    if (k == 0)
+    {
+        *counter = n;
+        *fetch_reset = 0;  // the first k_extend's fetch counter
+    }
     const long long npix = (long long)width * height;
     // stream jumps of the first and last frame this block covers, computed once
     __shared__ uint64_t s_jump[2][2];
@@ -274,6 +278,10 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
 #ifndef AR_SHD_REFILL_MIN0
 #define AR_SHD_REFILL_MIN0 32    // shadow rays of the first vertices
 #endif
+#ifndef AR_SHADE_GRID_PER_SM
+#define AR_SHADE_GRID_PER_SM 16  // k_shade blocks launched per SM (a grid-stride loop over the queue; more
+                                 // blocks than stay resident balance the uneven per-path work)
+#endif
 #ifndef AR_TRAV_MIN_BLOCKS
 #define AR_TRAV_MIN_BLOCKS 4     // blocks per SM the traversal kernels are compiled for (64 registers)
 #endif
@@ -293,6 +301,29 @@ __device__ __forceinline__ bool warp_refill(int* fetch, int n, bool active, bool
     if (active) return false;
     *q = base + __popc(idle & ((1u << lane_id()) - 1u));
     return *q < n;
+}
+
+// Counters a kernel zeroes for later kernels of the wave (block 0, thread 0,
+// before any other work): each is one that the kernel itself does not use and
+// that no kernel still running could use, so the per-depth counter resets need
+// no memset launches.
+struct CounterReset
+{
+    int* a;
+    int* b;
+    int* c;
+    int* d;
+};
+
+__device__ __forceinline__ void reset_counters(const CounterReset& r)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        if (r.a) *r.a = 0;
+        if (r.b) *r.b = 0;
+        if (r.c) *r.c = 0;
+        if (r.d) *r.d = 0;
+    }
 }
 
 // Shadow rays the traversal left unoccluded, for k_sdf_shadow (list ==
@@ -396,8 +427,9 @@ __global__ void __launch_bounds__(AR_BLOCK) k_sdf_extend(DevScene sc, PathState 
 
 __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScene sc, PathState ps, const int* __restrict__ queue,
                                                    const int* __restrict__ counter, int* fetch, unsigned int* err,
-                                                   int min_idle)
+                                                   int min_idle, CounterReset rs)
 {
+    reset_counters(rs);
     const int n = *counter;
     TravState<false> st;
     uint2 stk[AR_TRAV_STACK];
@@ -567,10 +599,11 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? 1 : AR_SHADE_MIN_BLOCKS
                                                   const int* __restrict__ counter, int* next_queue, int* next_counter,
                                                   int* shadow_counter, ShadeParams prm)
 {
+    const int n = *counter;
+    if (n == 0) return;  // the same for every thread of the block: deep bounces often have no paths left
     __shared__ float s_lam[AR_LAMBDA_LUT_RES * 4];
     for (int i = threadIdx.x; i < AR_LAMBDA_LUT_RES * 4; i += blockDim.x) s_lam[i] = sc.lut_lambda[i];
     __syncthreads();
-    const int n = *counter;
     const int stride = gridDim.x * blockDim.x;
     float g_med_albedo = 0.0f, g_med_emission = 0.0f;  // replay adjoint of the medium parameters
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride)
@@ -1120,8 +1153,10 @@ __global__ void __launch_bounds__(AR_BLOCK) k_sdf_shadow(DevScene sc, PathState 
 }
 
 __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_shadow(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ counter,
-                                                   int* fetch, SdfPending pend, unsigned int* err, int min_idle)
+                                                   int* fetch, SdfPending pend, unsigned int* err, int min_idle,
+                                                   CounterReset rs)
 {
+    reset_counters(rs);
     const int n = *counter;
     TravState<true> st;
     uint2 stk[AR_TRAV_STACK];
@@ -1318,12 +1353,17 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
     const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
     const int grid_p = sms * 8;
+    // the persistent traversal kernels launch as many blocks as stay
+    // resident: they fetch rays from a counter, so extra blocks would only add
+    // launch cost (most deep bounces have few or no paths left)
+    const int grid_t = sms * AR_TRAV_MIN_BLOCKS;
+    const int grid_s = sms * AR_SHADE_GRID_PER_SM;
     int* cnt = c.d_counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
     {
         StageScope st(c, ST_RAYGEN);
         k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, c.d_queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height,
-                                             rl.seed, rl.first_frame, cam, c.camera_inside);
+                                             rl.seed, rl.first_frame, cam, c.camera_inside, &cnt[AR_CNT_FETCH]);
         if (rl.guide) k_guide_init<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, n);
     }
     long long L = rl.guide ? 2 : 1;
@@ -1346,13 +1386,14 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     {
         const int cur = b & 1, nxt = cur ^ 1;
         int* qn = &cnt[AR_CNT_Q0 + cur];
-        cudaMemsetAsync(&cnt[AR_CNT_Q0 + nxt], 0, sizeof(int), s);
-        cudaMemsetAsync(&cnt[AR_CNT_SHADOW], 0, sizeof(int), s);
-        cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, (has_sdf ? 3 : 2) * sizeof(int), s);  // fetch (+ pending) counters
+        // k_extend zeroes the next queue, shadow queue, shadow fetch and pending
+        // counters; k_shadow zeroes the next k_extend's fetch counter
+        const CounterReset ext_rs{&cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], &cnt[AR_CNT_PEND]};
+        const CounterReset shd_rs{&cnt[AR_CNT_FETCH], nullptr, nullptr, nullptr};
         {
             StageScope st(c, ST_EXTEND);
-            k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, &cnt[AR_CNT_FETCH], c.d_err,
-                                                 b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN);
+            k_extend<<<grid_t, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, &cnt[AR_CNT_FETCH], c.d_err,
+                                                 b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN, ext_rs);
             if (has_sdf)
             {
                 k_sdf_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn);
@@ -1374,18 +1415,18 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
             int* nq = c.d_queue[nxt];
             int* nn = &cnt[AR_CNT_Q0 + nxt];
             if (rl.guide == 2)
-                k_shade<2, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+                k_shade<2, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
             else if (rl.guide)
-                k_shade<1, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+                k_shade<1, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
             else if (rl.adjoint)
-                k_shade<0, true><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+                k_shade<0, true><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
             else
-                k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+                k_shade<0, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
         }
         {
             StageScope st(c, ST_SHADOW);
-            k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd,
-                                                 c.d_err, b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN);
+            k_shadow<<<grid_t, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd,
+                                                 c.d_err, b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN, shd_rs);
             if (has_sdf)
             {
                 k_sdf_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pend_shd);
@@ -1423,10 +1464,11 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
     const int grid_p = sms * 8;
+    const int grid_t = sms * AR_TRAV_MIN_BLOCKS, grid_s = sms * AR_SHADE_GRID_PER_SM;
     int* cnt = wb.counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
     k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(wb.ps, wb.queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height, rl.seed,
-                                         rl.first_frame, cam, camera_inside);
+                                         rl.first_frame, cam, camera_inside, &cnt[AR_CNT_FETCH]);
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
@@ -1440,16 +1482,15 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
-        cudaMemsetAsync(&cnt[AR_CNT_Q0 + nxt], 0, sizeof(int), s);
-        cudaMemsetAsync(&cnt[AR_CNT_SHADOW], 0, sizeof(int), s);
-        cudaMemsetAsync(&cnt[AR_CNT_FETCH], 0, 3 * sizeof(int), s);
-        k_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur], &cnt[AR_CNT_FETCH], err,
-                                             b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN);
+        const CounterReset ext_rs{&cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], &cnt[AR_CNT_PEND]};
+        const CounterReset shd_rs{&cnt[AR_CNT_FETCH], nullptr, nullptr, nullptr};
+        k_extend<<<grid_t, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur], &cnt[AR_CNT_FETCH], err,
+                                             b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN, ext_rs);
         if (has_sdf) k_sdf_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur]);
-        k_shade<0, false><<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[AR_CNT_Q0 + cur],
+        k_shade<0, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[AR_CNT_Q0 + cur],
                                                    wb.queue[nxt], &cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], prm);
-        k_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd, err,
-                                             b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN);
+        k_shadow<<<grid_t, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd, err,
+                                             b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN, shd_rs);
         if (has_sdf) k_sdf_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, pend_shd);
     }
     k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);
