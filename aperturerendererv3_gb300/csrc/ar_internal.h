@@ -16,6 +16,9 @@
 
 namespace ar
 {
+#define AR_WAVE_PATHS_AUTO (1 << 25)      // ar_render's automatic wave size
+#define AR_WAVE_PATHS_ADJOINT (1 << 21)   // ar_adjoint's
+
 // Order of a frame's pixels among the paths of a wave: bands of 4 rows, each
 // cut into chunks 8 pixels wide taken left to right, row by row inside a
 // chunk.  When the width is a multiple of 8, 32 consecutive paths (one warp)

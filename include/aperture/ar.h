@@ -106,7 +106,8 @@ typedef struct ar_render_params
     int32_t use_nee;         /* next-event estimation with MIS (SceneSetting::bUseNEE_) */
     uint64_t seed;           /* global seed (GLOBAL_SEED = 0x9e3779b97f4a7c15) */
     int32_t first_frame;     /* frame index of the first sample */
-    int32_t wave_paths;      /* paths in flight per wave, 0 = automatic */
+    int32_t wave_paths;      /* paths in flight per wave, 0 = automatic (ar_render: up to 2^25,
+                                about 8 GB of device state; ar_adjoint: up to 2^21) */
     int32_t profile;         /* 1 = per-stage device times, 2 = traversal counters, 3 = both */
     int32_t guide;           /* AR_GUIDE_NONE, AR_GUIDE_VOXEL (SceneSetting::bUsePathGuiding_) or AR_GUIDE_MLP */
     float guide_unit;        /* voxel size of the guide (0 = 0.05, PATH_GUIDING_RESOLUTION_UNIT) */
