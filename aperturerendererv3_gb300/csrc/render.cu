@@ -14,6 +14,8 @@
 // Queues are compacted with warp ballots and one atomic per warp.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "ar_internal.h"
 #include "ar_rng.h"
 
@@ -278,9 +280,11 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
 #ifndef AR_SHD_REFILL_MIN0
 #define AR_SHD_REFILL_MIN0 32    // shadow rays of the first vertices
 #endif
-#ifndef AR_SHADE_GRID_PER_SM
-#define AR_SHADE_GRID_PER_SM 16  // k_shade blocks launched per SM (a grid-stride loop over the queue; more
-                                 // blocks than stay resident balance the uneven per-path work)
+#ifndef AR_SHADE_PATHS_PER_THREAD
+#define AR_SHADE_PATHS_PER_THREAD 4  // k_shade's grid: one thread per this many paths of the wave (a
+                                     // grid-stride loop; blocks far beyond residency balance the uneven
+                                     // per-path work, and about 4 paths per thread was fastest for both
+                                     // 2^21- and 2^25-path waves)
 #endif
 #ifndef AR_TRAV_MIN_BLOCKS
 #define AR_TRAV_MIN_BLOCKS 4     // blocks per SM the traversal kernels are compiled for (64 registers)
@@ -1357,7 +1361,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     // resident: they fetch rays from a counter, so extra blocks would only add
     // launch cost (most deep bounces have few or no paths left)
     const int grid_t = sms * AR_TRAV_MIN_BLOCKS;
-    const int grid_s = sms * AR_SHADE_GRID_PER_SM;
+    const int grid_s = std::max(2 * sms, (n + AR_BLOCK * AR_SHADE_PATHS_PER_THREAD - 1) / (AR_BLOCK * AR_SHADE_PATHS_PER_THREAD));
     int* cnt = c.d_counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
     {
@@ -1464,7 +1468,8 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
     const int grid_p = sms * 8;
-    const int grid_t = sms * AR_TRAV_MIN_BLOCKS, grid_s = sms * AR_SHADE_GRID_PER_SM;
+    const int grid_t = sms * AR_TRAV_MIN_BLOCKS;
+    const int grid_s = std::max(2 * sms, (n + AR_BLOCK * AR_SHADE_PATHS_PER_THREAD - 1) / (AR_BLOCK * AR_SHADE_PATHS_PER_THREAD));
     int* cnt = wb.counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
     k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(wb.ps, wb.queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height, rl.seed,
