@@ -72,6 +72,27 @@ def test_render_is_deterministic_and_wave_size_independent(cuda_device):
     assert np.all(np.isfinite(a)) and a.mean() > 0
 
 
+@pytest.mark.parametrize("size", [(37, 13), (5, 3), (1, 1)])
+def test_tile_order_and_waves_on_ragged_images(cuda_device, size):
+    """Paths of a wave cover the image in 8x4 tiles per warp; at sizes that cut
+    the tiles, with waves that straddle frames, every sample lands on its own
+    pixel: per-sample output equals the oracle's and does not change with the
+    wave size, bit for bit."""
+    from oracle import ref_runner as rr
+    objs, _, cam = scene("cornell_triangles")
+    r = SceneRenderer(objs)
+    spp, depth = 3, 8
+    kw = dict(fov=cam["fov"], max_depth=depth, per_sample=True)
+    runs = [r.Render(size, cam["origin"], cam["direction"], spp, wave_paths=w, **kw) for w in (0, 100, 7)]
+    for mean, per in runs[1:]:
+        assert np.array_equal(mean, runs[0][0]) and np.array_equal(per, runs[0][1])
+    if rr.available():
+        rmean, rper, _ = rr.render(objs, size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth,
+                                   per_sample_frames=spp)
+        assert close(runs[0][1], rper).mean() == 1.0
+        np.testing.assert_allclose(runs[0][0], rmean, rtol=1e-5, atol=1e-6)
+
+
 def test_errors_are_reported_not_raised_on_device(cuda_device):
     from aperturerendererv3_gb300 import ArError
     objs, _, cam = scene("cornell_triangles")
