@@ -280,6 +280,10 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
 #ifndef AR_SHD_REFILL_MIN0
 #define AR_SHD_REFILL_MIN0 32    // shadow rays of the first vertices
 #endif
+#ifndef AR_SHADE_MLP_MIN_BLOCKS
+#define AR_SHADE_MLP_MIN_BLOCKS 2    // k_shade<2> (MLP guide): blocks per SM it is compiled for (at 1,
+                                     // 201 registers and 11 % of warps active: 3.5 % slower)
+#endif
 #ifndef AR_SHADE_PATHS_PER_THREAD
 #define AR_SHADE_PATHS_PER_THREAD 4  // k_shade's grid: one thread per this many paths of the wave (a
                                      // grid-stride loop; blocks far beyond residency balance the uneven
@@ -599,7 +603,7 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
 }
 
 template <int GUIDE, bool ADJ>
-__global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? 1 : AR_SHADE_MIN_BLOCKS) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
+__global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS : AR_SHADE_MIN_BLOCKS) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
                                                   const int* __restrict__ counter, int* next_queue, int* next_counter,
                                                   int* shadow_counter, ShadeParams prm)
 {
