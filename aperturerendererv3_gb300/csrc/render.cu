@@ -608,7 +608,9 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                                                   int* shadow_counter, ShadeParams prm)
 {
     const int n = *counter;
-    if (n == 0) return;  // the same for every thread of the block: deep bounces often have no paths left
+    // blocks past the queue have nothing to do (the same for every thread of the
+    // block): deep bounces often have few or no paths left
+    if ((long long)blockIdx.x * blockDim.x >= n) return;
     __shared__ float s_lam[AR_LAMBDA_LUT_RES * 4];
     for (int i = threadIdx.x; i < AR_LAMBDA_LUT_RES * 4; i += blockDim.x) s_lam[i] = sc.lut_lambda[i];
     __syncthreads();
