@@ -584,6 +584,8 @@ ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch&
     if (!c.built) return fail(ctx, AR_ERR_STATE, "render before ar_scene_build");
     if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth <= 0 || prm->max_depth > 0xffff)
         return fail(ctx, AR_ERR_INVALID, "render: bad resolution, spp or depth");
+    if ((long long)prm->width * prm->height > 0x7fffffffll)
+        return fail(ctx, AR_ERR_INVALID, "render: more than 2^31 - 1 pixels");  // pixel indices are 32-bit
     AR_CUDA(ctx, cudaSetDevice(c.device));
     rl = RenderLaunch{};
     rl.width = prm->width;

@@ -89,6 +89,11 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
         c.last_error = "render_noalloc: bad resolution, spp or depth";
         return AR_ERR_INVALID;
     }
+    if ((long long)prm->width * prm->height > 0x7fffffffll)
+    {
+        c.last_error = "render_noalloc: more than 2^31 - 1 pixels";  // pixel indices are 32-bit
+        return AR_ERR_INVALID;
+    }
     if (prm->wave_paths > kMaxPaths)
     {
         c.last_error = "render_noalloc: wave_paths " + std::to_string(prm->wave_paths) + " exceeds the scratch limit of " +

@@ -101,5 +101,12 @@ def test_errors_are_reported_not_raised_on_device(cuda_device):
         r.Render((0, 16), cam["origin"], cam["direction"], 1)
     with pytest.raises(ArError):
         r.Render((16, 16), cam["origin"], cam["direction"], 1, max_depth=0)
+    # 2^31 pixels, past the 32-bit pixel index: refused before the output is touched
+    import ctypes as C
+    from aperturerendererv3_gb300 import _lib
+    r.build()
+    big = r.params((65536, 32768), cam["origin"], cam["direction"], 1, fov=cam["fov"])
+    out = (C.c_double * 3)()
+    assert r._lib.ar_render(r._ctx, C.byref(big), out, 0, None, None) == _lib.AR_ERR_INVALID
     with pytest.raises(ArError):
         SceneRenderer([]).Render((4, 4), (0, 0, 0), (0, 0, -1), 1)
