@@ -1362,7 +1362,6 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
     const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
-    const int grid_p = sms * 8;
     // the persistent traversal kernels launch as many blocks as stay
     // resident: they fetch rays from a counter, so extra blocks would only add
     // launch cost (most deep bounces have few or no paths left)
@@ -1406,7 +1405,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
                                                  b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN, ext_rs);
             if (has_sdf)
             {
-                k_sdf_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn);
+                k_sdf_extend<<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn);
                 ++L;
             }
         }
@@ -1416,7 +1415,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
             {
                 // network inference for every queued hit (tensor cores), before shading
                 cudaMemsetAsync(&cnt[AR_CNT_MLP], 0, sizeof(int), s);
-                k_mlp_query<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, c.d_mlp_list, &cnt[AR_CNT_MLP]);
+                k_mlp_query<<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, c.d_mlp_list, &cnt[AR_CNT_MLP]);
                 launch_mlp_infer(net, c.ps.q_pos, c.ps.q_wr, c.d_mlp_list, &cnt[AR_CNT_MLP], 0, c.ps.q_dist, nullptr, c.d_err,
                                  sms, s);
                 L += 2;
@@ -1439,7 +1438,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
                                                  c.d_err, b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN, shd_rs);
             if (has_sdf)
             {
-                k_sdf_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pend_shd);
+                k_sdf_shadow<<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pend_shd);
                 ++L;
             }
         }
@@ -1473,7 +1472,6 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int grid_n = (n + AR_BLOCK - 1) / AR_BLOCK;
-    const int grid_p = sms * 8;
     const int grid_t = sms * AR_TRAV_MIN_BLOCKS;
     const int grid_s = std::max(2 * sms, (n + AR_BLOCK * AR_SHADE_PATHS_PER_THREAD - 1) / (AR_BLOCK * AR_SHADE_PATHS_PER_THREAD));
     int* cnt = wb.counters;  // AR_CNT_* layout
@@ -1497,12 +1495,12 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
         const CounterReset shd_rs{&cnt[AR_CNT_FETCH], nullptr, nullptr, nullptr};
         k_extend<<<grid_t, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur], &cnt[AR_CNT_FETCH], err,
                                              b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN, ext_rs);
-        if (has_sdf) k_sdf_extend<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur]);
+        if (has_sdf) k_sdf_extend<<<grid_s, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur]);
         k_shade<0, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[AR_CNT_Q0 + cur],
                                                    wb.queue[nxt], &cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], prm);
         k_shadow<<<grid_t, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd, err,
                                              b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN, shd_rs);
-        if (has_sdf) k_sdf_shadow<<<grid_p, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, pend_shd);
+        if (has_sdf) k_sdf_shadow<<<grid_s, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, pend_shd);
     }
     k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);
     const long long npix = (long long)rl.width * rl.height;
