@@ -17,7 +17,8 @@
 
 namespace ar
 {
-// primitives: two float4 each, (kind, centre xyz), (size xyz, 0)
+// primitives: two float4 each, (kind, centre xyz), (size xyz, bounding
+// radius: sdf_bounding_radius, filled when the union is uploaded)
 struct SdfUnion
 {
     const float4* prims;
@@ -49,10 +50,38 @@ AR_HD float smin_poly(float a, float b, float k)
     return fminf(a, b) - h * h * k * 0.25f;
 }
 
+// radius of a sphere about the primitive's centre that holds it
+AR_HD float sdf_bounding_radius(float kind, float sx, float sy, float sz)
+{
+    const int k = (int)kind;
+    if (k == AR_SDF_SPHERE) return sx;
+    if (k == AR_SDF_BOX) return sqrtf(sx * sx + sy * sy + sz * sz);
+    return sx + sy;  // torus: major + minor radius
+}
+
+// The smooth union folded left to right.  A primitive whose distance b is at
+// least k above the running value d leaves smin_poly(d, b) = d exactly (its
+// blend weight is zero), so it is skipped: spheres after their distance, boxes
+// and tori already when their bounding sphere's distance, lowered by a margin
+// of 2^-20 (|q| + R) that covers the rounding of both evaluations of the same
+// q, is k above d.  Every skip returns what the full fold would, bit for bit.
 AR_HD float sdf_union(const SdfUnion& s, V3 p)
 {
     float d = sdf_prim(s.prims[0], s.prims[1], p);
-    for (int i = 1; i < s.count; ++i) d = smin_poly(d, sdf_prim(s.prims[2 * i], s.prims[2 * i + 1], p), s.k);
+    for (int i = 1; i < s.count; ++i)
+    {
+        const float4 a = s.prims[2 * i], b = s.prims[2 * i + 1];
+        if ((int)a.x != AR_SDF_SPHERE)
+        {
+            const V3 q = p - v3(a.y, a.z, a.w);
+            const float lq = length(q);
+            const float lower = (lq - b.w) - 0x1p-20f * (lq + b.w);
+            if (lower - d >= s.k) continue;
+        }
+        const float di = sdf_prim(a, b, p);
+        if (di - d >= s.k) continue;
+        d = smin_poly(d, di, s.k);
+    }
     return d;
 }
 

@@ -1142,8 +1142,11 @@ ar_status ar_scene_build(ar_ctx* ctx)
     if (nsdf)
     {
         const int n = (int)(c.sdf_prims.size() / 8);
+        std::vector<float> up(c.sdf_prims);
+        for (int i = 0; i < n; ++i)
+            up[8 * i + 7] = sdf_bounding_radius(up[8 * i], up[8 * i + 4], up[8 * i + 5], up[8 * i + 6]);
         AR_CUDA(ctx, alloc_dev(c.d_sdf, 2 * (size_t)n));
-        AR_CUDA(ctx, cudaMemcpy(c.d_sdf, c.sdf_prims.data(), c.sdf_prims.size() * sizeof(float), cudaMemcpyHostToDevice));
+        AR_CUDA(ctx, cudaMemcpy(c.d_sdf, up.data(), up.size() * sizeof(float), cudaMemcpyHostToDevice));
         c.sdf.prims = c.d_sdf;
         c.sdf.count = n;
         c.sdf.k = c.sdf_k;
