@@ -417,11 +417,36 @@ AR_HD LambdaSample sample_cie1931(float r0, float r1, float r2)
     const float XRatio = 1.0f / total;
     const float YRatio = 1.0f / total;
     const float ZRatio = 1.0f / total;
-    float lambda;
-    if (r0 < uniformRatio) lambda = r1 * (780.0f - 360.0f) + 360.0f;
-    else if (r0 < uniformRatio + XRatio) lambda = sample_cie_x(r1, r2);
-    else if (r0 < uniformRatio + XRatio + YRatio) lambda = sample_cie_y(r1);
-    else lambda = sample_cie_z(r1);
+    // Every lobe is lambda = clamp(T(mu + sig * ndtri(Fa + u (Fb - Fa)))) with T
+    // the identity (the two x lobes) or exp (y, z): the lane picks its lobe's
+    // constants and all lanes share one inverse-CDF evaluation, instead of a
+    // warp running up to four lobe branches one after the other.  Each lane
+    // performs the same operations on the same values as sample_cie_x / _y / _z.
+    const bool uni = r0 < uniformRatio;
+    const bool lx = !uni && r0 < uniformRatio + XRatio;
+    const bool ly = !uni && !lx && r0 < uniformRatio + XRatio + YRatio;
+    const bool lx0 = r1 < 0.8330258723493694f;  // the x lobe's first component
+    float Fa, Fb, mu, sig, u;
+    if (lx)
+    {
+        Fa = lx0 ? 7.4884543e-13f : 0.0000040030528583f;
+        Fb = lx0 ? 0.9999999836707862f : 1.0f;
+        mu = lx0 ? 595.7999999999999545f : 446.8000000000000114f;
+        sig = lx0 ? 33.3299999999999983f : 19.4400000000000013f;
+        u = r2;
+    }
+    else
+    {
+        Fa = ly ? 0.0000000020798312f : 0.0000049890553249f;
+        Fb = ly ? 0.9999953206338883f : 1.0f;
+        mu = ly ? 6.3269327170812479f : 6.1114040395252154f;
+        sig = ly ? 0.0750000000000000f : 0.0510000000000000f;
+        u = r1;
+    }
+    const float t = Fa + u * (Fb - Fa);
+    const float g = mu + sig * ndtrif(t);
+    const float h = lx ? g : arm_expf(g);
+    const float lambda = uni ? r1 * (780.0f - 360.0f) + 360.0f : clamp_lambda(h);
     const float pMix = uniformRatio * 1.0f / (780.0f - 360.0f) + XRatio * pdf_cie_x(lambda) +
                        YRatio * pdf_cie_y(lambda) + ZRatio * pdf_cie_z(lambda);
     LambdaSample s;
