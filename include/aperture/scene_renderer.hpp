@@ -207,6 +207,7 @@ class SceneRenderer
     int max_depth = 1000;           // the reference's MAX_TRACING_DEPTH
     bool use_nee = true;            // SceneSetting::bUseNEE_
     int guide = AR_GUIDE_NONE;      // SceneSetting::bUsePathGuiding_ (AR_GUIDE_VOXEL), or AR_GUIDE_MLP
+    bool denoise = false;           // SceneSetting::bDenoise_: Render returns the bilateral-filtered image
     uint64_t seed = 0x9e3779b97f4a7c15ULL;
 
     // Triangle mesh: n_vertices x 3 floats, 3 indices per triangle, one material per triangle.
@@ -302,10 +303,39 @@ class SceneRenderer
     std::vector<double> RenderXYZ(int2 size, float3 cameraOrigin, float3 cameraDirection, int sampleNum = 1024)
     {
         build();
-        const ar_render_params p = Params(size, cameraOrigin, cameraDirection, sampleNum);
+        ar_render_params p = Params(size, cameraOrigin, cameraDirection, sampleNum);
+        p.denoise_record = denoise ? 1 : 0;
         std::vector<double> xyz((size_t)size.x * size.y * 3);
         check(ar_render(ctx_, &p, xyz.data(), 0, nullptr, nullptr), "ar_render");
-        return xyz;
+        if (!denoise) return xyz;
+        std::vector<double> filtered(xyz.size());
+        check(ar_denoise(ctx_, xyz.data(), 0, filtered.data(), 0, nullptr), "ar_denoise");
+        return filtered;
+    }
+
+    // Where the next build makes the BVH: AR_BUILD_HOST (binned SAH, the
+    // default) or AR_BUILD_GPU (same node format, same hits).
+    void SetBuildMode(int mode)
+    {
+        check(ar_scene_set_build_mode(ctx_, mode), "ar_scene_set_build_mode");
+        dirty_ = true;
+    }
+    // wall time of the last BVH build
+    double BuildTimeMs()
+    {
+        build();
+        double ms = 0.0;
+        check(ar_scene_build_time(ctx_, &ms), "ar_scene_build_time");
+        return ms;
+    }
+    // Moves the mesh's vertices (same count) and refits the BVH on the GPU:
+    // the tree is kept, hits are exact for the moved mesh.
+    void RefitMesh(const std::vector<float3>& vertices)
+    {
+        build();
+        check(ar_scene_refit_mesh(ctx_, vertices.empty() ? nullptr : &vertices[0].x, (int)vertices.size(), 0, nullptr),
+              "ar_scene_refit_mesh");
+        mesh_vertices_ = vertices;
     }
 
     std::vector<float3> Render(int2 size, float3 cameraOrigin, float3 cameraDirection, int sampleNum = 1024)

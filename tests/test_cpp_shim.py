@@ -69,6 +69,22 @@ int main(int argc, char** argv) {
         std::fwrite(xyz.data(), sizeof(double), xyz.size(), f);
         std::fclose(f);
         std::printf("texels %lld\n", (long long)r.TexelCount());
+        // the denoised image, the GPU-built BVH (same hits), a refit of the moved mesh
+        auto dump = [&](const char* name, const std::vector<double>& d) {
+            FILE* g = std::fopen((std::string(argv[1]) + "/" + name).c_str(), "wb");
+            std::fwrite(d.data(), sizeof(double), d.size(), g);
+            std::fclose(g);
+        };
+        r.denoise = true;
+        dump("xyz_dn.bin", r.RenderXYZ({24, 16}, {0, 0, 1.4f}, {0, 0, -1}, 4));
+        r.denoise = false;
+        r.SetBuildMode(AR_BUILD_GPU);
+        std::printf("gpu_build_same %d\n", (int)(r.RenderXYZ({24, 16}, {0, 0, 1.4f}, {0, 0, -1}, 4) == xyz));
+        std::printf("build_ms_positive %d\n", (int)(r.BuildTimeMs() > 0.0));
+        std::vector<float3> moved = v;
+        for (float3& p : moved) p.y += 0.05f;
+        r.RefitMesh(moved);
+        dump("xyz_refit.bin", r.RenderXYZ({24, 16}, {0, 0, 1.4f}, {0, 0, -1}, 4));
     } catch (const Error& e) {
         std::printf("error %d %s\n", e.code, e.what());
         return 1;
@@ -123,6 +139,15 @@ def test_cpp_layer_equals_python_layer(tmp_path, cuda_device):
     assert (tmp_path / "py.bmp").read_bytes() == (tmp_path / "img.bmp").read_bytes()
     write_pfm(str(tmp_path / "py.pfm"), img)
     assert (tmp_path / "py.pfm").read_bytes() == (tmp_path / "img.pfm").read_bytes()
+    # denoiser, GPU build and refit through the C++ layer
+    assert "gpu_build_same 1" in out and "build_ms_positive 1" in out, out
+    den = r.Render((24, 16), (0, 0, 1.4), (0, 0, -1), 4, fov=40.0, max_depth=8, denoise=True)
+    assert np.array_equal(np.fromfile(tmp_path / "xyz_dn.bin", np.float64).reshape(den.shape), den)
+    moved = v.copy()
+    moved[:, 1] += np.float32(0.05)
+    r.refit_mesh(moved)
+    ref = r.Render((24, 16), (0, 0, 1.4), (0, 0, -1), 4, fov=40.0, max_depth=8)
+    assert np.array_equal(np.fromfile(tmp_path / "xyz_refit.bin", np.float64).reshape(ref.shape), ref)
 
 
 def test_cpp_layer_compiles_links_and_runs(tmp_path):
