@@ -228,6 +228,7 @@ struct Ctx
 {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaEvent_t order_event = nullptr;  // orders a caller's stream after the context's (ar_render_noalloc)
     std::string last_error;
     // host scene description
     std::vector<Material> materials;
@@ -388,6 +389,9 @@ cudaError_t launch_guide_update(Ctx& c, long long* launches);
 int guide_probe_count(Ctx& c);
 
 DevScene dev_scene(const Ctx& c);
+// 1 when a camera at cam_o starts inside a box, sphere or SDF object (host test;
+// SDF objects read the host copy of the volume cache)
+int camera_inside_any(const Ctx& c, const float cam_o[3]);
 
 // Wavefront working set supplied by the caller (allocation-free rendering).
 struct WaveBuffers

@@ -63,6 +63,41 @@ DevScene dev_scene(const Ctx& c)
     s.tex_count = c.tex_count;
     return s;
 }
+// intersection::Overlap for one object (core/render/intersection.cuh:312-327);
+// SDF objects evaluate their field on the host copy of the volume cache
+// (OverlapSDFObject, core/object/sdf/sdf_base.cuh:165-176)
+bool overlap_any(const Ctx& c, V3 p, int i)
+{
+    const Object& ob = c.objects[i];
+    if (ob.type != AR_OBJECT_SDF) return overlap_object(p, ob);
+    SdfObjField f;
+    f.kind = ob.pad[0];
+    f.prm = c.object_sdf[i];
+    f.vol = nullptr;
+    SdfVolume hv{};
+    const int vi = ob.pad[1];
+    if (f.kind == AR_SDF_OBJ_VOLUME && vi >= 0 && vi < (int)c.vol_host.size())
+    {
+        hv.data = c.vol_host[vi].data();
+        hv.dx = c.vol_dims[3 * vi];
+        hv.dy = c.vol_dims[3 * vi + 1];
+        hv.dz = c.vol_dims[3 * vi + 2];
+        hv.voxel_size_max = sdf_volume_voxel_size_max(hv.dx, hv.dy, hv.dz);
+        f.vol = &hv;
+    }
+    const V3 lp = mul(ob.w2o, p - ob.center);
+    return sdf_obj_eval(f, sdf_to_unit(lp, ob.extent)) <= 0.0f;
+}
+
+// 1 when the camera starts inside a non-triangle object (the first
+// intersection::Overlap of CalculateRadiance, core/render/render.cuh:536-538)
+int camera_inside_any(const Ctx& c, const float cam_o[3])
+{
+    const V3 co = v3(cam_o[0], cam_o[1], cam_o[2]);
+    for (size_t i = 0; i < c.objects.size(); ++i)
+        if (c.object_type[i] != AR_OBJECT_TRIANGLE && overlap_any(c, co, (int)i)) return 1;
+    return 0;
+}
 } // namespace ar
 
 namespace
@@ -551,33 +586,7 @@ bool cuda_device_ok(int device, std::string* why)
 }
 // Validates the render parameters and fills the launch description; resets
 // the per-render profile state and decides whether the camera starts inside
-// an object (intersection::Overlap, core/render/intersection.cuh:312-327).
-// intersection::Overlap for one object (core/render/intersection.cuh:312-327);
-// SDF objects evaluate their field on the host copy of the volume cache
-// (OverlapSDFObject, core/object/sdf/sdf_base.cuh:165-176)
-bool overlap_any(const Ctx& c, V3 p, int i)
-{
-    const Object& ob = c.objects[i];
-    if (ob.type != AR_OBJECT_SDF) return overlap_object(p, ob);
-    SdfObjField f;
-    f.kind = ob.pad[0];
-    f.prm = c.object_sdf[i];
-    f.vol = nullptr;
-    SdfVolume hv{};
-    const int vi = ob.pad[1];
-    if (f.kind == AR_SDF_OBJ_VOLUME && vi >= 0 && vi < (int)c.vol_host.size())
-    {
-        hv.data = c.vol_host[vi].data();
-        hv.dx = c.vol_dims[3 * vi];
-        hv.dy = c.vol_dims[3 * vi + 1];
-        hv.dz = c.vol_dims[3 * vi + 2];
-        hv.voxel_size_max = sdf_volume_voxel_size_max(hv.dx, hv.dy, hv.dz);
-        f.vol = &hv;
-    }
-    const V3 lp = mul(ob.w2o, p - ob.center);
-    return sdf_obj_eval(f, sdf_to_unit(lp, ob.extent)) <= 0.0f;
-}
-
+// an object (camera_inside_any).
 ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch& rl)
 {
     Ctx& c = ctx->c;
@@ -615,16 +624,7 @@ ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch&
         AR_CUDA(ctx, cudaMemsetAsync(c.d_stats, 0, 8 * sizeof(unsigned long long), c.stream));
     }
     // camera inside a medium (intersection::Overlap, core/render/intersection.cuh:312-327)
-    c.camera_inside = 0;
-    {
-        const V3 co = v3(rl.cam_o[0], rl.cam_o[1], rl.cam_o[2]);
-        for (size_t i = 0; i < c.objects.size(); ++i)
-            if (c.object_type[i] != AR_OBJECT_TRIANGLE && overlap_any(c, co, (int)i))
-            {
-                c.camera_inside = 1;
-                break;
-            }
-    }
+    c.camera_inside = camera_inside_any(c, rl.cam_o);
     return AR_OK;
 }
 
@@ -646,6 +646,7 @@ ar_status ar_create(ar_ctx** out, int device)
     c.device = device;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.order_event, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_err, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(c.d_err, 0, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_counters, AR_CNT_COUNT * sizeof(int));
@@ -694,6 +695,7 @@ ar_status ar_destroy(ar_ctx* ctx)
     free_dev(c.d_grad32);
     free_dev(c.d_adj);
     free_dev(c.d_grad_medium);
+    if (c.order_event) cudaEventDestroy(c.order_event);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete ctx;
     return AR_OK;

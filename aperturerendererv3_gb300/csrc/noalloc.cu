@@ -13,7 +13,9 @@
 // (8 MiB).  Every GPU that loads the library holds it until the process exits.
 // Its device address is looked up once per device with cudaGetSymbolAddress, on
 // the first call made with that device current; make that first call before
-// any stream capture begins.  All calls share the array and it keeps the last
+// any stream capture begins.  The address is kept for the life of the process:
+// cudaDeviceReset unloads the module (and ends every context of the device), so
+// no call may follow a reset of that device.  All calls share the array and it keeps the last
 // call's contents: each call re-initialises what must start fresh (queue
 // counters, the caller's output) before use.  Calls whose work overlaps on the
 // GPU (other streams, other host threads) race on the array; serialise them.
@@ -114,7 +116,7 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
         return AR_ERR_CUDA;
     }
     const int cap = prm->wave_paths > 0 ? prm->wave_paths : kMaxPaths;
-    WaveBuffers wb;
+    WaveBuffers wb{};
     unsigned char* cur = base;
     const size_t n = (size_t)cap;
     wb.ps.rng = carve<uint64_t>(cur, n);
@@ -152,7 +154,7 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
     wb.accum = out_xyz_device;
     wb.stream = stream ? (cudaStream_t)stream : c.stream;
 
-    RenderLaunch rl;
+    RenderLaunch rl{};
     rl.width = prm->width;
     rl.height = prm->height;
     rl.spp = prm->spp;
@@ -167,23 +169,23 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
     rl.seed = prm->seed;
     rl.first_frame = prm->first_frame;
     rl.profile = 0;
-    int camera_inside = 0;
-    {
-        const V3 co = v3(rl.cam_o[0], rl.cam_o[1], rl.cam_o[2]);
-        for (size_t i = 0; i < c.objects.size(); ++i)
-            if (c.object_type[i] != AR_OBJECT_TRIANGLE && overlap_object(co, c.objects[i]))
-            {
-                camera_inside = 1;
-                break;
-            }
-    }
+    // the same test as ar_render's (SDF objects evaluate their field; no allocation)
+    const int camera_inside = camera_inside_any(c, rl.cam_o);
     DevScene sc = dev_scene(c);
     sc.stats = nullptr;
     sc.camera_inside = camera_inside;
     const long long npix = (long long)rl.width * rl.height;
     const long long total = npix * rl.spp;
+    // work the context queued without waiting (ar_scene_update_texels with a
+    // NULL stream, for instance) comes first when the caller passes a stream
+    // of its own; the event was created with the context
+    if (wb.stream != c.stream)
+    {
+        e = cudaEventRecord(c.order_event, c.stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(wb.stream, c.order_event, 0);
+    }
     // the caller's buffer is the FP64 accumulator: clear it first
-    e = cudaMemsetAsync(out_xyz_device, 0, (size_t)npix * 3 * sizeof(double), wb.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(out_xyz_device, 0, (size_t)npix * 3 * sizeof(double), wb.stream);
     for (long long first = 0; first < total && e == cudaSuccess; first += cap)
     {
         const int nw = (int)std::min<long long>(cap, total - first);

@@ -15,6 +15,7 @@ Only numeric tables are extracted; the code that uses them is our own
 from __future__ import annotations
 
 import re
+import os
 import sys
 from pathlib import Path
 
@@ -56,7 +57,12 @@ def extract(ref_root: Path) -> dict[str, np.ndarray]:
 
 
 def main() -> None:
-    ref_root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) > 1:
+        ref_root = Path(sys.argv[1])
+    elif os.environ.get("AR_REFERENCE_ROOT"):
+        ref_root = Path(os.environ["AR_REFERENCE_ROOT"])
+    else:
+        sys.exit("usage: make_spectral_tables.py REFERENCE_CHECKOUT (or set AR_REFERENCE_ROOT)")
     tables = extract(ref_root)
     dst = Path(__file__).resolve().parent / "spectral_tables.npz"
     np.savez(dst, **tables)

@@ -258,9 +258,15 @@ ar_status ar_trace_any(ar_ctx* ctx, const float* rays, int n, int32_t* hit, void
  * exit), so at most AR_NOALLOC_MAX_PATHS paths are in flight per wave;
  * params->wave_paths above that is rejected with AR_ERR_INVALID (0 = the
  * maximum).  The first call on a device looks the array up with
- * cudaGetSymbolAddress and must happen before any stream capture.  Calls share
- * the array: calls that overlap on the GPU race, so serialise them.  No
- * cudaMalloc / cudaFree is made; profiling (params->profile) is rejected. */
+ * cudaGetSymbolAddress and must happen before any stream capture; the address
+ * is kept for the rest of the process.  cudaDeviceReset ends every ar_ctx of
+ * that device and unloads the array with the library's module, so after a
+ * reset this entry point must not be called again in that process.  Calls share
+ * the array: calls that overlap on the GPU race, so serialise them.  When
+ * `stream` is not the context's own stream, the call first makes it wait for
+ * the work the context has queued (e.g. ar_scene_update_texels with a NULL
+ * stream).  No cudaMalloc / cudaFree is made; profiling (params->profile) is
+ * rejected. */
 #define AR_NOALLOC_SCRATCH_BYTES (8u << 20)
 #define AR_NOALLOC_MAX_PATHS 43264
 ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* params, double* out_xyz_device, void* stream);

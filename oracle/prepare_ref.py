@@ -50,7 +50,9 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
-REF_ROOT = Path(os.environ.get("AR_REFERENCE_ROOT", "/root/reference"))
+# The reference checkout: given by the AR_REFERENCE_ROOT environment variable or
+# by `--reference PATH` on the command line; there is no default location.
+REF_ROOT = Path(os.environ["AR_REFERENCE_ROOT"]) if os.environ.get("AR_REFERENCE_ROOT") else None
 OUT = HERE / "_ref"
 SRC = OUT / "src"
 CORE = SRC / "core"
@@ -74,7 +76,7 @@ def _prepend(path: Path, text: str) -> None:
 
 
 def copy_tree() -> None:
-    if not (REF_ROOT / "core").is_dir():
+    if REF_ROOT is None or not (REF_ROOT / "core").is_dir():
         raise FileNotFoundError(f"reference checkout not found at {REF_ROOT}")
     if SRC.exists():
         shutil.rmtree(SRC)
@@ -214,7 +216,7 @@ PATCH_STAMP = ".ar_patch_version"
 def needs_prepare() -> bool:
     """True when the reference checkout is present and the patched copy is
     missing or was made by an older patch_tree()."""
-    if not (REF_ROOT / "core").is_dir():
+    if REF_ROOT is None or not (REF_ROOT / "core").is_dir():
         return False
     stamp = CORE / PATCH_STAMP
     return not stamp.exists() or stamp.read_text().strip() != PATCH_VERSION
@@ -259,6 +261,8 @@ def build_ref(jobs_hint: int = 0) -> Path:
 
 
 if __name__ == "__main__":
+    if "--reference" in sys.argv:
+        REF_ROOT = Path(sys.argv[sys.argv.index("--reference") + 1])
     if "--build-only" not in sys.argv:
         prepare()
         print("patched reference tree at", CORE)
