@@ -87,6 +87,8 @@ class ArRenderProfile(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+GUIDE_PROBE_FLOATS = 344  # AR_GUIDE_PROBE_FLOATS: Texture<4>::data_ as floats
+
 EXPORTED = [
     "ar_create", "ar_destroy", "ar_scene_set_materials", "ar_scene_set_objects", "ar_scene_set_mesh",
     "ar_scene_build", "ar_scene_stats", "ar_render", "ar_trace_closest", "ar_trace_any", "ar_last_render_stats",
@@ -97,7 +99,8 @@ EXPORTED = [
     "ar_diag_umma_gemm", "ar_diag_mlp", "ar_guide_mlp_stats", "ar_scene_set_sdf_union", "ar_scene_set_medium",
     "ar_adjoint_medium", "ar_tonemap", "ar_denoise", "ar_denoise_read", "ar_denoise_write",
     "ar_sdf_volume_add", "ar_sdf_volume_add_data", "ar_sdf_volume_read", "ar_sdf_volume_clear",
-    "ar_scene_set_build_mode", "ar_scene_build_time", "ar_scene_refit_mesh",
+    "ar_scene_set_build_mode", "ar_scene_build_time", "ar_scene_refit_mesh", "ar_guide_read", "ar_guide_write",
+    "ar_guide_read_records",
 ]
 
 _lib = None
@@ -167,6 +170,9 @@ def load() -> C.CDLL:
         "ar_scene_set_build_mode": (C.c_int, [vp, C.c_int32]),
         "ar_scene_build_time": (C.c_int, [vp, P(C.c_double)]),
         "ar_scene_refit_mesh": (C.c_int, [vp, vp, C.c_int, C.c_int, vp]),
+        "ar_guide_read": (C.c_int, [vp, P(C.c_int32), C.c_int32, vp, vp, vp]),
+        "ar_guide_write": (C.c_int, [vp, C.c_int32, vp, vp, vp, C.c_float]),
+        "ar_guide_read_records": (C.c_int, [vp, P(C.c_int32), C.c_int32, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

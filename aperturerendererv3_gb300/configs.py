@@ -169,6 +169,59 @@ def reference_cornell(light=(10.0, 10.0, 10.0)) -> list[SceneObject]:
     return objs
 
 
+def _lerp32(a, b, v) -> tuple:
+    """lerp(a, b, v) = a (1 - v) + b v in float32, per channel (core/vector.cuh:241-243)."""
+    a = np.asarray(a, np.float32)
+    b, v = np.float32(b), np.float32(v)
+    return tuple(float(x) for x in (a * (np.float32(1.0) - v) + b * v).astype(np.float32))
+
+
+GLASS_TEST_CAMERA = dict(origin=(0.0, 0.0, 1.1), direction=(0.0, 0.0, -1.0), fov=60.0)
+
+
+def glass_test_scene(position=(0.0, 0.0, 0.0), ior_strength: float = 1.0, abbe: float = 20.0,
+                     tilt: float = 0.0) -> list[SceneObject]:
+    """SceneHelper::CreateGlassTestScene (core/helper/scene_helper.h:172-258): five
+    glass spheres and three tilted glass slabs (Fresnel, refraction with Abbe
+    dispersion, Beer-Lambert absorption, total internal reflection), a small
+    spherical light and three GGX slabs; colours as color::* (core/render/color.cuh)."""
+    px, py, pz = (float(c) for c in position)
+
+    def at(x, y, z):
+        return (float(np.float32(x) + np.float32(px)), float(np.float32(y) + np.float32(py)),
+                float(np.float32(z) + np.float32(pz)))
+
+    def ior(b):
+        return _lerp32((1.0,), b, ior_strength)[0]
+
+    white, yellow, cyan = (1.0, 1.0, 1.0), (1.0, 1.0, 0.0), (0.0, 1.0, 1.0)
+    red, blue, purple = (1.0, 0.0, 0.0), (0.0, 0.0, 1.0), (1.0, 0.0, 1.0)
+    azure, orange = (0.25, 0.5, 1.0), (1.0, 0.5, 0.25)
+    ball, slab = (0.125, 0.125, 0.125), (0.125, 0.125, 0.01)
+    G = Material.CreateGlassPureColor
+    S, C = OBJECT_SPHERE, OBJECT_CUBE
+    return [
+        SceneObject(at(0.0, 0.25, 0.125), ball, G(white, ior(1.6), 1.0, abbe, tilt), (0.0, 0.0, 0.0), S),
+        SceneObject(at(0.125, 0.25, -0.125), (0.05, 0.05, 0.05), Material.CreateLight((25.0, 25.0, 25.0)),
+                    (0.0, 0.0, 0.0), S),
+        SceneObject(at(-0.25, 0.0, -0.125), ball, G(yellow, ior(1.5), 1.0, abbe, tilt), (0.0, 0.0, 0.0), S),
+        SceneObject(at(0.25, 0.0, 0.125), ball, G(cyan, ior(1.55), 1.0, abbe, tilt), (0.0, 0.0, 0.0), S),
+        SceneObject(at(0.0, 0.0, 0.0), ball, G(_lerp32(red, 1.0, 0.01), ior(1.45), 1.0, abbe, tilt), (0.0, 0.0, 0.0), S),
+        SceneObject(at(0.0, -0.25, -0.125), ball, G(_lerp32(blue, 1.0, 0.01), ior(1.5), 1.0, abbe, tilt),
+                    (0.0, 0.0, 0.0), S),
+        SceneObject(at(0.0, 0.0, 0.25), slab, G(azure, ior(1.5), 25.0, abbe, tilt), (0.0, 0.0, 0.0), C),
+        SceneObject(at(0.0, -0.25, 0.3), slab, G(_lerp32(red, 1.0, 0.25), ior(1.5), 25.0, abbe, tilt),
+                    (30.0, 0.0, 0.0), C),
+        SceneObject(at(0.0, 0.25, 0.3), slab, G(_lerp32(purple, 1.0, 0.25), ior(1.5), 25.0, abbe, tilt),
+                    (-30.0, 0.0, 0.0), C),
+        SceneObject(at(0.0, 0.0, -0.25), slab, Material.CreateGGXPureColor(orange, 0.1, 1.0, 1.0), (0.0, 0.0, 0.0), C),
+        SceneObject(at(0.0, -0.25, -0.3), slab, Material.CreateGGXPureColor(_lerp32(white, 0.0, 0.9), 0.1, 0.0, 0.5),
+                    (-30.0, 0.0, 0.0), C),
+        SceneObject(at(0.0, 0.25, -0.3), slab, Material.CreateGGXPureColor(_lerp32(white, 0.0, 0.5), 0.5, 1.0, 1.0),
+                    (30.0, 0.0, 0.0), C),
+    ]
+
+
 def random_triangles(n: int, seed: int = 1) -> np.ndarray:
     """(n, 9) float32 triangle vertices."""
     rng = np.random.default_rng(seed)

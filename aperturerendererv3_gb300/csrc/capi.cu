@@ -241,17 +241,12 @@ void free_guide(Ctx& c)
     c.pg_path_cap = 0;
 }
 
-// Voxel-guide storage: dense index table over the scene's voxel box (voxel =
-// floor(p / unit), as the reference keys its sparse volume) and a probe pool.
-ar_status ensure_guide(ar_ctx* ctx, float unit, long long npix)
+// The voxel guide's probe pool and key hash (voxel = floor(p / unit), as the
+// reference keys its sparse volume), kept while the unit stays the same.
+ar_status ensure_guide_pool(ar_ctx* ctx, float unit)
 {
     Ctx& c = ctx->c;
-    if (!(unit > 0.0f)) unit = 0.05f;
-    if (c.d_pg_keys && c.pg_unit == unit && c.ps.maskq && c.pg_path_cap == c.ps.capacity &&
-        (long long)c.gs_capacity >= AR_PG_COLLECT_DEPTH * npix)
-        return AR_OK;
-    const bool keep_probes = c.d_pg_keys && c.pg_unit == unit;
-    if (!keep_probes)
+    if (!(c.d_pg_keys && c.pg_unit == unit))
     {
         free_guide(c);
         // probe pool of 131072 probes (182 MB) and a hash at load factor <= 1/4
@@ -277,6 +272,20 @@ ar_status ensure_guide(ar_ctx* ctx, float unit, long long npix)
         c.guide.mask = (unsigned)(slots - 1);
         c.guide.inv_unit = 1.0f / unit;
     }
+    return AR_OK;
+}
+
+// Voxel-guide storage: dense index table over the scene's voxel box (voxel =
+// floor(p / unit), as the reference keys its sparse volume) and a probe pool.
+ar_status ensure_guide(ar_ctx* ctx, float unit, long long npix)
+{
+    Ctx& c = ctx->c;
+    if (!(unit > 0.0f)) unit = 0.05f;
+    if (c.d_pg_keys && c.pg_unit == unit && c.ps.maskq && c.pg_path_cap == c.ps.capacity &&
+        (long long)c.gs_capacity >= AR_PG_COLLECT_DEPTH * npix)
+        return AR_OK;
+    ar_status st = ensure_guide_pool(ctx, unit);
+    if (st != AR_OK) return st;
     // per-path collection slots use the wavefront buffers' stride; the record
     // buffer holds a whole frame (up to AR_PG_COLLECT_DEPTH records per pixel)
     const int wave_cap = c.ps.capacity;
@@ -1502,6 +1511,158 @@ ar_status ar_guide_reset(ar_ctx* ctx, int32_t* n_probes)
     if (n_probes) *n_probes = guide_probe_count(c);
     free_guide(c);
     free_mlp(c);
+    return AR_OK;
+}
+
+// Probe set of the voxel guide, ordered by probe index: keys as pg::GetVoxelGrid
+// returns them (x, y, z, face), the Texture<4> texels and counts.
+ar_status ar_guide_read(ar_ctx* ctx, int32_t* n, int32_t capacity, int32_t* keys, float* texels, uint64_t* counts)
+{
+    if (!ctx || !n) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
+    const int np = c.d_pg_keys ? guide_probe_count(c) : 0;
+    *n = np;
+    if (!keys && !texels && !counts) return AR_OK;
+    if (capacity < np) return fail(ctx, AR_ERR_INVALID, "guide_read: capacity below the probe count");
+    if (keys)
+    {
+        std::vector<unsigned long long> hk((size_t)c.pg_hash_slots);
+        std::vector<int> hv((size_t)c.pg_hash_slots);
+        AR_CUDA(ctx, cudaMemcpy(hk.data(), c.d_pg_keys, hk.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        AR_CUDA(ctx, cudaMemcpy(hv.data(), c.d_pg_vals, hv.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        const int lim = 1 << (AR_PG_KEY_BITS - 1);
+        const unsigned long long m = (1ull << AR_PG_KEY_BITS) - 1ull;
+        for (int i = 0; i < 4 * np; ++i) keys[i] = INT32_MIN;
+        for (size_t sl = 0; sl < hk.size(); ++sl)
+        {
+            const unsigned long long k = hk[sl];
+            const int v = hv[sl];
+            if (k == AR_PG_KEY_EMPTY || v < 0 || v >= np) continue;
+            keys[4 * v + 0] = (int)(k & m) - lim;
+            keys[4 * v + 1] = (int)((k >> AR_PG_KEY_BITS) & m) - lim;
+            keys[4 * v + 2] = (int)((k >> (2 * AR_PG_KEY_BITS)) & m) - lim;
+            keys[4 * v + 3] = (int)(k >> (3 * AR_PG_KEY_BITS));
+        }
+    }
+    if (texels || counts)
+    {
+        std::vector<Probe> pr((size_t)np);
+        if (np) AR_CUDA(ctx, cudaMemcpy(pr.data(), c.d_pg_probes, pr.size() * sizeof(Probe), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < np; ++i)
+        {
+            if (texels) std::memcpy(texels + (size_t)i * AR_GUIDE_PROBE_FLOATS, pr[i].data, AR_GUIDE_PROBE_FLOATS * sizeof(float));
+            if (counts) counts[i] = pr[i].count;
+        }
+    }
+    return AR_OK;
+}
+
+// Replaces the probe set (keys, texels and counts as ar_guide_read gives them)
+// and sets the voxel unit; the next guided ar_render with the same guide_unit
+// samples from these probes and keeps learning into them.
+ar_status ar_guide_write(ar_ctx* ctx, int32_t n, const int32_t* keys, const float* texels, const uint64_t* counts,
+                         float unit)
+{
+    if (!ctx || n < 0 || (n > 0 && (!keys || !texels || !counts))) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    if (!(unit > 0.0f)) unit = 0.05f;
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
+    ar_status st = ensure_guide_pool(ctx, unit);
+    if (st != AR_OK) return st;
+    if (n > c.pg_capacity) return fail(ctx, AR_ERR_INVALID, "guide_write: more probes than the pool holds");
+    std::vector<unsigned long long> hk((size_t)c.pg_hash_slots, AR_PG_KEY_EMPTY);
+    std::vector<int> hv((size_t)c.pg_hash_slots, -1);
+    for (int i = 0; i < n; ++i)
+    {
+        const unsigned long long k = guide_pack(VoxelKey{keys[4 * i], keys[4 * i + 1], keys[4 * i + 2], keys[4 * i + 3]});
+        if (k == AR_PG_KEY_EMPTY) return fail(ctx, AR_ERR_INVALID, "guide_write: key out of range");
+        unsigned sl = guide_hash(k) & c.guide.mask;
+        int probe = 0;
+        for (; probe < AR_PG_HASH_PROBES; ++probe)
+        {
+            if (hk[sl] == k) return fail(ctx, AR_ERR_INVALID, "guide_write: duplicate key");
+            if (hk[sl] == AR_PG_KEY_EMPTY) break;
+            sl = (sl + 1u) & c.guide.mask;
+        }
+        if (probe == AR_PG_HASH_PROBES) return fail(ctx, AR_ERR_INVALID, "guide_write: hash chain too long");
+        hk[sl] = k;
+        hv[sl] = i;
+    }
+    std::vector<Probe> pr((size_t)n);
+    for (int i = 0; i < n; ++i)
+    {
+        pr[i] = Probe{};
+        std::memcpy(pr[i].data, texels + (size_t)i * AR_GUIDE_PROBE_FLOATS, AR_GUIDE_PROBE_FLOATS * sizeof(float));
+        pr[i].count = counts[i];
+    }
+    AR_CUDA(ctx, cudaMemcpy(c.d_pg_keys, hk.data(), hk.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    AR_CUDA(ctx, cudaMemcpy(c.d_pg_vals, hv.data(), hv.size() * sizeof(int), cudaMemcpyHostToDevice));
+    AR_CUDA(ctx, cudaMemset(c.d_pg_probes, 0, (size_t)c.pg_capacity * sizeof(Probe)));
+    AR_CUDA(ctx, cudaMemset(c.d_pg_temp, 0, (size_t)c.pg_capacity * sizeof(Probe)));
+    if (n) AR_CUDA(ctx, cudaMemcpy(c.d_pg_probes, pr.data(), pr.size() * sizeof(Probe), cudaMemcpyHostToDevice));
+    const int meta[4] = {n, 0, 0, 0};
+    AR_CUDA(ctx, cudaMemcpy(c.d_pg_meta, meta, sizeof(meta), cudaMemcpyHostToDevice));
+    c.guide.probe_count = n > 0 ? 1 : 0;
+    return AR_OK;
+}
+
+// Radiance records of the last guided frame, in the order the kernels wrote
+// them: key (x, y, z, face), direction, XYZ radiance.
+ar_status ar_guide_read_records(ar_ctx* ctx, int32_t* n, int32_t capacity, int32_t* keys, float* dirs,
+                                float* radiance)
+{
+    if (!ctx || !n) return AR_ERR_INVALID;
+    Ctx& c = ctx->c;
+    AR_CUDA(ctx, cudaSetDevice(c.device));
+    AR_CUDA(ctx, cudaStreamSynchronize(c.stream));
+    int meta[4] = {0, 0, 0, 0};
+    if (c.d_pg_meta) AR_CUDA(ctx, cudaMemcpy(meta, c.d_pg_meta, sizeof(meta), cudaMemcpyDeviceToHost));
+    const int nr = std::min(meta[1], c.gs.capacity);
+    *n = nr;
+    if (!keys && !dirs && !radiance) return AR_OK;
+    if (capacity < nr) return fail(ctx, AR_ERR_INVALID, "guide_read_records: capacity below the record count");
+    std::vector<unsigned long long> k((size_t)nr);
+    std::vector<float4> d((size_t)nr), r((size_t)nr);
+    if (nr)
+    {
+        AR_CUDA(ctx, cudaMemcpy(k.data(), c.gs.key, k.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        AR_CUDA(ctx, cudaMemcpy(d.data(), c.gs.dir, d.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        AR_CUDA(ctx, cudaMemcpy(r.data(), c.gs.radiance, r.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    }
+    const int lim = 1 << (AR_PG_KEY_BITS - 1);
+    const unsigned long long m = (1ull << AR_PG_KEY_BITS) - 1ull;
+    for (int i = 0; i < nr; ++i)
+    {
+        if (keys)
+        {
+            if (k[i] == AR_PG_KEY_EMPTY)
+            {
+                keys[4 * i] = keys[4 * i + 1] = keys[4 * i + 2] = keys[4 * i + 3] = INT32_MIN;
+            }
+            else
+            {
+                keys[4 * i + 0] = (int)(k[i] & m) - lim;
+                keys[4 * i + 1] = (int)((k[i] >> AR_PG_KEY_BITS) & m) - lim;
+                keys[4 * i + 2] = (int)((k[i] >> (2 * AR_PG_KEY_BITS)) & m) - lim;
+                keys[4 * i + 3] = (int)(k[i] >> (3 * AR_PG_KEY_BITS));
+            }
+        }
+        if (dirs)
+        {
+            dirs[3 * i] = d[i].x;
+            dirs[3 * i + 1] = d[i].y;
+            dirs[3 * i + 2] = d[i].z;
+        }
+        if (radiance)
+        {
+            radiance[3 * i] = r[i].x;
+            radiance[3 * i + 1] = r[i].y;
+            radiance[3 * i + 2] = r[i].z;
+        }
+    }
     return AR_OK;
 }
 

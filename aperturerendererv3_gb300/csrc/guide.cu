@@ -138,6 +138,8 @@ cudaError_t launch_guide_update(Ctx& c, long long* launches)
     k_pg_claim<<<sms * 4, 256, 0, s>>>(c.gs, c.d_pg_keys, c.d_pg_vals, c.guide.mask, c.d_pg_meta, c.pg_capacity);
     k_pg_accumulate<<<sms * 4, 256, 0, s>>>(c.gs, c.guide, c.d_pg_temp);
     k_pg_merge<<<sms * 8, 256, 0, s>>>(c.d_pg_probes, c.d_pg_temp, c.d_pg_meta, c.pg_capacity);
+    // the frame's record count stays readable (ar_guide_read_records) after the reset
+    cudaMemcpyAsync(&c.d_pg_meta[1], c.gs.count, sizeof(int), cudaMemcpyDeviceToDevice, s);
     cudaMemsetAsync(c.gs.count, 0, sizeof(int), s);
     if (launches) *launches += 3;
     return cudaGetLastError();

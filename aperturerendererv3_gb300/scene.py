@@ -578,6 +578,40 @@ class SceneRenderer:
         check(self._ctx, self._lib.ar_guide_stats(self._ctx, C.byref(n), C.byref(cap)))
         return n.value, cap.value
 
+    def guide_probes(self) -> dict:
+        """The voxel guide's probes, by probe index: keys (n, 4) int32 (voxel x, y, z,
+        face), texels (n, 86, 4) float32 (Texture<4>::data_), counts (n,) uint64."""
+        n = C.c_int32()
+        check(self._ctx, self._lib.ar_guide_read(self._ctx, C.byref(n), 0, None, None, None))
+        k = np.zeros((n.value, 4), np.int32)
+        t = np.zeros((n.value, _lib.GUIDE_PROBE_FLOATS // 4, 4), np.float32)
+        c = np.zeros(n.value, np.uint64)
+        check(self._ctx, self._lib.ar_guide_read(self._ctx, C.byref(n), n.value, k.ctypes.data, t.ctypes.data,
+                                                 c.ctypes.data))
+        return {"keys": k, "texels": t, "counts": c}
+
+    def set_guide_probes(self, keys, texels, counts, unit: float = 0.0) -> None:
+        """Replaces the voxel guide's probes (the layout guide_probes returns)."""
+        k = np.ascontiguousarray(keys, np.int32).reshape(-1, 4)
+        t = np.ascontiguousarray(texels, np.float32).reshape(len(k), -1)
+        c = np.ascontiguousarray(counts, np.uint64).reshape(len(k))
+        assert t.shape[1] == _lib.GUIDE_PROBE_FLOATS
+        self.build()
+        check(self._ctx, self._lib.ar_guide_write(self._ctx, len(k), k.ctypes.data, t.ctypes.data, c.ctypes.data,
+                                                  float(unit)))
+
+    def guide_records(self) -> dict:
+        """Radiance records of the last guided frame: keys (n, 4) int32, dirs (n, 3),
+        radiance (n, 3) XYZ, in the order the kernels emitted them."""
+        n = C.c_int32()
+        check(self._ctx, self._lib.ar_guide_read_records(self._ctx, C.byref(n), 0, None, None, None))
+        k = np.zeros((n.value, 4), np.int32)
+        d = np.zeros((n.value, 3), np.float32)
+        r = np.zeros((n.value, 3), np.float32)
+        check(self._ctx, self._lib.ar_guide_read_records(self._ctx, C.byref(n), n.value, k.ctypes.data,
+                                                         d.ctypes.data, r.ctypes.data))
+        return {"keys": k, "dirs": d, "radiance": r}
+
     def mlp_stats(self) -> tuple[int, float]:
         """MLP guide: (training steps taken, loss sum of the last step)."""
         n, loss = C.c_int32(), C.c_float()

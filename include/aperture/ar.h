@@ -345,6 +345,29 @@ ar_status ar_guide_stats(ar_ctx* ctx, int32_t* n_probes, int32_t* capacity);
 /* MLP guide: training steps taken and the loss sum of the last one. */
 ar_status ar_guide_mlp_stats(ar_ctx* ctx, int32_t* steps, float* last_loss);
 
+/* The voxel guide's probe set (the reference keeps it in the SCENE_PROBES /
+ * INDIRECT_INDEX_VOLUME device symbols, core/render/render.cuh:43-50, that
+ * SceneRenderer::UpdatePathGuidingSample fills, core/scene.cu:409-570).
+ * Probes are ordered by probe index.  keys: 4 int32 per probe, the
+ * (voxel x, y, z, face) that pg::GetVoxelGrid returns
+ * (core/guiding/guiding_bin.cuh:109-114); texels: AR_GUIDE_PROBE_FLOATS floats
+ * per probe, Texture<4>::data_ (86 float4: 8x8 leaf, 4x4, 2x2, 1x1 mips, pad,
+ * core/guiding/octahedron.cuh:203-240); counts: Texture<4>::count_.
+ * ar_guide_read: *n receives the probe count; NULL buffers query it only.
+ * ar_guide_write: replaces the probe set and the voxel unit (0 = 0.05); a
+ * guided ar_render with the same guide_unit then samples these probes and
+ * keeps learning into them. */
+#define AR_GUIDE_PROBE_FLOATS 344
+ar_status ar_guide_read(ar_ctx* ctx, int32_t* n, int32_t capacity, int32_t* keys, float* texels, uint64_t* counts);
+ar_status ar_guide_write(ar_ctx* ctx, int32_t n, const int32_t* keys, const float* texels, const uint64_t* counts,
+                         float unit);
+/* Radiance records of the last guided frame (pg::PathGuidingSample,
+ * core/guiding/guiding.cuh:22-32, as CalculateRadiance writes them,
+ * core/render/render.cuh:909-963), in the order the kernels emitted them:
+ * key (4 int32, as above), direction (3 floats), XYZ radiance (3 floats). */
+ar_status ar_guide_read_records(ar_ctx* ctx, int32_t* n, int32_t capacity, int32_t* keys, float* dirs,
+                                float* radiance);
+
 ar_status ar_get_error_word(ar_ctx* ctx, uint32_t* word);
 ar_status ar_clear_error_word(ar_ctx* ctx);
 const char* ar_last_error(ar_ctx* ctx);

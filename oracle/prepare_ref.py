@@ -147,6 +147,12 @@ def patch_tree() -> None:
     _sub(cfg, r"#define BVH_PACK_NODE", "// #define BVH_PACK_NODE")
     _sub(cfg, r"#define MAX_TRACING_DEPTH 1000",
          "inline int REF_MAX_TRACING_DEPTH = 1000;\n#define MAX_TRACING_DEPTH (REF_MAX_TRACING_DEPTH)")
+    # runtime voxel unit of the guide (the reference compiles in 0.05,
+    # core/config.cuh:43, core/guiding/guiding_bin.cuh:102-107)
+    _sub(CORE / "guiding" / "guiding_bin.cuh", r"constexpr float invUnit = 1\.0f / PATH_GUIDING_RESOLUTION_UNIT;",
+         "const float invUnit = REF_PG_INV_UNIT;")
+    _sub(cfg, r"#define PATH_GUIDING_RESOLUTION_UNIT 0\.05\n",
+         "#define PATH_GUIDING_RESOLUTION_UNIT 0.05\ninline float REF_PG_INV_UNIT = 1.0f / PATH_GUIDING_RESOLUTION_UNIT;\n")
 
     # (6) deterministic transcendentals everywhere in the copied tree.
     fn_re = re.compile(r"\b(" + "|".join(MATH_FUNCS) + r")\s*\(")
@@ -209,7 +215,7 @@ def patch_tree() -> None:
 
 
 # bump when patch_tree() changes, so an existing patched copy is redone
-PATCH_VERSION = "4"
+PATCH_VERSION = "5"
 PATCH_STAMP = ".ar_patch_version"
 
 

@@ -16,6 +16,14 @@
 //           RenderCamera (core/scene.cu:135-189), OpenMP over pixels;
 //           optionally with the denoiser's per-pixel records
 //           (denoise::RecordScreenGBuffer / RecordScreenStatisticBuffer)
+//   render  with params.guide: CalculateRadiance<true, NEE, true> over a given
+//           voxel-guide probe set, also returning its radiance records
+//           (core/render/render.cuh:553-638, 909-963)
+//   pgupdate one probe update over given records (core/scene.cu:409-570,
+//           core/guiding/guiding.cuh:373-517), kernel loop bodies restated
+//           around the reference's own probe functions
+//   tonemap the per-pixel display transform of Camera::RenderToFile with the
+//           reference's tone curves (core/camera.cu:64-89, core/tonemap.cuh)
 //   denoise the loop of denoise::Bilateral16x16<7> (core/denoise/denoise.cuh:
 //           360-443) per output pixel, calling the reference's weight,
 //           t-test and sample transforms
@@ -30,12 +38,14 @@
 #include <string>
 #include <set>
 #include <chrono>
+#include <algorithm>
 #include <omp.h>
 
 #include "scene.hpp"
 #include "render/render.cuh"
 #include "spectrum/spectrum_lut.cuh"
 #include "denoise/denoise.cuh"
+#include "tonemap.cuh"
 // the t-quantile table the denoiser's t-test reads
 #include "denoise/t_quantile.cu"
 // explicit SDF instantiations the intersection dispatch links against
@@ -239,6 +249,8 @@ struct RenderParams
     uint64_t seed;
     int32_t first_frame, per_sample_frames;
     int32_t denoise;  // 1: record the denoiser's G-buffer and sample moments and append them
+    int32_t guide;    // 1: CalculateRadiance<true, NEE, true> over the probe set given as a 4th file
+    float guide_inv_unit;  // 1 / voxel unit of pg::GetVoxelLocation (the reference's 1 / 0.05 = 20)
 };
 // Plain per-pixel layouts of the denoiser records (40 bytes each), shared with
 // the GPU library's ar_denoise_read / ar_denoise_write.
@@ -386,7 +398,179 @@ static void collect_cells(float3 rgb, std::set<uint64_t>& pts)
             }
 }
 
-static int cmd_render(const char* scene_path, const char* params_path, const char* out_path)
+// ---------------------------------------------------------------- probes
+// Probe-set file: int32 n; n x int4 key (pg::GetVoxelGrid: voxel xyz, face);
+// n x Octahedron::data_ (totalPixelCountWithPad_ x float4); n x uint64 count_.
+struct ProbeSet
+{
+    std::vector<int4> keys;
+    std::vector<Octahedron> probes;
+};
+
+static ProbeSet read_probes(const std::vector<char>& b, size_t* at_io)
+{
+    constexpr int ALL = Octahedron::totalPixelCountWithPad_;
+    size_t at = *at_io;
+    if (b.size() < at + 4) die("bad probe file");
+    const int n = *reinterpret_cast<const int32_t*>(b.data() + at);
+    at += 4;
+    if (n < 0 || b.size() < at + (size_t)n * (16 + ALL * 16 + 8)) die("bad probe file (size)");
+    ProbeSet ps;
+    ps.keys.resize(n);
+    ps.probes.resize(n);
+    memcpy(ps.keys.data(), b.data() + at, (size_t)n * 16);
+    at += (size_t)n * 16;
+    for (int i = 0; i < n; ++i)
+    {
+        memcpy(ps.probes[i].data_, b.data() + at, ALL * 16);
+        at += ALL * 16;
+    }
+    for (int i = 0; i < n; ++i)
+    {
+        memcpy(&ps.probes[i].count_, b.data() + at, 8);
+        at += 8;
+    }
+    *at_io = at;
+    return ps;
+}
+
+static void write_probes(const char* path, const ProbeSet& ps)
+{
+    constexpr int ALL = Octahedron::totalPixelCountWithPad_;
+    const int32_t n = (int32_t)ps.keys.size();
+    write_file(path, &n, 4);
+    write_file(path, ps.keys.data(), (size_t)n * 16, true);
+    for (int i = 0; i < n; ++i) write_file(path, ps.probes[i].data_, ALL * 16, true);
+    for (int i = 0; i < n; ++i) write_file(path, &ps.probes[i].count_, 8, true);
+}
+
+// The index volume QueryProbe reads (core/render/render.cuh:434-458): a dense
+// box over the keys' voxels, PATH_GUIDING_FACE_COUNT entries per voxel,
+// SIZE_T_MAX where no probe is allocated -- what UpdatePathGuidingSample grows
+// (core/scene.cu:440-500).
+static std::vector<size_t> index_volume(const ProbeSet& ps, int3* start, int3* end, int3* size)
+{
+    if (ps.keys.empty())
+    {
+        *start = *end = *size = int3{0, 0, 0};
+        return {};
+    }
+    int3 lo{INT32_MAX, INT32_MAX, INT32_MAX}, hi{INT32_MIN, INT32_MIN, INT32_MIN};
+    for (const int4& k : ps.keys)
+    {
+        lo = int3{std::min(lo.x, k.x), std::min(lo.y, k.y), std::min(lo.z, k.z)};
+        hi = int3{std::max(hi.x, k.x), std::max(hi.y, k.y), std::max(hi.z, k.z)};
+    }
+    *start = lo;
+    *end = hi;
+    *size = pg::DimsFromBoundsInclusive(lo, hi);
+    std::vector<size_t> vol((size_t)size->x * size->y * size->z * PATH_GUIDING_FACE_COUNT, SIZE_T_MAX);
+    for (size_t i = 0; i < ps.keys.size(); ++i)
+    {
+        const int4 k = ps.keys[i];
+        if (k.w < 0 || k.w >= PATH_GUIDING_FACE_COUNT) die("probe key with a bad face");
+        const size_t lin = (size_t)(k.x - lo.x) + (size_t)size->x * ((size_t)(k.y - lo.y) + (size_t)size->y * (size_t)(k.z - lo.z));
+        vol[lin * PATH_GUIDING_FACE_COUNT + (size_t)k.w] = i;
+    }
+    return vol;
+}
+
+// One probe update as SceneRenderer::UpdatePathGuidingSample runs it
+// (core/scene.cu:409-570): every record's key gets a probe (new probes start
+// zeroed), AccumulateSamplesToOctaLeafKernel's body per record in record
+// order, then MergeProbeKernel's body for every probe the frame touched
+// (core/guiding/guiding.cuh:373-517), which ends in Texture::GenerateMipmaps.
+// in: probe-set file; records file int32 n + n x {int4 key, float3 dir,
+// float3 radiance}.  out: the updated probe set (new probes after the old, in
+// key order as the reference's sorted unique grids).
+static int cmd_pgupdate(const char* probe_path, const char* rec_path, const char* out_path)
+{
+    std::vector<char> pb = read_file(probe_path);
+    size_t at = 0;
+    ProbeSet ps = read_probes(pb, &at);
+    std::vector<char> rb = read_file(rec_path);
+    const int nrec = *reinterpret_cast<const int32_t*>(rb.data());
+    struct Rec { int32_t key[4]; float dir[3]; float rad[3]; };
+    static_assert(sizeof(Rec) == 40, "record layout");
+    if (rb.size() < 4 + (size_t)nrec * sizeof(Rec)) die("bad record file");
+    std::vector<Rec> recs(nrec);
+    memcpy(recs.data(), rb.data() + 4, (size_t)nrec * sizeof(Rec));
+    // keys without a probe, sorted and unique, take the next indices
+    auto less = [](const int4& a, const int4& b) {
+        if (a.x != b.x) return a.x < b.x;
+        if (a.y != b.y) return a.y < b.y;
+        if (a.z != b.z) return a.z < b.z;
+        return a.w < b.w;
+    };
+    std::vector<int4> fresh;
+    {
+        std::vector<int4> known = ps.keys;
+        std::sort(known.begin(), known.end(), less);
+        for (const Rec& r : recs)
+        {
+            const int4 k{r.key[0], r.key[1], r.key[2], r.key[3]};
+            if (!std::binary_search(known.begin(), known.end(), k, less)) fresh.push_back(k);
+        }
+        std::sort(fresh.begin(), fresh.end(), less);
+        fresh.erase(std::unique(fresh.begin(), fresh.end(), [&](const int4& a, const int4& b) { return !less(a, b) && !less(b, a); }), fresh.end());
+    }
+    for (const int4& k : fresh)
+    {
+        ps.keys.push_back(k);
+        ps.probes.emplace_back();
+        memset(static_cast<void*>(&ps.probes.back()), 0, sizeof(Octahedron));
+    }
+    int3 vs, ve, vd;
+    std::vector<size_t> vol = index_volume(ps, &vs, &ve, &vd);
+    const pg::ProbeIndexLookup lookup{vol.data(), vs, vd};
+    std::vector<Octahedron> temp(ps.probes.size());
+    for (auto& t : temp) memset(static_cast<void*>(&t), 0, sizeof(Octahedron));
+    constexpr int res = Octahedron::resolution_;
+    for (const Rec& r : recs)
+    {
+        const size_t realIndex = lookup(int4{r.key[0], r.key[1], r.key[2], r.key[3]});
+        if (realIndex == SIZE_T_MAX) continue;
+        const float3 dir = normalize(float3{r.dir[0], r.dir[1], r.dir[2]});
+        const int2 pix = pg::DirectionToLeafPixel(dir);
+        Octahedron& cp = temp[realIndex];
+        float4* leaf = &cp.data_[0];
+        const int idx = pix.y * res + pix.x;
+        const float J = pg::JacobianUVToOctahedronSphereDirection(dir);
+        const float3 rj = float3{r.rad[0], r.rad[1], r.rad[2]} * J;
+        leaf[idx].x += rj.x;
+        leaf[idx].y += rj.y;
+        leaf[idx].z += rj.z;
+        cp.count_ += 1ull;
+    }
+    constexpr int N = Octahedron::resolution2_;
+    for (size_t p = 0; p < ps.probes.size(); ++p)
+    {
+        const Octahedron& probeNew = temp[p];
+        const unsigned long long countNew = probeNew.count_;
+        if (countNew == 0ull) continue;
+        Octahedron& probeOld = ps.probes[p];
+        const unsigned long long countOld = probeOld.count_;
+        const double invDen = 1.0 / static_cast<double>(countOld + countNew);
+        const double alpha = static_cast<double>(countOld) * invDen;
+        for (int k = 0; k < N; ++k)
+        {
+            float4 oldValue = probeOld.data_[k];
+            const float4 newValue = probeNew.data_[k];
+            oldValue.x = static_cast<float>(static_cast<double>(oldValue.x) * alpha + static_cast<double>(newValue.x) * invDen);
+            oldValue.y = static_cast<float>(static_cast<double>(oldValue.y) * alpha + static_cast<double>(newValue.y) * invDen);
+            oldValue.z = static_cast<float>(static_cast<double>(oldValue.z) * alpha + static_cast<double>(newValue.z) * invDen);
+            probeOld.data_[k] = oldValue;
+        }
+        probeOld.count_ = std::min(PATH_GUIDING_PROBE_MAX_STORE_COUNT, countOld + countNew);
+        probeOld.GenerateMipmaps();
+    }
+    write_probes(out_path, ps);
+    printf("{\"probes\": %zu, \"new\": %zu, \"records\": %d}\n", ps.probes.size(), fresh.size(), nrec);
+    return 0;
+}
+
+static int cmd_render(const char* scene_path, const char* params_path, const char* out_path,
+                      const char* probe_path)
 {
     std::vector<char> sb = read_file(scene_path);
     std::vector<char> pb = read_file(params_path);
@@ -427,7 +611,9 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
         sdf::REF_HOST_SDF_COUNT = (uint32_t)vol_info.size();
     }
     RenderParams prm;
-    memcpy(&prm, pb.data(), sizeof(prm));
+    memset(&prm, 0, sizeof(prm));
+    memcpy(&prm, pb.data(), std::min(pb.size(), sizeof(prm)));
+    if (!(prm.guide_inv_unit > 0.0f)) prm.guide_inv_unit = REF_PG_INV_UNIT;
 
     // scene objects through the reference's own constructors
     std::vector<SceneObject> objs;
@@ -538,11 +724,33 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
     SPECTRUM_LUT_LAMBDA = lam.data();
     REF_MAX_TRACING_DEPTH = prm.max_depth;
     SCENE_PROBES_COUNTS = 0;
+    // voxel guide: the given probe set behind the index volume QueryProbe reads
+    ProbeSet guide_set;
+    std::vector<size_t> guide_vol;
+    if (prm.guide)
+    {
+        if (!probe_path) die("guided render without a probe file");
+        std::vector<char> gb = read_file(probe_path);
+        size_t at = 0;
+        guide_set = read_probes(gb, &at);
+        int3 vs, ve, vd;
+        guide_vol = index_volume(guide_set, &vs, &ve, &vd);
+        SCENE_PROBES = guide_set.probes.data();
+        SCENE_PROBES_COUNTS = guide_set.probes.size();
+        INDIRECT_VOLUME_START = vs;
+        INDIRECT_VOLUME_END = ve;
+        INDIRECT_VOLUME_SIZE = vd;
+        INDIRECT_INDEX_VOLUME = guide_vol.data();
+        REF_PG_INV_UNIT = prm.guide_inv_unit;
+    }
+    // radiance records of the per-sample frames: PATH_GUIDING_COLLECT_DEPTH per pixel sample
 
     const int W = prm.width, H = prm.height;
     const size_t npix = (size_t)W * H;
     std::vector<double> sums(npix * 3, 0.0);
     std::vector<float> per_sample((size_t)prm.per_sample_frames * npix * 3, 0.0f);
+    std::vector<pg::PathGuidingSample> records(prm.guide ? (size_t)prm.per_sample_frames * npix * PATH_GUIDING_COLLECT_DEPTH : 0);
+    std::vector<pg::PathGuidingSample> scratch_records(prm.guide ? (size_t)npix * PATH_GUIDING_COLLECT_DEPTH : 0);
     const float3 camO = f3(prm.cam_origin), camD = f3(prm.cam_dir);
     const float FOV = prm.fov_deg * 3.1415926f / 180.0f;
     const float aspect = static_cast<float>(W) / fmaxf(1.0f, static_cast<float>(H));
@@ -579,7 +787,15 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
             float4 r;
             denoise::ScreenGBuffer* gbp = prm.denoise ? &gbuf[p] : nullptr;
             denoise::ScreenStatisticsBuffer* stp = prm.denoise ? &stats[p] : nullptr;
-            if (prm.use_nee) r = CalculateRadiance<true, true, false>(&seed, camO, rayDirection, nullptr, gbp, stp);
+            if (prm.guide)
+            {
+                pg::PathGuidingSample* rec = s < prm.per_sample_frames
+                                                 ? &records[((size_t)s * npix + p) * PATH_GUIDING_COLLECT_DEPTH]
+                                                 : &scratch_records[(size_t)p * PATH_GUIDING_COLLECT_DEPTH];
+                if (prm.use_nee) r = CalculateRadiance<true, true, true>(&seed, camO, rayDirection, rec, gbp, stp);
+                else r = CalculateRadiance<true, false, true>(&seed, camO, rayDirection, rec, gbp, stp);
+            }
+            else if (prm.use_nee) r = CalculateRadiance<true, true, false>(&seed, camO, rayDirection, nullptr, gbp, stp);
             else r = CalculateRadiance<true, false, false>(&seed, camO, rayDirection, nullptr, gbp, stp);
             float3 result = make_f3(r);
             result = max(float3{0}, result);
@@ -598,6 +814,24 @@ static int cmd_render(const char* scene_path, const char* params_path, const cha
     auto t1 = std::chrono::steady_clock::now();
     write_file(out_path, sums.data(), sums.size() * 8);
     if (prm.per_sample_frames) write_file(out_path, per_sample.data(), per_sample.size() * 4, true);
+    if (prm.guide)
+    {
+        // per pixel sample, PATH_GUIDING_COLLECT_DEPTH x {int32 valid, int4 key, float3 dir, float3 radiance}
+        std::vector<int32_t> flat(records.size() * 11);
+        for (size_t i = 0; i < records.size(); ++i)
+        {
+            const pg::PathGuidingSample& g = records[i];
+            int32_t* o = &flat[i * 11];
+            o[0] = g.valid_ ? 1 : 0;
+            o[1] = g.voxelGrid_.x;
+            o[2] = g.voxelGrid_.y;
+            o[3] = g.voxelGrid_.z;
+            o[4] = g.voxelGrid_.w;
+            memcpy(&o[5], &g.radianceDirection_, 12);
+            memcpy(&o[8], &g.radiance_, 12);
+        }
+        write_file(out_path, flat.data(), flat.size() * 4, true);
+    }
     if (prm.denoise)
     {
         std::vector<PlainGBuf> pg(npix);
@@ -731,6 +965,36 @@ static int cmd_guide(const char* in_path, const char* out_path)
     return 0;
 }
 
+// ---------------------------------------------------------------- tonemap
+// in: int32 n, float exposure, int32 tone (0 ACES, 1 Gamma, 2 linear), n x float3 XYZ.
+// out: n x RGBA8, the per-pixel body of Camera::RenderToFile (core/camera.cu:
+// 64-89): tonemapFunction(XYZ2SRGBLinearD65(value * exp)), saturate, x 255
+// truncated, alpha 255; the tone curves are core/tonemap.cuh's.
+static int cmd_tonemap(const char* in_path, const char* out_path)
+{
+    std::vector<char> b = read_file(in_path);
+    if (b.size() < 12) die("bad tonemap input");
+    const int n = *reinterpret_cast<const int32_t*>(b.data());
+    const float exposure = *reinterpret_cast<const float*>(b.data() + 4);
+    const int tone = *reinterpret_cast<const int32_t*>(b.data() + 8);
+    if (n < 0 || b.size() < 12 + (size_t)n * 12) die("bad tonemap input (size)");
+    const float* xyz = reinterpret_cast<const float*>(b.data() + 12);
+    std::vector<unsigned char> out((size_t)n * 4);
+    for (int i = 0; i < n; ++i)
+    {
+        const float3 value = float3{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]} * exposure;
+        const float3 lin = XYZ2SRGBLinearD65(value);
+        float3 res = tone == 0 ? ACES(lin) : (tone == 1 ? Gamma(lin) : lin);
+        res = saturate(res);
+        out[4 * (size_t)i] = static_cast<unsigned char>(res.x * 255);
+        out[4 * (size_t)i + 1] = static_cast<unsigned char>(res.y * 255);
+        out[4 * (size_t)i + 2] = static_cast<unsigned char>(res.z * 255);
+        out[4 * (size_t)i + 3] = static_cast<unsigned char>(255);
+    }
+    write_file(out_path, out.data(), out.size());
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 2) die("usage: ref_cpu kat | lut <lattice> <out> | trace|brute <tris> <rays> <out> | render <scene> <params> <out>");
@@ -738,7 +1002,10 @@ int main(int argc, char** argv)
     if (cmd == "kat") return cmd_kat();
     if (cmd == "lut" && argc == 4) return cmd_lut(argv[2], argv[3]);
     if ((cmd == "trace" || cmd == "brute") && argc == 5) return cmd_trace(argv[2], argv[3], argv[4], cmd == "brute");
-    if (cmd == "render" && argc == 5) return cmd_render(argv[2], argv[3], argv[4]);
+    if (cmd == "render" && argc == 5) return cmd_render(argv[2], argv[3], argv[4], nullptr);
+    if (cmd == "render" && argc == 6) return cmd_render(argv[2], argv[3], argv[4], argv[5]);
+    if (cmd == "tonemap" && argc == 4) return cmd_tonemap(argv[2], argv[3]);
+    if (cmd == "pgupdate" && argc == 5) return cmd_pgupdate(argv[2], argv[3], argv[4]);
     if (cmd == "guide" && argc == 4) return cmd_guide(argv[2], argv[3]);
     if (cmd == "denoise" && argc == 4) return cmd_denoise(argv[2], argv[3]);
     if (cmd == "sdfvol" && argc == 4) return cmd_sdfvol(argv[2], argv[3]);

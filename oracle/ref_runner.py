@@ -25,7 +25,11 @@ OBJ_DTYPE = np.dtype([("type", "<i4"), ("shading", "<i4"), ("center", "<f4", 3),
 VOL_DTYPE = np.dtype([("fn", "<i4"), ("params", "<f4", 4), ("dims", "<i4", 3)])
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("max_depth", "<i4"),
                          ("cam_origin", "<f4", 3), ("cam_dir", "<f4", 3), ("fov", "<f4"), ("use_nee", "<i4"),
-                         ("seed", "<u8"), ("first_frame", "<i4"), ("per_sample", "<i4"), ("denoise", "<i4")])
+                         ("seed", "<u8"), ("first_frame", "<i4"), ("per_sample", "<i4"), ("denoise", "<i4"),
+                         ("guide", "<i4"), ("guide_inv_unit", "<f4")])
+PROBE_FLOATS = 344  # Octahedron::data_ (86 float4) as floats
+# one radiance record of the guided integrator: valid, key (voxel xyz, face), direction, XYZ radiance
+GREC_DTYPE = np.dtype([("valid", "<i4"), ("key", "<i4", 4), ("dir", "<f4", 3), ("radiance", "<f4", 3)])
 # denoiser records in the driver's plain layout (the GPU library's ar_denoise_read layout)
 GBUF_DTYPE = np.dtype([("h", "<u2", 14), ("depth", "<f4"), ("valid", "<u4"), ("frames", "<u4")])
 STAT_DTYPE = np.dtype([("num", "<u4"), ("mean", "<f4", 3), ("m2n", "<f4", 3), ("m3n", "<f4", 3)])
@@ -101,27 +105,72 @@ def sdf_volume(fn: int, params, dims) -> np.ndarray:
         return np.frombuffer((td / "out.bin").read_bytes(), np.float32).reshape(dims[2], dims[1], dims[0]).copy()
 
 
+def probe_bytes(probes: dict) -> bytes:
+    """A probe set (keys (n, 4) int32, texels (n, 86, 4) float32, counts (n,) uint64) in the
+    oracle's file format."""
+    k = np.ascontiguousarray(probes["keys"], np.int32).reshape(-1, 4)
+    t = np.ascontiguousarray(probes["texels"], np.float32).reshape(len(k), PROBE_FLOATS)
+    c = np.ascontiguousarray(probes["counts"], np.uint64).reshape(len(k))
+    return np.int32(len(k)).tobytes() + k.tobytes() + t.tobytes() + c.tobytes()
+
+
+def _read_probes(raw: bytes) -> dict:
+    n = int(np.frombuffer(raw[:4], np.int32)[0])
+    at = 4
+    k = np.frombuffer(raw[at: at + 16 * n], np.int32).reshape(n, 4).copy()
+    at += 16 * n
+    t = np.frombuffer(raw[at: at + 4 * PROBE_FLOATS * n], np.float32).reshape(n, PROBE_FLOATS // 4, 4).copy()
+    at += 4 * PROBE_FLOATS * n
+    c = np.frombuffer(raw[at: at + 8 * n], np.uint64).copy()
+    return {"keys": k, "texels": t, "counts": c}
+
+
+def guide_update(probes: dict, keys, dirs, radiance) -> dict:
+    """One probe update of the reference (UpdatePathGuidingSample's accumulate and
+    merge) over the given radiance records, from the given probe set."""
+    exe = ensure_built()
+    k = np.ascontiguousarray(keys, np.int32).reshape(-1, 4)
+    rec = np.zeros(len(k), np.dtype([("key", "<i4", 4), ("dir", "<f4", 3), ("rad", "<f4", 3)]))
+    rec["key"], rec["dir"], rec["rad"] = k, np.asarray(dirs, np.float32), np.asarray(radiance, np.float32)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "probes.bin").write_bytes(probe_bytes(probes))
+        (td / "rec.bin").write_bytes(np.int32(len(rec)).tobytes() + rec.tobytes())
+        r = subprocess.run([str(exe), "pgupdate", str(td / "probes.bin"), str(td / "rec.bin"), str(td / "out.bin")],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference oracle failed: " + r.stderr)
+        return _read_probes((td / "out.bin").read_bytes())
+
+
 def render(objects, size, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
            seed=0x9E3779B97F4A7C15, first_frame=0, per_sample_frames=0, mesh=None, threads=None, denoise=False,
-           volumes=None):
+           volumes=None, guide_probes=None, guide_unit=0.05):
     """Returns (mean XYZ (H, W, 3) float64, per-sample XYZ or None, stats dict); with
     denoise=True the stats dict also holds the denoiser records under "gbuffer" and
-    "moments" ((H, W) arrays of GBUF_DTYPE / STAT_DTYPE)."""
+    "moments" ((H, W) arrays of GBUF_DTYPE / STAT_DTYPE).  With guide_probes (a probe
+    set as probe_bytes takes it) the reference's guided integrator runs over those
+    probes (voxel unit guide_unit) and the stats dict holds the radiance records of
+    the per-sample frames under "records" ((frames, H, W, 5) of GREC_DTYPE)."""
     exe = ensure_built()
     w, h = int(size[0]), int(size[1])
     prm = np.zeros(1, PARAMS_DTYPE)
+    guided = guide_probes is not None
     prm[0] = (w, h, spp, max_depth, origin, direction, fov, 1 if use_nee else 0, seed, first_frame, per_sample_frames,
-              1 if denoise else 0)
+              1 if denoise else 0, 1 if guided else 0, np.float32(1.0) / np.float32(guide_unit))
     with tempfile.TemporaryDirectory() as td:
         td = Path(td)
         (td / "scene.bin").write_bytes(scene_bytes(objects, mesh, volumes))
         (td / "params.bin").write_bytes(prm.tobytes())
+        args = [str(exe), "render", str(td / "scene.bin"), str(td / "params.bin"), str(td / "out.bin")]
+        if guided:
+            (td / "probes.bin").write_bytes(probe_bytes(guide_probes))
+            args.append(str(td / "probes.bin"))
         env = dict(os.environ)
         if threads:
             env["OMP_NUM_THREADS"] = str(threads)
         env.setdefault("OMP_PROC_BIND", "close")
-        r = subprocess.run([str(exe), "render", str(td / "scene.bin"), str(td / "params.bin"), str(td / "out.bin")],
-                           capture_output=True, text=True, env=env)
+        r = subprocess.run(args, capture_output=True, text=True, env=env)
         if r.returncode != 0:
             raise RuntimeError("reference oracle failed: " + r.stderr)
         stats = json.loads(r.stdout.strip().splitlines()[-1])
@@ -133,6 +182,11 @@ def render(objects, size, origin, direction, spp, *, fov=60.0, max_depth=1000, u
     if per_sample_frames:
         per = np.frombuffer(raw[at: at + npix * 12 * per_sample_frames], np.float32).reshape(per_sample_frames, h, w, 3)
         at += npix * 12 * per_sample_frames
+    if guided:
+        nrec = per_sample_frames * npix * 5
+        stats["records"] = np.frombuffer(raw[at: at + nrec * GREC_DTYPE.itemsize], GREC_DTYPE).reshape(
+            per_sample_frames, h, w, 5).copy()
+        at += nrec * GREC_DTYPE.itemsize
     if denoise:
         stats["gbuffer"] = np.frombuffer(raw[at: at + npix * GBUF_DTYPE.itemsize], GBUF_DTYPE).reshape(h, w).copy()
         at += npix * GBUF_DTYPE.itemsize
@@ -211,3 +265,21 @@ def luts(lattice: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     lam = np.frombuffer(raw[: 840 * 16], np.float32).reshape(840, 4)
     rgb = np.frombuffer(raw[840 * 16:], np.float32).reshape(-1, 4)
     return lam, rgb
+
+
+def tonemap(xyz, exposure: float, tone: str) -> np.ndarray:
+    """The reference's display transform (Camera::RenderToFile's pixel loop with
+    core/tonemap.cuh's curves) on float32 XYZ (H, W, 3): RGBA8 (H, W, 4)."""
+    exe = ensure_built()
+    x = np.ascontiguousarray(xyz, np.float32)
+    h, w, _ = x.shape
+    code = {"aces": 0, "gamma": 1, "linear": 2}[tone]
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "in.bin").write_bytes(np.int32(h * w).tobytes() + np.float32(exposure).tobytes() +
+                                    np.int32(code).tobytes() + x.tobytes())
+        r = subprocess.run([str(exe), "tonemap", str(td / "in.bin"), str(td / "out.bin")], capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference oracle failed: " + r.stderr)
+        return np.frombuffer((td / "out.bin").read_bytes(), np.uint8).reshape(h, w, 4).copy()

@@ -14,8 +14,10 @@ Fixtures:
   trace_small.npz        triangles, rays, and closest-hit ids / t from the
                          reference BVH traversal (ties: smallest id)
   render_*.npz           per-sample XYZ of small renders of the reference's own
-                         Cornell box and of the triangle Cornell box (first
-                         bounce and full depth) from the reference integrator
+                         Cornell box, the triangle Cornell box, a small terrain
+                         and the reference's glass test scene (first bounce and
+                         full depth) from the reference integrator
+                         (`--renders NAME ...` regenerates only those)
 """
 from __future__ import annotations
 
@@ -37,6 +39,9 @@ RENDERS = {
     "render_cornell_depth1": ("cornell_triangles", 24, 24, 2, 1),
     "render_cornell_depth8": ("cornell_triangles", 24, 24, 2, 8),
     "render_terrain_small_depth16": ("terrain_small", 24, 24, 2, 16),
+    "render_glass_depth1": ("glass_cornell", 24, 24, 2, 1),
+    "render_glass_full": ("glass_cornell", 32, 32, 4, 1000),
+    "render_glass_sky_full": ("glass_test", 24, 24, 4, 1000),
 }
 
 
@@ -46,6 +51,10 @@ def scene_by_name(name):
         return configs.reference_cornell(), None, configs.REFERENCE_CORNELL_CAMERA
     if name == "cornell_triangles":
         return configs.cornell_triangles(), None, configs.CORNELL_CAMERA
+    if name == "glass_cornell":  # the reference's glass test scene inside its Cornell box
+        return configs.reference_cornell() + configs.glass_test_scene(), None, configs.GLASS_TEST_CAMERA
+    if name == "glass_test":  # the glass test scene alone, under the sky
+        return configs.glass_test_scene(), None, configs.GLASS_TEST_CAMERA
     if name == "terrain_small":
         objs, mesh = configs.terrain_scene(res=48, n_spheres=8, seed=7)
         return objs, mesh, configs.TERRAIN_CAMERA
@@ -59,7 +68,19 @@ def trace_case(seed: int = 3, ntri: int = 6000, nray: int = 4096):
     return tris, rays
 
 
+def render_fixtures(names) -> None:
+    for name in names:
+        scene, w, h, spp, depth = RENDERS[name]
+        objs, mesh, cam = scene_by_name(scene)
+        mean, per, _ = rr.render(objs, (w, h), cam["origin"], cam["direction"], spp, fov=cam["fov"],
+                                 max_depth=depth, per_sample_frames=spp, mesh=mesh)
+        np.savez(HERE / f"{name}.npz", per_sample=per, mean=mean, scene=scene, size=(w, h), spp=spp, depth=depth)
+
+
 def main() -> None:
+    if "--renders" in sys.argv:  # only the named render fixtures
+        render_fixtures(sys.argv[sys.argv.index("--renders") + 1:])
+        return
     k = rr.kat()
     (HERE / "spectral_kat.json").write_text(json.dumps(k))
     rng = np.random.default_rng(11)
@@ -81,11 +102,7 @@ def main() -> None:
     payload = tgh.make_payload(n, seed=4)
     np.savez(HERE / "guide_probe.npz", n=n, payload=np.frombuffer(payload, np.uint8),
              ref_out=rr.guide_eval(payload, n))
-    for name, (scene, w, h, spp, depth) in RENDERS.items():
-        objs, mesh, cam = scene_by_name(scene)
-        mean, per, _ = rr.render(objs, (w, h), cam["origin"], cam["direction"], spp, fov=cam["fov"],
-                                 max_depth=depth, per_sample_frames=spp, mesh=mesh)
-        np.savez(HERE / f"{name}.npz", per_sample=per, mean=mean, scene=scene, size=(w, h), spp=spp, depth=depth)
+    render_fixtures(RENDERS)
     print("golden fixtures written to", HERE)
 
 

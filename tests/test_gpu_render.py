@@ -1,7 +1,9 @@
 """Integrator parity: the GPU wavefront integrator against the reference's own
 CalculateRadiance (core/render/render.cuh:460-999) run on the CPU with the same
 per-pixel random streams.  First-bounce radiance must agree within 1e-5
-relative per sample; full paths are compared the same way."""
+relative per sample; full paths are compared the same way, including the
+reference's glass test scene (SceneHelper::CreateGlassTestScene,
+core/helper/scene_helper.h:172-258) inside its Cornell box and under the sky."""
 import numpy as np
 import pytest
 
@@ -30,7 +32,11 @@ def close(ours, ref):
 
 @pytest.mark.parametrize("name", ["render_refcornell_depth1", "render_cornell_depth1",
                                   "render_refcornell_full", "render_cornell_depth8",
-                                  "render_terrain_small_depth16"])
+                                  "render_terrain_small_depth16",
+                                  # the reference's glass test scene: Fresnel, refraction with Abbe
+                                  # dispersion, Beer-Lambert absorption, total internal reflection
+                                  # (core/render/material.cuh:48-314)
+                                  "render_glass_depth1", "render_glass_full", "render_glass_sky_full"])
 def test_golden_per_sample_parity(cuda_device, name):
     g = np.load(GOLDEN / f"{name}.npz")
     objs, mesh, cam = scene(str(g["scene"]))
@@ -47,7 +53,8 @@ def test_golden_per_sample_parity(cuda_device, name):
 
 
 @pytest.mark.parametrize("name,size,spp,depth", [("cornell_triangles", (96, 96), 4, 8),
-                                                   ("terrain_small", (80, 45), 3, 16)])
+                                                   ("terrain_small", (80, 45), 3, 16),
+                                                   ("glass_cornell", (64, 64), 4, 1000)])
 def test_larger_render_vs_live_oracle(cuda_device, name, size, spp, depth):
     from oracle import ref_runner as rr
     if not rr.available():
