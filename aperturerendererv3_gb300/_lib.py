@@ -100,7 +100,7 @@ EXPORTED = [
     "ar_adjoint_medium", "ar_tonemap", "ar_denoise", "ar_denoise_read", "ar_denoise_write",
     "ar_sdf_volume_add", "ar_sdf_volume_add_data", "ar_sdf_volume_read", "ar_sdf_volume_clear",
     "ar_scene_set_build_mode", "ar_scene_build_time", "ar_scene_refit_mesh", "ar_guide_read", "ar_guide_write",
-    "ar_guide_read_records",
+    "ar_guide_read_records", "ar_render_frame", "ar_set_exposure",
 ]
 
 _lib = None
@@ -173,6 +173,8 @@ def load() -> C.CDLL:
         "ar_guide_read": (C.c_int, [vp, P(C.c_int32), C.c_int32, vp, vp, vp]),
         "ar_guide_write": (C.c_int, [vp, C.c_int32, vp, vp, vp, C.c_float]),
         "ar_guide_read_records": (C.c_int, [vp, P(C.c_int32), C.c_int32, vp, vp, vp]),
+        "ar_render_frame": (C.c_int, [vp, P(ArRenderParams), C.c_int32, C.c_int32, vp, vp, vp, vp, vp]),
+        "ar_set_exposure": (C.c_int, [vp, C.c_float]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -26,7 +26,7 @@ LIB = PKG / "libaperture_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["capi.cu", "render.cu", "trace.cu", "noalloc.cu", "guide.cu", "adjoint.cu", "mlp.cu", "tonemap.cu",
-              "denoise.cu", "sdfvol.cu", "bvh_gpu.cu"]
+              "denoise.cu", "sdfvol.cu", "bvh_gpu.cu", "frame.cu"]
 CPP_SOURCES = ["bvh_build.cpp"]
 
 

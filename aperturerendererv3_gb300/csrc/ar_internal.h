@@ -229,6 +229,10 @@ struct Ctx
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t order_event = nullptr;  // orders a caller's stream after the context's (ar_render_noalloc)
+    float exposure = 1.0f;               // display exposure of ar_render_frame (ar_set_exposure)
+    double* d_frame_xyz = nullptr;       // ar_render_frame: the frame's sample per pixel
+    double* d_frame_dn = nullptr;        // ar_render_frame: denoiser input and output
+    long long frame_cap = 0;             // pixels of the two buffers above
     std::string last_error;
     // host scene description
     std::vector<Material> materials;

@@ -704,6 +704,8 @@ ar_status ar_destroy(ar_ctx* ctx)
     free_dev(c.d_grad32);
     free_dev(c.d_adj);
     free_dev(c.d_grad_medium);
+    free_dev(c.d_frame_xyz);
+    free_dev(c.d_frame_dn);
     if (c.order_event) cudaEventDestroy(c.order_event);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete ctx;

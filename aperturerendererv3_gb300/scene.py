@@ -578,6 +578,35 @@ class SceneRenderer:
         check(self._ctx, self._lib.ar_guide_stats(self._ctx, C.byref(n), C.byref(cap)))
         return n.value, cap.value
 
+    def SetExposure(self, exp: float) -> None:
+        """Exposure of RenderFrame's display image (SceneRenderer::SetExposure, core/scene.hpp:97)."""
+        check(self._ctx, self._lib.ar_set_exposure(self._ctx, float(exp)))
+
+    def RenderFrame(self, hdrTarget, ldrTarget, size, cameraOrigin, cameraDirection, frameIndex: int, toneType: int,
+                    oddTarget=None, evenTarget=None, *, fov: float = 60.0, max_depth: int = 1000,
+                    use_nee: bool = True, seed: int = GLOBAL_SEED, guide: int = 0, guide_unit: float = 0.0,
+                    denoise: bool = False, stream=None) -> None:
+        """One progressive frame (SceneRenderer::Render(hdrTarget, ldrTarget, size, ...,
+        frameIndex, toneType, oddTarget, evenTarget), core/scene.hpp:109-114): renders
+        sample frameIndex of every pixel and folds it into hdrTarget (CUDA float32
+        (H, W, 3), running mean) and, if given, oddTarget / evenTarget; ldrTarget (CUDA
+        int32 (H, W) or None) receives the 0xAARRGGBB display image, toneType 0 linear,
+        1 gamma, 2 ACES."""
+        self.build()
+        p = self.params(size, cameraOrigin, cameraDirection, 1, fov, max_depth, use_nee, seed, int(frameIndex),
+                        0, False, guide, guide_unit, 0, denoise)
+
+        def ptr(t):
+            if t is None:
+                return None
+            assert t.is_cuda and t.is_contiguous()
+            return t.data_ptr()
+        w, h = int(size[0]), int(size[1])
+        assert hdrTarget.numel() == 3 * w * h and (ldrTarget is None or ldrTarget.numel() == w * h)
+        check(self._ctx, self._lib.ar_render_frame(self._ctx, C.byref(p), int(frameIndex), int(toneType),
+                                                   ptr(hdrTarget), ptr(ldrTarget), ptr(oddTarget), ptr(evenTarget),
+                                                   stream))
+
     def guide_probes(self) -> dict:
         """The voxel guide's probes, by probe index: keys (n, 4) int32 (voxel x, y, z,
         face), texels (n, 86, 4) float32 (Texture<4>::data_), counts (n,) uint64."""

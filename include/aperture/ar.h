@@ -240,6 +240,40 @@ ar_status ar_scene_stats(ar_ctx* ctx, int64_t* n_nodes, int64_t* n_slots, int32_
 ar_status ar_render(ar_ctx* ctx, const ar_render_params* params, double* out_xyz, int out_is_device,
                     float* per_sample_xyz, void* stream);
 
+/* Progressive rendering, one frame per call: SceneRenderer::Render(hdrTarget,
+ * ldrTarget, size, cameraOrigin, cameraDirection, frameIndex, toneType,
+ * oddTarget, evenTarget, radianceSampleBuffer, screenGBuffer,
+ * screenStatisticsBuffer) (core/scene.hpp:109-114, core/scene.cu:240-366).
+ * Renders one sample per pixel with frame index frame_index (the same paths as
+ * sample frame_index of ar_render; params->spp and first_frame are ignored)
+ * and folds it into the caller's DEVICE buffers:
+ *   hdr   3 floats per pixel, the float32 running mean of linear XYZ:
+ *         hdr = hdr (1 - r) + sample r with r = 1 / (1 + frame_index)
+ *         (RenderCamera, core/scene.cu:178-180), so frame 0 replaces any
+ *         finite contents (NaN or inf stay, as in the reference);
+ *   odd / even (both or neither) the same over odd / even frames at rate
+ *         1 / (1 + frame_index / 2) (core/scene.cu:181-191);
+ *   ldr   (optional) one uint32 per pixel, 0xAARRGGBB: XYZ -> linear sRGB,
+ *         times the exposure (ar_set_exposure), then tone_type
+ *         AR_FRAME_TONE_LINEAR / _GAMMA / _ACES (the reference's toneType
+ *         0 / 1 / 2, core/scene.cu:113-131), clamped, x 255 truncated.
+ * With params->guide the voxel / MLP guide learns from the frame, as the
+ * reference updates its probes after every frame; its radiance records and
+ * G-buffer live in the context (the reference's caller-owned
+ * radianceSampleBuffer / screenGBuffer / screenStatisticsBuffer).  With
+ * params->denoise_record the display image is made from the running mean
+ * filtered by ar_denoise (SceneSetting::bDenoise_, core/scene.cu:324-348).
+ * Returns after the frame is finished (the reference synchronises the device);
+ * `stream` (optional) is synchronised first. */
+#define AR_FRAME_TONE_LINEAR 0
+#define AR_FRAME_TONE_GAMMA 1
+#define AR_FRAME_TONE_ACES 2
+ar_status ar_render_frame(ar_ctx* ctx, const ar_render_params* params, int32_t frame_index, int32_t tone_type,
+                          float* hdr, uint32_t* ldr, float* odd, float* even, void* stream);
+/* Display exposure of ar_render_frame's ldr image (SceneRenderer::SetExposure,
+ * core/scene.hpp:97, core/scene.cu:752-755; default 1). */
+ar_status ar_set_exposure(ar_ctx* ctx, float exposure);
+
 /* Closest / any hit for n rays.  rays: device pointer, 8 floats per ray
  * (ox, oy, oz, tmin, dx, dy, dz, tmax), direction normalised by the caller.
  * prim_id: device int32[n] (-1 = miss).  t: device float[n] (closest only,

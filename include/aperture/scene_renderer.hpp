@@ -347,6 +347,31 @@ class SceneRenderer
         return out;
     }
 
+    // One progressive frame (SceneRenderer::Render(hdrTarget, ldrTarget, size,
+    // origin, direction, frameIndex, toneType, oddTarget, evenTarget,
+    // radianceSampleBuffer, screenGBuffer, screenStatisticsBuffer),
+    // core/scene.hpp:109-114): device buffers owned by the caller, hdrTarget the
+    // float32 running mean of XYZ, ldrTarget 0xAARRGGBB (toneType 0 linear,
+    // 1 gamma, 2 ACES).  The guide's radiance records and the denoiser's
+    // G-buffer and moments live in the context, so the last three arguments are
+    // accepted for the reference's signature and must be null.
+    void Render(float3* hdrTarget, unsigned int* ldrTarget, int2 size, float3 cameraOrigin, float3 cameraDirection,
+                int frameIndex, int toneType, float3* oddTarget = nullptr, float3* evenTarget = nullptr,
+                void* radianceSampleBuffer = nullptr, void* screenGBuffer = nullptr,
+                void* screenStatisticsBuffer = nullptr)
+    {
+        if (radianceSampleBuffer || screenGBuffer || screenStatisticsBuffer)
+            throw Error(AR_ERR_INVALID, "record buffers are kept by the context; pass null");
+        build();
+        ar_render_params p = Params(size, cameraOrigin, cameraDirection, 1);
+        p.denoise_record = denoise ? 1 : 0;
+        check(ar_render_frame(ctx_, &p, frameIndex, toneType, &hdrTarget->x, ldrTarget,
+                              oddTarget ? &oddTarget->x : nullptr, evenTarget ? &evenTarget->x : nullptr, nullptr),
+              "ar_render_frame");
+    }
+    // SceneRenderer::SetExposure (core/scene.hpp:97): exposure of the frame's display image
+    void SetExposure(float exp) { check(ar_set_exposure(ctx_, exp), "ar_set_exposure"); }
+
     // d(loss)/d(texels) into gradTexelsDevice (float64, TexelCount()) from
     // dLossDXyzDevice (float32, 3 per pixel), for the render with the same arguments.
     void Adjoint(const float* dLossDXyzDevice, double* gradTexelsDevice, int2 size, float3 cameraOrigin,

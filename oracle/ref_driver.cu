@@ -24,6 +24,7 @@
 //           around the reference's own probe functions
 //   tonemap the per-pixel display transform of Camera::RenderToFile with the
 //           reference's tone curves (core/camera.cu:64-89, core/tonemap.cuh)
+//   frametone the display kernel of the progressive Render (core/scene.cu:22-131)
 //   denoise the loop of denoise::Bilateral16x16<7> (core/denoise/denoise.cuh:
 //           360-443) per output pixel, calling the reference's weight,
 //           t-test and sample transforms
@@ -995,6 +996,36 @@ static int cmd_tonemap(const char* in_path, const char* out_path)
     return 0;
 }
 
+// ---------------------------------------------------------------- frametone
+// in: int32 n, float exposure, int32 toneType, n x float3 XYZ (the HDR running
+// mean).  out: n x uint32, the Tonemap kernel's plain branch (core/scene.cu:
+// 113-131): XYZ2SRGBLinearD65, x exposure, toneType 1 Gamma / 2 ACES, then
+// 0xff000000 | r << 16 | g << 8 | b of 255 x saturate_.
+static int cmd_frametone(const char* in_path, const char* out_path)
+{
+    std::vector<char> b = read_file(in_path);
+    if (b.size() < 12) die("bad frametone input");
+    const int n = *reinterpret_cast<const int32_t*>(b.data());
+    const float exposure_ = *reinterpret_cast<const float*>(b.data() + 4);
+    const int toneType = *reinterpret_cast<const int32_t*>(b.data() + 8);
+    if (n < 0 || b.size() < 12 + (size_t)n * 12) die("bad frametone input (size)");
+    const float* xyz = reinterpret_cast<const float*>(b.data() + 12);
+    std::vector<uint32_t> out(n);
+    for (int id = 0; id < n; ++id)
+    {
+        const float3 result = XYZ2SRGBLinearD65(float3{xyz[3 * id], xyz[3 * id + 1], xyz[3 * id + 2]});
+        float3 value = result * exposure_;
+        if (toneType == 1) value = Gamma(value);
+        else if (toneType == 2) value = ACES(value);
+        const unsigned int red = static_cast<unsigned int>(255.0f * saturate_(value.x));
+        const unsigned int green = static_cast<unsigned int>(255.0f * saturate_(value.y));
+        const unsigned int blue = static_cast<unsigned int>(255.0f * saturate_(value.z));
+        out[id] = 0xff000000 | (red << 16) | (green << 8) | blue;
+    }
+    write_file(out_path, out.data(), out.size() * 4);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 2) die("usage: ref_cpu kat | lut <lattice> <out> | trace|brute <tris> <rays> <out> | render <scene> <params> <out>");
@@ -1005,6 +1036,7 @@ int main(int argc, char** argv)
     if (cmd == "render" && argc == 5) return cmd_render(argv[2], argv[3], argv[4], nullptr);
     if (cmd == "render" && argc == 6) return cmd_render(argv[2], argv[3], argv[4], argv[5]);
     if (cmd == "tonemap" && argc == 4) return cmd_tonemap(argv[2], argv[3]);
+    if (cmd == "frametone" && argc == 4) return cmd_frametone(argv[2], argv[3]);
     if (cmd == "pgupdate" && argc == 5) return cmd_pgupdate(argv[2], argv[3], argv[4]);
     if (cmd == "guide" && argc == 4) return cmd_guide(argv[2], argv[3]);
     if (cmd == "denoise" && argc == 4) return cmd_denoise(argv[2], argv[3]);

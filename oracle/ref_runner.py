@@ -283,3 +283,20 @@ def tonemap(xyz, exposure: float, tone: str) -> np.ndarray:
         if r.returncode != 0:
             raise RuntimeError("reference oracle failed: " + r.stderr)
         return np.frombuffer((td / "out.bin").read_bytes(), np.uint8).reshape(h, w, 4).copy()
+
+
+def frame_tonemap(hdr, exposure: float, tone_type: int) -> np.ndarray:
+    """The display kernel of the reference's progressive Render (core/scene.cu:22-131,
+    plain branch) on a float32 XYZ running mean (H, W, 3): uint32 0xAARRGGBB (H, W)."""
+    exe = ensure_built()
+    x = np.ascontiguousarray(hdr, np.float32)
+    h, w, _ = x.shape
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "in.bin").write_bytes(np.int32(h * w).tobytes() + np.float32(exposure).tobytes() +
+                                    np.int32(tone_type).tobytes() + x.tobytes())
+        r = subprocess.run([str(exe), "frametone", str(td / "in.bin"), str(td / "out.bin")], capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference oracle failed: " + r.stderr)
+        return np.frombuffer((td / "out.bin").read_bytes(), np.uint32).reshape(h, w).copy()
