@@ -61,7 +61,7 @@ class ArRenderParams(C.Structure):
                 ("cam_origin", F3), ("cam_dir", F3), ("fov_deg", C.c_float), ("use_nee", C.c_int32),
                 ("seed", C.c_uint64), ("first_frame", C.c_int32), ("wave_paths", C.c_int32),
                 ("profile", C.c_int32), ("guide", C.c_int32), ("guide_unit", C.c_float),
-                ("guide_train_steps", C.c_int32), ("denoise_record", C.c_int32)]
+                ("guide_train_steps", C.c_int32), ("denoise_record", C.c_int32), ("guide_frames", C.c_int32)]
 
 
 GUIDE_NONE = 0

@@ -287,7 +287,8 @@ ar_status ensure_guide(ar_ctx* ctx, float unit, long long npix)
     ar_status st = ensure_guide_pool(ctx, unit);
     if (st != AR_OK) return st;
     // per-path collection slots use the wavefront buffers' stride; the record
-    // buffer holds a whole frame (up to AR_PG_COLLECT_DEPTH records per pixel)
+    // buffer holds a whole update window (up to AR_PG_COLLECT_DEPTH records per
+    // path of its frames; `npix` is the window's path count)
     const int wave_cap = c.ps.capacity;
     const size_t ns = (size_t)AR_PG_COLLECT_DEPTH * wave_cap;
     const size_t nrec = (size_t)AR_PG_COLLECT_DEPTH * (size_t)npix;
@@ -460,7 +461,8 @@ ar_status ensure_mlp(ar_ctx* ctx)
 }
 
 // one Adam step of the network on the frame's radiance records
-cudaError_t mlp_train_frame(Ctx& c, long long* launches)
+// Adam steps after an update window of `frames` frames: mlp_steps_per_frame per frame
+cudaError_t mlp_train_frame(Ctx& c, int frames, long long* launches)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
@@ -474,7 +476,8 @@ cudaError_t mlp_train_frame(Ctx& c, long long* launches)
         e = launch_mlp_bias_start(c.d_mlp_w32, c.gs.radiance, c.gs.count, c.stream);
         if (launches) *launches += 1;
     }
-    for (int k = 0; k < c.mlp_steps_per_frame && e == cudaSuccess; ++k)
+    const int steps = c.mlp_steps_per_frame * std::max(1, frames);
+    for (int k = 0; k < steps && e == cudaSuccess; ++k)
     {
         // each step trains on its own subset of the frame's records; the loss of the last one is kept
         e = cudaMemsetAsync(c.d_mlp_loss, 0, sizeof(float), c.stream);
@@ -1248,13 +1251,16 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     // waves, 1083 with 2^25)
     int cap = prm->wave_paths > 0 ? prm->wave_paths : AR_WAVE_PATHS_AUTO;
     if ((long long)cap > total) cap = (int)total;
-    // guided frames learn from the previous frame: waves never straddle frames
-    if (rl.guide && (long long)cap > npix) cap = (int)npix;
+    // guided frames learn after every update window of guide_frames frames:
+    // waves never straddle a window
+    if (prm->guide_frames < 0) return fail(ctx, AR_ERR_INVALID, "render: negative guide_frames");
+    const long long window = rl.guide ? npix * std::max(1, prm->guide_frames) : total;
+    if (rl.guide && (long long)cap > window) cap = (int)window;
     st = ensure_waves(ctx, cap);
     if (st != AR_OK) return st;
     if (rl.guide)
     {
-        st = ensure_guide(ctx, prm->guide_unit, npix);
+        st = ensure_guide(ctx, prm->guide_unit, std::min(window, total));
         if (st != AR_OK) return st;
     }
     if (rl.guide == 2)
@@ -1285,9 +1291,9 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     cudaError_t e = cudaSuccess;
     for (long long first = 0; first < total && e == cudaSuccess;)
     {
-        // a wave never crosses a frame boundary in guided mode
+        // a wave never crosses an update window in guided mode
         long long n_ll = std::min<long long>(cap, total - first);
-        if (rl.guide) n_ll = std::min<long long>(n_ll, npix - first % npix);
+        if (rl.guide) n_ll = std::min<long long>(n_ll, window - first % window);
         const int n = (int)n_ll;
         e = launch_render_wave(c, rl, first, n, d_samples, &launches);
         if (e == cudaSuccess) e = launch_accumulate(c, rl, first, n, c.d_accum, &launches);
@@ -1295,13 +1301,15 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
         if (e == cudaSuccess && per_sample_xyz)
             e = cudaMemcpyAsync(per_sample_xyz + 3 * first, d_samples, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, c.stream);
         first += n;
-        if (rl.guide && e == cudaSuccess && first % npix == 0)
+        if (rl.guide && e == cudaSuccess && (first % window == 0 || first == total))
         {
-            // end of a frame: learn from its radiance records (core/scene.cu:258-273); the
-            // network trains first (the probe update clears the record count)
+            // end of an update window (one frame by default): learn from its radiance
+            // records (core/scene.cu:258-273); the network trains first (the probe
+            // update clears the record count)
             if (rl.guide == 2)
             {
-                e = mlp_train_frame(c, &launches);
+                const long long frames = (first - ((first - 1) / window) * window + npix - 1) / npix;
+                e = mlp_train_frame(c, (int)frames, &launches);
                 rl.mlp_ready = c.mlp_step >= AR_MLP_WARMUP_STEPS ? 1 : 0;
             }
             if (e == cudaSuccess) e = launch_guide_update(c, &launches);

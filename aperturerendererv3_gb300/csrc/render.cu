@@ -771,7 +771,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             {
                 const float4 mq = ps.maskq[p];
                 maskq = v3(mq.x, mq.y, mq.z);
-                pgProb = guide_probability(prm.frame);
+                pgProb = guide_probability((int)ps.frame[p]);  // the path's own frame (waves may hold several)
                 const bool eligible = h.hit && !S.delta && !S.pure_light && !media.inside;
                 if constexpr (GUIDE == 2)
                 {

@@ -362,7 +362,7 @@ class SceneRenderer:
 
     def params(self, size, cameraOrigin, cameraDirection, sampleNum, fov=60.0, max_depth=1000, use_nee=True,
                seed=GLOBAL_SEED, first_frame=0, wave_paths=0, profile=False, guide=0,
-               guide_unit=0.0, guide_train_steps=0, denoise_record=False) -> ArRenderParams:
+               guide_unit=0.0, guide_train_steps=0, denoise_record=False, guide_frames=0) -> ArRenderParams:
         p = ArRenderParams()
         p.width, p.height = int(size[0]), int(size[1])
         p.spp = int(sampleNum)
@@ -379,12 +379,13 @@ class SceneRenderer:
         p.guide_unit = float(guide_unit)
         p.guide_train_steps = int(guide_train_steps)
         p.denoise_record = 1 if denoise_record else 0
+        p.guide_frames = int(guide_frames)
         return p
 
     def Render(self, size, cameraOrigin, cameraDirection, sampleNum: int = 1024, *, fov: float = 60.0,
                max_depth: int = 1000, use_nee: bool = True, seed: int = GLOBAL_SEED, first_frame: int = 0,
                per_sample: bool = False, wave_paths: int = 0, profile: bool = False, guide: int = 0,
-               guide_unit: float = 0.0, guide_train_steps: int = 0, denoise: bool = False):
+               guide_unit: float = 0.0, guide_train_steps: int = 0, denoise: bool = False, guide_frames: int = 0):
         """Mean linear XYZ per pixel, shape (height, width, 3), float64.
 
         With per_sample=True also returns every sample's XYZ, shape
@@ -393,12 +394,14 @@ class SceneRenderer:
         after every frame (and persist across calls until MarkNeedResetGuiding);
         guide=2 adds the tensor-core MLP guide, trained online on the same
         records and sampled instead of the probes once it has trained.
+        guide_frames=k > 1 updates the guide after every k frames instead of
+        every frame (the k frames share waves).
         denoise=True (SceneSetting::bDenoise_) records the denoiser's G-buffer
         and sample moments during the render (starting over at first_frame 0)
         and returns the filtered image instead of the raw mean."""
         self._build()
         p = self.params(size, cameraOrigin, cameraDirection, sampleNum, fov, max_depth, use_nee, seed, first_frame,
-                        wave_paths, profile, guide, guide_unit, guide_train_steps, denoise)
+                        wave_paths, profile, guide, guide_unit, guide_train_steps, denoise, guide_frames)
         w, h = p.width, p.height
         out = np.zeros((h, w, 3), np.float64)
         ps = np.zeros((p.spp, h, w, 3), np.float32) if per_sample else None

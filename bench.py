@@ -24,6 +24,7 @@ sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -123,6 +124,19 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def traversal_work(workload: str):
+    """Per-ray algorithmic traversal work frozen by oracle/make_traversal_work.py (or None)."""
+    p = ROOT / "profiles" / f"traversal_work_{workload}.json"
+    return json.loads(p.read_text()) if p.exists() else None
+
+
+def limiter_summary(workload: str):
+    """What bounds the closest-hit kernel, from the committed ncu summary of a small
+    case (issue activity, SIMT efficiency, L2 and DRAM throughput), or None."""
+    p = ROOT / "profiles" / f"k_extend_limiter_{workload}.json"
+    return json.loads(p.read_text()) if p.exists() else None
+
+
 def profile_traffic(workload: str):
     """DRAM bytes per extend launch from the committed ncu summary (or None)."""
     p = ROOT / "profiles" / "traffic.json"
@@ -180,20 +194,26 @@ def run_reference(args, w) -> dict:
             "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def guided_extra(r, w, cam, steps: int) -> dict:
-    """Same workload with the voxel guide learning online (one frame per spp)."""
+def guided_extra(r, w, cam, steps: int, window: int = 16) -> dict:
+    """Same workload with the voxel guide learning online: updates after every
+    frame (the reference's schedule: one frame per wave) and after every
+    `window` frames (the window's frames share waves)."""
     size, spp, depth = w["size"], w["spp"], w["depth"]
+    out = {}
+    for key, gf in (("per_frame", 1), (f"window_{window}", window)):
+        r.MarkNeedResetGuiding()
+        r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, guide=1, guide_frames=gf)
+        ms = []
+        for k in range(steps):
+            r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, guide=1,
+                     first_frame=(k + 1) * spp, guide_frames=gf)
+            ms.append(r.last_render_stats()[0])
+        n_probes, _ = r.guide_stats()
+        out[key] = {"value": size[0] * size[1] * spp / (float(np.mean(ms)) / 1e3) / 1e6, "unit": "Msamples/s",
+                    "ms_per_step": float(np.mean(ms)), "steps": steps, "probes": n_probes, "guide_frames": gf}
     r.MarkNeedResetGuiding()
-    r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, guide=1)
-    ms = []
-    for k in range(steps):
-        r.Render(size, cam["origin"], cam["direction"], spp, fov=cam["fov"], max_depth=depth, guide=1,
-                 first_frame=(k + 1) * spp)
-        ms.append(r.last_render_stats()[0])
-    n_probes, _ = r.guide_stats()
-    r.MarkNeedResetGuiding()
-    return {"value": size[0] * size[1] * spp / (float(np.mean(ms)) / 1e3) / 1e6, "unit": "Msamples/s",
-            "ms_per_step": float(np.mean(ms)), "steps": steps, "probes": n_probes}
+    out["value"], out["unit"] = out[f"window_{window}"]["value"], "Msamples/s"
+    return out
 
 
 def rel_mse(img, ref) -> float:
@@ -201,45 +221,85 @@ def rel_mse(img, ref) -> float:
     return float((((img - ref) ** 2) / (ref ** 2 + 1e-2)).sum(-1).mean())
 
 
-def guide_compare_extra(r, w, cam, ref_spp: int = 2048, chunk: int = 4) -> dict:
+def scene_extent(objs, mesh) -> float:
+    """Largest side of the mesh's bounding box (the terrain: its unit square)."""
+    v = np.asarray(mesh.vertices, np.float64).reshape(-1, 3)
+    return float((v.max(0) - v.min(0)).max())
+
+
+def guide_compare_extra(r, w, cam, objs, mesh, ref_spp: int = 2048, window: int = 8, crop: int = 64) -> dict:
     """Voxel guide vs MLP guide at equal wall time, each learning from scratch
     (training included), scored by rel-MSE against a converged plain render of
     the same view (ref_spp samples per pixel, FP64 accumulation, disjoint
-    sample streams).  Both render in calls of `chunk` frames; the voxel guide
-    renders the workload's spp, the MLP guide as many chunks as fit in the
-    voxel guide's wall time."""
-    import numpy as np
+    sample streams) whose central crop x crop pixels are checked against the
+    FP64 CPU oracle (oracle/pt64) rendering the same pixels and streams.  The
+    voxel guide uses a 64^3 grid over the scene (voxel = extent / 64).  Guided
+    renders update after every `window` frames (calls of `window` frames); the
+    voxel guide is also run with the reference's update after every frame.  The
+    voxel guide renders the workload's spp; the others as many windows as fit
+    in its wall time."""
     size, spp, depth = w["size"], w["spp"], w["depth"]
     kw = dict(fov=cam["fov"], max_depth=depth)
+    unit = scene_extent(objs, mesh) / 64.0
+    t0 = time.perf_counter()
     ref = r.Render(size, cam["origin"], cam["direction"], ref_spp, first_frame=1 << 20, **kw)
-    ref_ms = r.last_render_stats()[0]
-    out = {"reference": {"spp": ref_spp, "ms": ref_ms, "kind": "plain render, FP64 accumulation"}}
+    out = {"reference": {"spp": ref_spp, "ms": r.last_render_stats()[0], "kind": "plain render, FP64 accumulation"},
+           "voxel_unit": unit, "window_frames": window}
+    # the reference image's crop against the FP64 oracle (same pixels, same random streams)
+    x0, y0 = (size[0] - crop) // 2, (size[1] - crop) // 2
+    try:
+        from oracle import pt64
+        t1 = time.perf_counter()
+        s64 = pt64.Scene64(objs, mesh)
+        ref64 = s64.render_crop(size, (x0, y0, crop, crop), cam["origin"], cam["direction"], ref_spp,
+                                first_frame=1 << 20, **kw)
+        rc = ref[y0:y0 + crop, x0:x0 + crop]
+        rel = np.abs(rc - ref64) / np.maximum(np.abs(ref64), 1e-3)
+        out["reference"]["fp64_pin"] = {"crop": [x0, y0, crop, crop], "rel_mse": rel_mse(rc, ref64),
+                                        "max_rel_diff": float(rel.max()), "median_rel_diff": float(np.median(rel)),
+                                        "s": time.perf_counter() - t1}
+    except Exception as e:  # the pin is a check beside the number; report why it is missing
+        ref64 = None
+        out["reference"]["fp64_pin"] = {"unavailable": str(e)}
 
-    def run(mode, frames=None, budget=None, steps=0):
+    def run(mode, frames=None, budget=None, steps=0, gf=window):
         r.MarkNeedResetGuiding()
         acc, n = None, 0
-        t0 = time.perf_counter()
+        t_start = time.perf_counter()
+        chunk = gf if mode else window
         while frames is None or n < frames:
             img = r.Render(size, cam["origin"], cam["direction"], chunk, guide=mode, first_frame=n,
-                           guide_train_steps=steps, **kw)
+                           guide_train_steps=steps, guide_unit=unit, guide_frames=gf, **kw)
             acc = img * chunk if acc is None else acc + img * chunk
             n += chunk
-            if budget is not None and time.perf_counter() - t0 >= budget:
+            if budget is not None and time.perf_counter() - t_start >= budget:
                 break
-        return acc / n, n, time.perf_counter() - t0
+        return acc / n, n, time.perf_counter() - t_start
+
+    def score(img):
+        d = {"rel_mse": rel_mse(img, ref)}
+        if ref64 is not None:
+            d["rel_mse_fp64_crop"] = rel_mse(img[y0:y0 + crop, x0:x0 + crop], ref64)
+        return d
 
     vox, n_vox, t_vox = run(1, frames=spp)
-    out["voxel"] = {"spp": n_vox, "s": t_vox, "rel_mse": rel_mse(vox, ref)}
+    out["voxel"] = {"spp": n_vox, "s": t_vox, **score(vox)}
+    vox1, n1, t1 = run(1, budget=t_vox, gf=1)
+    out["voxel_per_frame"] = {"spp": n1, "s": t1, **score(vox1)}
     for key, steps_per_frame in (("mlp", 8), ("mlp_32_steps", 32)):
         mlp, n_mlp, t_mlp = run(2, budget=t_vox, steps=steps_per_frame)
         steps, loss = r.mlp_stats()
-        out[key] = {"spp": n_mlp, "s": t_mlp, "rel_mse": rel_mse(mlp, ref), "train_steps": steps,
+        out[key] = {"spp": n_mlp, "s": t_mlp, **score(mlp), "train_steps": steps,
                     "steps_per_frame": steps_per_frame, "last_loss_sum": loss}
     r.MarkNeedResetGuiding()
     plain, n_plain, t_plain = run(0, budget=t_vox)
-    out["plain"] = {"spp": n_plain, "s": t_plain, "rel_mse": rel_mse(plain, ref)}
+    out["plain"] = {"spp": n_plain, "s": t_plain, **score(plain)}
+    best_vox = min(out["voxel"]["rel_mse"], out["voxel_per_frame"]["rel_mse"])
+    best_mlp = min(out["mlp"]["rel_mse"], out["mlp_32_steps"]["rel_mse"])
     out["mlp_over_voxel"] = out["mlp"]["rel_mse"] / out["voxel"]["rel_mse"]
+    out["best_mlp_over_best_voxel"] = best_mlp / best_vox
     out["epsilon"] = 1e-2
+    out["s"] = time.perf_counter() - t0
     return out
 
 
@@ -507,6 +567,7 @@ def main() -> None:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     from aperturerendererv3_gb300 import SceneRenderer
+    from aperturerendererv3_gb300._lib import ArRenderParams
 
     objs, mesh, cam, extra_args = build_workload(args.workload)
     r = SceneRenderer(objs, device=local, mesh=mesh, **extra_args)
@@ -560,12 +621,28 @@ def main() -> None:
     for k in ("extend_rays", "extend_node_visits", "extend_prim_tests", "shadow_rays", "shadow_node_visits",
               "shadow_prim_tests"):
         prof[k] = counters[k]
-    node_b, slot_b, ray_io_b = 80, 48, 16 + 16 + 4 + 4 + 16 + 4 + 4  # node, primitive slot, per-ray state in/out
-    alg_bytes = prof["extend_node_visits"] * node_b + prof["extend_prim_tests"] * slot_b + prof["extend_rays"] * ray_io_b
+    # algorithmic bytes of the step's closest-hit traversal: the work a binary SAH
+    # BVH needs for the same rays (frozen per ray by the reference oracle:
+    # profiles/traversal_work_<workload>.json), so the figure does not move when
+    # this project's node layout or traversal changes
+    work = traversal_work(args.workload)
+    cam_rays = samples
+    bounce_rays = max(0, prof["extend_rays"] - cam_rays)
+    if work is not None:
+        alg_bytes = cam_rays * work["camera"]["bytes"] + bounce_rays * work["bounce"]["bytes"]
+        alg_def = ("binary SAH BVH work per ray frozen by the reference oracle (" + work["definition"] + "): camera "
+                   f"{work['camera']['bytes']:.1f} B x {cam_rays} rays + bounce {work['bounce']['bytes']:.1f} B x "
+                   f"{bounce_rays} rays")
+    else:  # workloads without a frozen figure: this BVH's own work
+        node_b, slot_b, ray_io_b = 80, 48, 16 + 16 + 4 + 4 + 16 + 4 + 4
+        alg_bytes = (prof["extend_node_visits"] * node_b + prof["extend_prim_tests"] * slot_b +
+                     prof["extend_rays"] * ray_io_b)
+        alg_def = "this BVH: 80 B x node visits + 48 B x primitive slots tested + 64 B ray state per ray"
     launches_ext = max(1, prof["extend_launches"])
     achieved = alg_bytes / (prof["extend_ms"] / 1e3) / 1e9
     peaks = measured_peaks()
     traffic = profile_traffic(args.workload)
+    own_bytes = prof["extend_node_visits"] * 80 + prof["extend_prim_tests"] * 48 + prof["extend_rays"] * 64
     out = {
         "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -573,7 +650,9 @@ def main() -> None:
         "config": {"workload": args.workload, "width": size[0], "height": size[1], "spp": spp, "max_depth": depth,
                    "guide": ["none", "voxel", "mlp"][args.guide], "paths_per_step": samples, "parallelism": "replicas" if world > 1 else "single-gpu",
                    "l2": "inputs larger than L2 (path state ~170 B x 33.5M paths in flight)"},
-        "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 100,
+        # per step the call reads its render parameters from host memory and copies
+        # the FP64 mean image back; the scene stays resident
+        "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": ctypes.sizeof(ArRenderParams),
                 "d2h_bytes_per_step": size[0] * size[1] * 3 * 8},
         "gpu_launches": launches,
         "clocks": clocks,
@@ -582,7 +661,9 @@ def main() -> None:
                      "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
                      "traffic": traffic,
                      "alg_bytes_per_launch": alg_bytes / launches_ext,
-                     "alg_bytes_def": "80 B x node visits + 48 B x primitive slots tested + 64 B ray state per ray"},
+                     "alg_bytes_def": alg_def,
+                     "this_bvh_bytes_per_launch": own_bytes / launches_ext,
+                     "limiter": limiter_summary(args.workload)},
         "stages_ms": {k: prof[k] for k in ("raygen_ms", "extend_ms", "shade_ms", "shadow_ms", "finalize_ms")},
         "traversal": {k: prof[k] for k in ("extend_rays", "extend_node_visits", "extend_prim_tests", "shadow_rays",
                                            "shadow_node_visits", "shadow_prim_tests")},
@@ -590,7 +671,7 @@ def main() -> None:
     if not args.no_extras:
         extras = {}
         for name, fn in (("guided_voxel", lambda: guided_extra(r, w, cam, 3)),
-                         ("guide_compare", lambda: guide_compare_extra(r, w, cam)),
+                         ("guide_compare", lambda: guide_compare_extra(r, w, cam, objs, mesh)),
                          ("adjoint", lambda: adjoint_extra(local, 3)),
                          ("combined", lambda: combined_extra(local) if args.workload != "combined" else
                           {"note": "the headline is the combined workload"}),

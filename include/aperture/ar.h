@@ -113,12 +113,18 @@ typedef struct ar_render_params
     float guide_unit;        /* voxel size of the guide (0 = 0.05, PATH_GUIDING_RESOLUTION_UNIT) */
     int32_t guide_train_steps; /* AR_GUIDE_MLP: Adam steps after each frame (0 = 8) */
     int32_t denoise_record;  /* 1: record the denoiser's per-pixel G-buffer and sample moments (ar_denoise) */
+    int32_t guide_frames;    /* guided rendering: frames between two guide updates (0 = 1, the reference's
+                                update after every frame); the frames of one update window share waves */
 } ar_render_params;
 
 /* Path guiding modes.  With AR_GUIDE_VOXEL, ar_render renders one frame (one
  * sample per pixel) at a time and, after each frame, folds its radiance records
  * into the context's voxel probes (core/scene.cu:240-273, 409-570); the probes
- * persist across ar_render calls until ar_guide_reset or a scene rebuild. */
+ * persist across ar_render calls until ar_guide_reset or a scene rebuild.
+ * With params->guide_frames = k > 1 the update comes after every k frames
+ * instead, over all their records (the same count-weighted running mean the
+ * per-frame updates build, so only the probes the k frames sample from are
+ * older); the k frames then run together in waves of up to k x pixels paths. */
 #define AR_GUIDE_NONE 0
 #define AR_GUIDE_VOXEL 1
 /* AR_GUIDE_MLP (no reference counterpart): the voxel probes learn as with

@@ -1179,6 +1179,7 @@ static R med_transmittance(const Scene& S, V o, V d, R dist)
 struct Params
 {
     int width, height, spp, max_depth, use_nee, first_frame, threads;
+    int crop_x0 = 0, crop_y0 = 0, crop_w = 0, crop_h = 0;  // crop_w > 0: only this window of pixels
     uint64_t seed;
     R cam_o[3], cam_d[3], fov;
 };
@@ -1494,6 +1495,10 @@ static void run(const Scene& S, const Params& P, double* mean, double* per_sampl
     for (size_t p = 0; p < S.prim_type.size(); ++p)
         if (S.prim_type[p] != OBJ_TRIANGLE && overlap(cam.o, S.objs[p])) cam_inside = true;
     const long long npix = (long long)P.width * P.height;
+    // pixels to render: the whole image, or a crop window (indices local to the window,
+    // random streams and camera rays of the full image's pixels)
+    const bool crop = P.crop_w > 0;
+    const long long nwork = crop ? (long long)P.crop_w * P.crop_h : npix;
     const int nt = std::max(1, P.threads);
     std::atomic<long long> next(0);
     std::vector<std::vector<double>> gpart(grad ? nt : 0);
@@ -1507,8 +1512,9 @@ static void run(const Scene& S, const Params& P, double* mean, double* per_sampl
             gpart[tid].assign(S.texels.size(), 0.0);
             G = &gpart[tid];
         }
-        for (long long pix; (pix = next.fetch_add(1)) < npix;)
+        for (long long q; (q = next.fetch_add(1)) < nwork;)
         {
+            const long long pix = crop ? (long long)(P.crop_y0 + q / P.crop_w) * P.width + (P.crop_x0 + q % P.crop_w) : q;
             double acc[3] = {0, 0, 0};
             for (int s = 0; s < P.spp; ++s)
             {
@@ -1546,7 +1552,7 @@ static void run(const Scene& S, const Params& P, double* mean, double* per_sampl
                 }
             }
             if (mean)
-                for (int k = 0; k < 3; ++k) mean[3 * pix + k] = acc[k] / P.spp;
+                for (int k = 0; k < 3; ++k) mean[3 * q + k] = acc[k] / P.spp;
         }
     };
     std::vector<std::thread> th;
@@ -1835,6 +1841,24 @@ static Params to_params(const int32_t* ip, const double* dp, uint64_t seed)
     }
     P.fov = dp[6];
     return P;
+}
+
+// mean of the crop window (x0, y0, w, h) of the image the params describe, in window order
+int pt64_render_crop(const pt64_scene* s, const int32_t* ip, const double* dp, uint64_t seed, const int32_t* window,
+                     double* mean)
+{
+    if (!s || !ip || !dp || !window || !mean) return -1;
+    Params P = to_params(ip, dp, seed);
+    if (P.width <= 0 || P.height <= 0 || P.spp <= 0 || P.max_depth <= 0) return -1;
+    P.crop_x0 = window[0];
+    P.crop_y0 = window[1];
+    P.crop_w = window[2];
+    P.crop_h = window[3];
+    if (P.crop_x0 < 0 || P.crop_y0 < 0 || P.crop_w <= 0 || P.crop_h <= 0 || P.crop_x0 + P.crop_w > P.width ||
+        P.crop_y0 + P.crop_h > P.height)
+        return -1;
+    run(*reinterpret_cast<const Scene*>(s), P, mean, nullptr, nullptr, nullptr);
+    return 0;
 }
 
 int pt64_render(const pt64_scene* s, const int32_t* ip, const double* dp, uint64_t seed, double* mean, double* per_sample)

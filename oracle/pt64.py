@@ -47,6 +47,8 @@ def load() -> C.CDLL:
         lib.pt64_destroy.argtypes = [vp]
         lib.pt64_render.restype = i32
         lib.pt64_render.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
+        lib.pt64_render_crop.restype = i32
+        lib.pt64_render_crop.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
         lib.pt64_adjoint.restype = i32
         lib.pt64_adjoint.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
         _lib = lib
@@ -157,6 +159,19 @@ class Scene64:
         if rc != 0:
             raise ValueError("FP64 oracle: bad render parameters")
         return (mean, ps) if per_sample else mean
+
+    def render_crop(self, size, window, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
+                    seed=0x9E3779B97F4A7C15, first_frame=0, threads=0):
+        """Per-pixel mean XYZ (h, w, 3) of the window (x0, y0, w, h) of a size[0] x size[1]
+        image: the same pixels, camera rays and random streams as in the full render."""
+        ip, dp = self._params(size, origin, direction, spp, fov, max_depth, use_nee, first_frame,
+                              threads or os.cpu_count() or 1)
+        win = np.array(window, np.int32)
+        mean = np.zeros((int(win[3]), int(win[2]), 3), np.float64)
+        rc = load().pt64_render_crop(self._h, ip.ctypes.data, dp.ctypes.data, seed, win.ctypes.data, mean.ctypes.data)
+        if rc != 0:
+            raise ValueError("FP64 oracle: bad crop parameters")
+        return mean
 
     def adjoint_medium(self, dl_dxyz, size, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
                        seed=0x9E3779B97F4A7C15, first_frame=0, threads=0):

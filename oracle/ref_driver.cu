@@ -11,6 +11,9 @@
 //   trace   BuildBVH + intersection::TraverseBVH<false> over triangles
 //           (core/bvh/bvh.cuh:142-422, core/render/intersection.cuh:148-283),
 //           or brute force
+//   tracecount the reference's BuildBVH tree walked near-first with a slab test
+//           that also requires tEnter <= tExit: node pops and triangle tests
+//           per ray (the traversal roofline's algorithmic work)
 //   render  CalculateRadiance<true, NEE, false> per pixel sample
 //           (core/render/render.cuh:460-999) behind the camera model of
 //           RenderCamera (core/scene.cu:135-189), OpenMP over pixels;
@@ -225,6 +228,113 @@ static int cmd_trace(const char* tri_path, const char* ray_path, const char* out
     printf("{\"build_s\": %.4f, \"trace_s\": %.4f, \"nodes\": %zu, \"node_visits\": %llu, \"prim_tests\": %llu, \"threads\": %d}\n",
            std::chrono::duration<double>(t1 - t0).count(), std::chrono::duration<double>(t2 - t1).count(),
            bvh.nodes_.size(), visits, tests, omp_get_max_threads());
+    return 0;
+}
+
+// ---------------------------------------------------------------- tracecount
+// The traversal work a binary SAH BVH needs for a ray set: the reference's
+// BuildBVH tree (core/bvh/bvh.cuh:142-422) walked near-first as TraverseBVH
+// does (core/render/intersection.cuh:148-283), but with the slab test also
+// requiring tEnter <= tExit (the reference's FastAABBHit, core/bvh/bvh.cuh:
+// 424-444, omits it and so visits every box in front of the ray).  Counts the
+// nodes popped and the triangles tested; the hits equal TraverseBVH's.
+static bool slab_hit(const float3 o, const float3 inv, const float3 lo, const float3 hi, float tmin, float tmax, float* tenter)
+{
+    const float3 t0 = (lo - o) * inv;
+    const float3 t1 = (hi - o) * inv;
+    const float3 tn = min(t0, t1);
+    const float3 tf = max(t0, t1);
+    const float te = fmaxf(fmaxf(tn.x, tn.y), tn.z);
+    const float tx = fminf(fminf(tf.x, tf.y), tf.z);
+    *tenter = te;
+    return te <= tx && tx >= fmaxf(0.0f, tmin) && te <= tmax;
+}
+
+static int cmd_tracecount(const char* tri_path, const char* ray_path, const char* out_path)
+{
+    std::vector<char> tb = read_file(tri_path);
+    std::vector<char> rb = read_file(ray_path);
+    const int ntri = *reinterpret_cast<const int32_t*>(tb.data());
+    const float* tris = reinterpret_cast<const float*>(tb.data() + 4);
+    const int nray = *reinterpret_cast<const int32_t*>(rb.data());
+    const float* rays = reinterpret_cast<const float*>(rb.data() + 4);
+    std::vector<PrimitiveProxy> proxy(ntri);
+    for (int i = 0; i < ntri; ++i)
+    {
+        const float* v = tris + (size_t)i * 9;
+        PrimitiveProxy pp;
+        pp.boundMin_ = float3{fminf(v[0], fminf(v[3], v[6])), fminf(v[1], fminf(v[4], v[7])), fminf(v[2], fminf(v[5], v[8]))};
+        pp.boundMax_ = float3{fmaxf(v[0], fmaxf(v[3], v[6])), fmaxf(v[1], fmaxf(v[4], v[7])), fmaxf(v[2], fmaxf(v[5], v[8]))};
+        pp.center_ = float3{(pp.boundMin_.x + pp.boundMax_.x) * 0.5f, (pp.boundMin_.y + pp.boundMax_.y) * 0.5f, (pp.boundMin_.z + pp.boundMax_.z) * 0.5f};
+        proxy[i] = pp;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    const BVHHost bvh = BuildBVH(proxy);
+    auto t1 = std::chrono::steady_clock::now();
+    const BVHNode* nodes = bvh.nodes_.data();
+    const int* idx = bvh.objectIndices_.data();
+    std::vector<int32_t> ids(nray);
+    std::vector<float> ts(nray);
+    std::vector<uint32_t> visits(nray), tests(nray);
+    const TriIntersector isect{tris, ntri};
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int r = 0; r < nray; ++r)
+    {
+        const float* q = rays + (size_t)r * 8;
+        const float3 o{q[0], q[1], q[2]}, d{q[4], q[5], q[6]};
+        const float tmin = q[3];
+        IntersectionContext res{};
+        res.distance_ = q[7];
+        const float3 inv = invSafe(d);
+        int stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        uint32_t nv = 0, nt = 0;
+        while (sp)
+        {
+            const BVHNode& n = nodes[stack[--sp]];
+            ++nv;
+            float te;
+            if (!slab_hit(o, inv, n.boundMin_, n.boundMax_, tmin, res.distance_, &te)) continue;
+            if (n.count_ > 0)
+            {
+                for (int i = 0; i < n.count_; ++i)
+                {
+                    ++nt;
+                    isect(0, idx[n.first_ + i], o, d, tmin, res.distance_, &res);
+                }
+                continue;
+            }
+            float tl = 0.0f, tr = 0.0f;
+            const bool hl = slab_hit(o, inv, nodes[n.left_].boundMin_, nodes[n.left_].boundMax_, tmin, res.distance_, &tl);
+            const bool hr = slab_hit(o, inv, nodes[n.right_].boundMin_, nodes[n.right_].boundMax_, tmin, res.distance_, &tr);
+            if (hl && hr && sp + 2 <= 128)
+            {
+                stack[sp++] = tl > tr ? n.left_ : n.right_;
+                stack[sp++] = tl > tr ? n.right_ : n.left_;
+            }
+            else if (hl && sp < 128) stack[sp++] = n.left_;
+            else if (hr && sp < 128) stack[sp++] = n.right_;
+        }
+        ids[r] = res.bHit_ ? res.objectIndex_ : -1;
+        ts[r] = res.bHit_ ? res.distance_ : -1.0f;
+        visits[r] = nv;
+        tests[r] = nt;
+    }
+    auto t2 = std::chrono::steady_clock::now();
+    unsigned long long sv = 0, st = 0;
+    for (int r = 0; r < nray; ++r)
+    {
+        sv += visits[r];
+        st += tests[r];
+    }
+    write_file(out_path, ids.data(), ids.size() * 4);
+    write_file(out_path, ts.data(), ts.size() * 4, true);
+    write_file(out_path, visits.data(), visits.size() * 4, true);
+    write_file(out_path, tests.data(), tests.size() * 4, true);
+    printf("{\"build_s\": %.4f, \"trace_s\": %.4f, \"nodes\": %zu, \"node_visits\": %llu, \"prim_tests\": %llu, \"threads\": %d}\n",
+           std::chrono::duration<double>(t1 - t0).count(), std::chrono::duration<double>(t2 - t1).count(),
+           bvh.nodes_.size(), sv, st, omp_get_max_threads());
     return 0;
 }
 
@@ -1035,6 +1145,7 @@ int main(int argc, char** argv)
     if ((cmd == "trace" || cmd == "brute") && argc == 5) return cmd_trace(argv[2], argv[3], argv[4], cmd == "brute");
     if (cmd == "render" && argc == 5) return cmd_render(argv[2], argv[3], argv[4], nullptr);
     if (cmd == "render" && argc == 6) return cmd_render(argv[2], argv[3], argv[4], argv[5]);
+    if (cmd == "tracecount" && argc == 5) return cmd_tracecount(argv[2], argv[3], argv[4]);
     if (cmd == "tonemap" && argc == 4) return cmd_tonemap(argv[2], argv[3]);
     if (cmd == "frametone" && argc == 4) return cmd_frametone(argv[2], argv[3]);
     if (cmd == "pgupdate" && argc == 5) return cmd_pgupdate(argv[2], argv[3], argv[4]);

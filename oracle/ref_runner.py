@@ -300,3 +300,30 @@ def frame_tonemap(hdr, exposure: float, tone_type: int) -> np.ndarray:
         if r.returncode != 0:
             raise RuntimeError("reference oracle failed: " + r.stderr)
         return np.frombuffer((td / "out.bin").read_bytes(), np.uint32).reshape(h, w).copy()
+
+
+def trace_count(tris: np.ndarray, rays: np.ndarray, threads=None):
+    """Closest hits through the reference's BuildBVH tree walked with a slab test that
+    requires tEnter <= tExit: (prim_id, t, node pops per ray, triangle tests per ray, stats)."""
+    exe = ensure_built()
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    n = len(rays)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "tris.bin").write_bytes(np.int32(len(tris)).tobytes() + tris.tobytes())
+        (td / "rays.bin").write_bytes(np.int32(n).tobytes() + rays.tobytes())
+        env = dict(os.environ)
+        if threads:
+            env["OMP_NUM_THREADS"] = str(threads)
+        r = subprocess.run([str(exe), "tracecount", str(td / "tris.bin"), str(td / "rays.bin"), str(td / "out.bin")],
+                           capture_output=True, text=True, env=env)
+        if r.returncode != 0:
+            raise RuntimeError("reference oracle failed: " + r.stderr)
+        stats = json.loads(r.stdout.strip().splitlines()[-1])
+        raw = (td / "out.bin").read_bytes()
+    ids = np.frombuffer(raw[: 4 * n], np.int32).copy()
+    t = np.frombuffer(raw[4 * n: 8 * n], np.float32).copy()
+    visits = np.frombuffer(raw[8 * n: 12 * n], np.uint32).copy()
+    tests = np.frombuffer(raw[12 * n: 16 * n], np.uint32).copy()
+    return ids, t, visits, tests, stats

@@ -81,3 +81,40 @@ def test_mlp_guide_on_terrain(cuda_device):
     assert np.all(np.isfinite(img)) and img.mean() > 0
     assert r.mlp_stats()[0] == 8 * 16
     assert r.error_word() == 0
+
+
+@pytest.mark.parametrize("name,objs,mesh,cam", scenes()[:1])
+def test_guide_update_windows(cuda_device, name, objs, mesh, cam):
+    """guide_frames = k: the guide updates after every k frames and the k frames
+    share waves.  k = 1 is the per-frame update; the first window of k frames has
+    no probes yet and draws exactly what the unguided render draws; the windowed
+    render learns and stays unbiased."""
+    size = (48, 40)
+    kw = dict(fov=cam["fov"], max_depth=16)
+    r = SceneRenderer(objs, mesh=mesh)
+    a = r.Render(size, cam["origin"], cam["direction"], 6, guide=1, **kw)
+    r.MarkNeedResetGuiding()
+    b = r.Render(size, cam["origin"], cam["direction"], 6, guide=1, guide_frames=1, **kw)
+    assert np.array_equal(a, b)
+    r.MarkNeedResetGuiding()
+    plain = r.Render(size, cam["origin"], cam["direction"], 4, **kw)
+    w4 = r.Render(size, cam["origin"], cam["direction"], 4, guide=1, guide_frames=4, **kw)
+    assert np.array_equal(plain, w4)
+    assert r.guide_stats()[0] > 0
+    r.MarkNeedResetGuiding()
+    size, spp = (64, 64), 256
+    plain = r.Render(size, cam["origin"], cam["direction"], spp, **kw)
+    guided = r.Render(size, cam["origin"], cam["direction"], spp, guide=1, guide_frames=16, **kw)
+    _, launches_windowed = r.last_render_stats()
+    r.MarkNeedResetGuiding()
+    r.Render(size, cam["origin"], cam["direction"], spp, guide=1, **kw)
+    _, launches_per_frame = r.last_render_stats()
+    assert launches_windowed < launches_per_frame / 8
+    m_plain, m_guided = plain[..., 1].mean(), guided[..., 1].mean()
+    assert abs(m_guided - m_plain) < 0.03 * m_plain, (m_plain, m_guided)
+    for mode in (2,):
+        r.MarkNeedResetGuiding()
+        img = r.Render(size, cam["origin"], cam["direction"], 64, guide=mode, guide_frames=8, **kw)
+        assert r.mlp_stats()[0] == 8 * 64  # eight Adam steps per frame, taken after each window
+        assert abs(img[..., 1].mean() - m_plain) < 0.05 * m_plain
+    assert r.error_word() == 0
