@@ -7,8 +7,8 @@ on 256 random texels (among those the render reaches):
 * against the FP64 CPU adjoint of the same paths (oracle/pt64), depth 8 with
   Russian roulette: both hold the survival probabilities fixed, the unbiased
   choice;
-* against central finite differences with h = 1e-3 of the same seeded render,
-  depth 3: no roulette fires there (it starts at the third non-delta vertex,
+* against central finite differences of the same seeded render (h = 1e-3,
+  and steps inside the spectral LUT cell), depth 3: no roulette fires there (it starts at the third non-delta vertex,
   core/render/render.cuh:838-859).  With roulette on, a same-seed difference
   quotient differentiates the realisation, in which the survival probability
   q = clamp(throughput) cancels the albedos before an unclamped roulette
@@ -67,26 +67,50 @@ def test_adjoint_vs_fp64_adjoint_at_scale(cuda_device):
     assert r.error_word() == 0
 
 
+LUT_RES = 512  # RGB -> spectrum lattice: planes at (i + 0.5) / 512 per channel
+
+
+def _lattice_distance(x):
+    g = np.asarray(x, np.float64) * LUT_RES - 0.5
+    return np.abs(g - np.round(g)) / LUT_RES
+
+
 def test_adjoint_vs_central_differences_at_scale(cuda_device):
+    """Depth 3, NEE on.  Two step sizes per probed channel: h = 1e-3 as the
+    workload states, and a step inside the channel's cell of the spectral LUT
+    lattice (at most 1e-3).  The lattice cell is 1 / 512 wide, less than 2h, so
+    an h = 1e-3 difference averages the slopes of two cells of the trilinear
+    spectral albedo; inside a cell the estimator is linear in the channel and
+    the difference quotient is its exact derivative.  An NEE decision
+    (u < sqrt(throughput)) of a path through the texel can flip under the
+    perturbation: a few channels, each a large jump, are left out of the
+    aggregates."""
     r, tex_a, target, kw, g, probe, _ = _setup(depth=3)
     flat = tex_a.reshape(-1).astype(np.float64)
-    fd = np.empty(len(probe))
-    for k, i in enumerate(probe):
-        vals, at = [], []
-        for sgn in (+1.0, -1.0):
-            x32 = flat.astype(np.float32)
-            x32[i] = np.float32(flat[i] + sgn * 1e-3)
-            r.update_texels(x32)
-            im = r.Render(SIZE, CAM["origin"], CAM["direction"], SPP, **kw)
-            vals.append(((im - target) ** 2).sum())
-            at.append(float(x32[i]))
-        fd[k] = (vals[0] - vals[1]) / (at[0] - at[1])
+
+    def fd(step_of):
+        out = np.empty(len(probe))
+        for k, i in enumerate(probe):
+            vals, at = [], []
+            for sgn in (+1.0, -1.0):
+                x32 = flat.astype(np.float32)
+                x32[i] = np.float32(flat[i] + sgn * step_of(i))
+                r.update_texels(x32)
+                im = r.Render(SIZE, CAM["origin"], CAM["direction"], SPP, **kw)
+                vals.append(((im - target) ** 2).sum())
+                at.append(float(x32[i]))
+            out[k] = (vals[0] - vals[1]) / (at[0] - at[1])
+        return out
+
+    fd_h = fd(lambda i: 1e-3)
+    fd_cell = fd(lambda i: min(1e-3, 0.45 * float(_lattice_distance(flat[i]))))
     r.update_texels(flat.astype(np.float32))
     a = g[probe]
-    rel = np.abs(a - fd) / np.abs(fd)
-    agg = np.linalg.norm(a - fd) / np.linalg.norm(fd)
-    # an NEE decision (u < sqrt(throughput)) of a path through the texel can flip
-    # under the perturbation: a few texels, each a large jump
-    assert np.mean(rel < 1e-2) > 0.9, (np.mean(rel < 1e-2), np.sort(rel)[-8:])
-    ok = rel < 0.5
-    assert np.linalg.norm((a - fd)[ok]) / np.linalg.norm(fd[ok]) < 1e-2, agg
+    rel_cell = np.abs(a - fd_cell) / np.abs(fd_cell)
+    rel_h = np.abs(a - fd_h) / np.abs(fd_h)
+    assert np.mean(rel_cell < 1e-2) > 0.95, (np.mean(rel_cell < 1e-2), np.sort(rel_cell)[-8:])
+    ok = rel_cell < 0.1
+    assert np.linalg.norm((a - fd_cell)[ok]) / np.linalg.norm(fd_cell[ok]) < 1e-2
+    assert np.median(rel_h) < 1e-2 and np.mean(rel_h < 5e-2) > 0.9, (np.median(rel_h), np.mean(rel_h < 5e-2))
+    ok = rel_h < 0.1
+    assert np.linalg.norm((a - fd_h)[ok]) / np.linalg.norm(fd_h[ok]) < 2e-2
