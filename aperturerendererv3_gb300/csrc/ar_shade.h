@@ -13,6 +13,13 @@
 #define AR_MAT_DIFFUSE 0
 #define AR_MAT_LIGHT 1
 #define AR_MAT_GLASS 2
+// shading models a scene can hold, as bits of the BSDF functions' MATS template
+// argument: a kernel built for a scene without some model compiles its code out
+#define AR_MATS_DIFFUSE (1 << 0)
+#define AR_MATS_LIGHT (1 << 1)
+#define AR_MATS_GLASS (1 << 2)
+#define AR_MATS_GGX (1 << 3)
+#define AR_MATS_ALL 15
 #define AR_MAT_GGX 3
 
 #define AR_PERFECT_DELTA_SURFACE 0.99f
@@ -341,14 +348,15 @@ AR_HD float ggx_bounded_vndf_pdf(V3 V, V3 N, V3 L, float alpha)
 
 // ---------------------------------------------------------------- BSDF
 // core/render/material.cuh:48-165 (spectral branch)
+template <int MATS = AR_MATS_ALL>
 AR_HD float eval_bsdf_cos(float lambda, const Basis& lb, const Material& m, V3 rayDir, V3 L, const Hit& h,
                           const Media& media)
 {
     const V3 N = h.nrm;
     const float NoL = fmaxf(0.0f, dot(N, L));
-    if (m.shading == AR_MAT_DIFFUSE) return interact(m.albedo_c, lb) * (NoL / AR_PI_F);
+    if ((MATS & AR_MATS_DIFFUSE) && m.shading == AR_MAT_DIFFUSE) return interact(m.albedo_c, lb) * (NoL / AR_PI_F);
     if (m.shading == AR_MAT_LIGHT) return 0.0f;
-    if (m.shading == AR_MAT_GGX)
+    if ((MATS & AR_MATS_GGX) && m.shading == AR_MAT_GGX)
     {
         const V3 V = normalize(-rayDir);
         const float NoV = fmaxf(0.0f, dot(N, V));
@@ -368,7 +376,7 @@ AR_HD float eval_bsdf_cos(float lambda, const Basis& lb, const Material& m, V3 r
         const float diff = kD * (1.0f - F) * albL * (NoL / AR_PI_F);
         return spec + diff;
     }
-    if (m.shading == AR_MAT_GLASS)
+    if ((MATS & AR_MATS_GLASS) && m.shading == AR_MAT_GLASS)
     {
         const float IOR = ior_from_abbe(lambda, m.ior, m.abbe);
         float transmittance = 1.0f;
@@ -398,12 +406,13 @@ AR_HD float eval_bsdf_cos(float lambda, const Basis& lb, const Material& m, V3 r
 }
 
 // core/render/material.cuh:316-371
+template <int MATS = AR_MATS_ALL>
 AR_HD float bsdf_pdf(const Basis& lb, const Material& m, V3 N, V3 rayDir, V3 L)
 {
     const V3 V = -rayDir;
     const float NoL = fmaxf(0.0f, dot(N, L));
-    if (m.shading == AR_MAT_DIFFUSE) return NoL > 0.0f ? (NoL * (1.0f / AR_PI_F)) : 0.0f;
-    if (m.shading == AR_MAT_GGX)
+    if ((MATS & AR_MATS_DIFFUSE) && m.shading == AR_MAT_DIFFUSE) return NoL > 0.0f ? (NoL * (1.0f / AR_PI_F)) : 0.0f;
+    if ((MATS & AR_MATS_GGX) && m.shading == AR_MAT_GGX)
     {
         const float NoV = fmaxf(0.0f, dot(N, V));
         if (NoV <= 0.0f || NoL <= 0.0f) return 0.0f;
@@ -444,14 +453,14 @@ AR_HD BsdfSample bsdf_sample_default()
 
 // core/render/material.cuh:167-314 followed by :373-409 (EvaluateMaterial).
 // Rand is a callable returning the next uniform in (0, 1].
-template <typename Rand>
+template <int MATS = AR_MATS_ALL, typename Rand>
 AR_HD BsdfSample evaluate_material(float lambda, const Basis& lb, Rand& rand, const Material& m, V3 rayDir,
                                    const Hit& h, const Media& cur)
 {
     BsdfSample r = bsdf_sample_default();
     const V3 N = h.nrm;
     const V3 V = -rayDir;
-    if (m.shading == AR_MAT_DIFFUSE)
+    if ((MATS & AR_MATS_DIFFUSE) && m.shading == AR_MAT_DIFFUSE)
     {
         const float e0 = rand(), e1 = rand(), e2 = rand();
         const DirSample s = sample_cosine_hemisphere(e0, e1, e2, N);
@@ -468,7 +477,7 @@ AR_HD BsdfSample evaluate_material(float lambda, const Basis& lb, Rand& rand, co
         r.terminate = true;
         r.pure_light = true;
     }
-    else if (m.shading == AR_MAT_GLASS)
+    else if ((MATS & AR_MATS_GLASS) && m.shading == AR_MAT_GLASS)
     {
         const float IOR = ior_from_abbe(lambda, m.ior, m.abbe);
         r.delta = true;
@@ -505,7 +514,7 @@ AR_HD BsdfSample evaluate_material(float lambda, const Basis& lb, Rand& rand, co
             r.media.vertex = h.pos;
         }
     }
-    else if (m.shading == AR_MAT_GGX)
+    else if ((MATS & AR_MATS_GGX) && m.shading == AR_MAT_GGX)
     {
         r.emissive = m.emissive;
         const float NoV = fmaxf(0.0f, dot(N, V));
@@ -560,7 +569,7 @@ AR_HD BsdfSample evaluate_material(float lambda, const Basis& lb, Rand& rand, co
     }
     r.media.obj = h.obj;
     r.media.depth = cur.depth + 1;
-    r.brdf = eval_bsdf_cos(lambda, lb, m, rayDir, r.next_dir, h, cur);
+    r.brdf = eval_bsdf_cos<MATS>(lambda, lb, m, rayDir, r.next_dir, h, cur);
     return r;
 }
 
@@ -599,25 +608,20 @@ AR_HD void obb_axes(const Object& o, V3* ux, V3* uy, V3* uz)
     *uz = normalize(v3(o.o2w.r0.z, o.o2w.r1.z, o.o2w.r2.z));
 }
 
-struct BoxFacets
+// Facet i of an oriented box light (core/nee/nee.cuh:153-251 lists them in
+// this order): outward normal, centre, the two in-plane axes and half sizes.
+// Computed per facet on demand, so no six-facet table has to live in memory.
+AR_HD void box_facet(V3 ux, V3 uy, V3 uz, V3 c, V3 e, int i, V3* n, V3* ctr, V3* t, V3* b, float* s1, float* s2)
 {
-    V3 n[6], c[6], t[6], b[6];
-    float s1[6], s2[6], area[6];
-};
-
-AR_HD void box_facets(const Object& o, BoxFacets* f)
-{
-    V3 ux, uy, uz;
-    obb_axes(o, &ux, &uy, &uz);
-    const V3 c = o.center, e = o.extent;
-    f->n[0] = ux; f->n[1] = -ux; f->n[2] = uy; f->n[3] = -uy; f->n[4] = uz; f->n[5] = -uz;
-    f->c[0] = c + ux * e.x; f->c[1] = c - ux * e.x; f->c[2] = c + uy * e.y;
-    f->c[3] = c - uy * e.y; f->c[4] = c + uz * e.z; f->c[5] = c - uz * e.z;
-    f->t[0] = uy; f->t[1] = uy; f->t[2] = ux; f->t[3] = ux; f->t[4] = ux; f->t[5] = ux;
-    f->b[0] = uz; f->b[1] = uz; f->b[2] = uz; f->b[3] = uz; f->b[4] = uy; f->b[5] = uy;
-    f->s1[0] = e.y; f->s1[1] = e.y; f->s1[2] = e.x; f->s1[3] = e.x; f->s1[4] = e.x; f->s1[5] = e.x;
-    f->s2[0] = e.z; f->s2[1] = e.z; f->s2[2] = e.z; f->s2[3] = e.z; f->s2[4] = e.y; f->s2[5] = e.y;
-    for (int i = 0; i < 6; ++i) f->area[i] = 4.0f * f->s1[i] * f->s2[i];
+    switch (i)
+    {
+    case 0: *n = ux; *ctr = c + ux * e.x; *t = uy; *b = uz; *s1 = e.y; *s2 = e.z; break;
+    case 1: *n = -ux; *ctr = c - ux * e.x; *t = uy; *b = uz; *s1 = e.y; *s2 = e.z; break;
+    case 2: *n = uy; *ctr = c + uy * e.y; *t = ux; *b = uz; *s1 = e.x; *s2 = e.z; break;
+    case 3: *n = -uy; *ctr = c - uy * e.y; *t = ux; *b = uz; *s1 = e.x; *s2 = e.z; break;
+    case 4: *n = uz; *ctr = c + uz * e.z; *t = ux; *b = uy; *s1 = e.x; *s2 = e.y; break;
+    default: *n = -uz; *ctr = c - uz * e.z; *t = ux; *b = uy; *s1 = e.x; *s2 = e.y; break;
+    }
 }
 
 // core/nee/nee.cuh:56-62
@@ -639,52 +643,68 @@ AR_HD float area_to_solid_angle_pdf(V3 sp, V3 lp, V3 ln, float pA)
     return pA * (d2 / cosY);
 }
 
-// core/nee/nee.cuh:153-251
+// core/nee/nee.cuh:153-251.  The facets with a positive facing weight, in facet
+// order, form the selection list; the loops run over all six facets and skip
+// the others, and the chosen facet's geometry is computed again from its index.
 template <typename Rand>
 AR_HD LightSample sample_box_light(Rand& rand, const Object& box, V3 p)
 {
     LightSample ls;
     ls.valid = false;
-    BoxFacets f;
-    box_facets(box, &f);
-    int idx[6];
+    V3 ux, uy, uz;
+    obb_axes(box, &ux, &uy, &uz);
+    const V3 c = box.center, e = box.extent;
     float w[6];
     int cnt = 0;
+    int first = -1;
     float sum = 0;
+#pragma unroll
     for (int i = 0; i < 6; ++i)
     {
-        const float cw = facing_weight(f.n[i], f.c[i], p, f.area[i]);
-        if (cw > 0.0f)
+        V3 n, ctr, t, b;
+        float s1, s2;
+        box_facet(ux, uy, uz, c, e, i, &n, &ctr, &t, &b, &s1, &s2);
+        w[i] = facing_weight(n, ctr, p, 4.0f * s1 * s2);
+        if (w[i] > 0.0f)
         {
-            idx[cnt] = i;
-            w[cnt] = cw;
-            sum += cw;
+            if (first < 0) first = i;
+            sum += w[i];
             ++cnt;
         }
     }
     if (cnt == 0) return ls;
-    int slot = 0;
-    int face = idx[0];
+    int face = first;
     {
         const float r = rand() * sum;
         float acc = 0;
-        for (int k = 0; k < cnt; ++k)
+        bool found = false;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
         {
-            acc += w[k];
-            if (r <= acc)
+            if (!found && w[i] > 0.0f)
             {
-                slot = k;
-                face = idx[k];
-                break;
+                acc += w[i];
+                if (r <= acc)
+                {
+                    face = i;
+                    found = true;
+                }
             }
         }
     }
+    float fw = w[0];
+#pragma unroll
+    for (int i = 1; i < 6; ++i)
+        if (face == i) fw = w[i];
+    V3 fn, fc, ft, fb;
+    float fs1, fs2;
+    box_facet(ux, uy, uz, c, e, face, &fn, &fc, &ft, &fb, &fs1, &fs2);
     const float u1 = 2.0f * rand() - 1.0f;
     const float u2 = 2.0f * rand() - 1.0f;
-    ls.point = f.c[face] + f.t[face] * (u1 * f.s1[face]) + f.b[face] * (u2 * f.s2[face]);
-    ls.normal = f.n[face];
-    ls.p_facet = 1.0f * (w[slot] / sum);
-    ls.p_a = 1.0f / f.area[face];
+    ls.point = fc + ft * (u1 * fs1) + fb * (u2 * fs2);
+    ls.normal = fn;
+    ls.p_facet = 1.0f * (fw / sum);
+    ls.p_a = 1.0f / (4.0f * fs1 * fs2);
     ls.valid = true;
     return ls;
 }
@@ -722,23 +742,28 @@ AR_HD LightSample sample_sphere_light(Rand& rand, const Object& sph, V3 p)
 // core/nee/nee.cuh:64-151
 AR_HD float box_light_pdf_omega(const Object& o, float selectProb, V3 sp, V3 lp, V3 ln)
 {
-    BoxFacets f;
-    box_facets(o, &f);
+    V3 ux, uy, uz;
+    obb_axes(o, &ux, &uy, &uz);
+    const V3 c = o.center, e = o.extent;
     int hitFacet = -1;
+#pragma unroll
     for (int i = 0; i < 6; ++i)
     {
-        if (dot(f.n[i], ln) > 0.999f)
-        {
-            hitFacet = i;
-            break;
-        }
+        V3 n, ctr, t, b;
+        float s1, s2;
+        box_facet(ux, uy, uz, c, e, i, &n, &ctr, &t, &b, &s1, &s2);
+        if (hitFacet < 0 && dot(n, ln) > 0.999f) hitFacet = i;
     }
     if (hitFacet < 0)
     {
         float best = 1e30f;
+#pragma unroll
         for (int i = 0; i < 6; ++i)
         {
-            const float d = fabsf(dot(f.n[i], lp - f.c[i]));
+            V3 n, ctr, t, b;
+            float s1, s2;
+            box_facet(ux, uy, uz, c, e, i, &n, &ctr, &t, &b, &s1, &s2);
+            const float d = fabsf(dot(n, lp - ctr));
             if (d < best)
             {
                 best = d;
@@ -747,14 +772,19 @@ AR_HD float box_light_pdf_omega(const Object& o, float selectProb, V3 sp, V3 lp,
         }
     }
     float sum = 0.0f, wHit = 0.0f, aHit = 0.0f;
+#pragma unroll
     for (int i = 0; i < 6; ++i)
     {
-        const float w = facing_weight(f.n[i], f.c[i], sp, f.area[i]);
+        V3 n, ctr, t, b;
+        float s1, s2;
+        box_facet(ux, uy, uz, c, e, i, &n, &ctr, &t, &b, &s1, &s2);
+        const float area = 4.0f * s1 * s2;
+        const float w = facing_weight(n, ctr, sp, area);
         sum += w;
         if (i == hitFacet)
         {
             wHit = w;
-            aHit = f.area[i];
+            aHit = area;
         }
     }
     if (sum <= 0.0f || wHit <= 0.0f) return 0.0f;

@@ -538,6 +538,9 @@ __global__ void __launch_bounds__(AR_BLOCK) k_mlp_query(DevScene sc, PathState p
 }
 
 // ---------------------------------------------------------------- shade
+#ifndef AR_SHADE_LEAN_MIN_BLOCKS
+#define AR_SHADE_LEAN_MIN_BLOCKS 2  // the same for the opaque-surface instantiation (AR_FEAT_SURFACE)
+#endif
 #ifndef AR_SHADE_MIN_BLOCKS
 #define AR_SHADE_MIN_BLOCKS 2    // blocks per SM the unguided / voxel-guided shade kernels are compiled for
 #endif
@@ -602,8 +605,20 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
     }
 }
 
-template <int GUIDE, bool ADJ>
-__global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS : AR_SHADE_MIN_BLOCKS) k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
+// Scene features a k_shade instantiation handles, fixed at compile time: the
+// BSDF models (AR_MATS_* bits), the participating medium and albedo textures.
+// Scenes of opaque surfaces only (no glass, medium or textures, the camera
+// outside every object) run an instantiation without that code: the same
+// arithmetic for everything it keeps, less code and fewer registers.
+#define AR_FEAT_MEDIUM (1 << 4)
+#define AR_FEAT_TEX (1 << 5)
+#define AR_FEAT_ALL (AR_MATS_ALL | AR_FEAT_MEDIUM | AR_FEAT_TEX)
+#define AR_FEAT_SURFACE (AR_MATS_DIFFUSE | AR_MATS_LIGHT | AR_MATS_GGX)
+
+template <int GUIDE, bool ADJ, int FEAT = AR_FEAT_ALL>
+__global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
+                                            : (FEAT == AR_FEAT_SURFACE ? AR_SHADE_LEAN_MIN_BLOCKS : AR_SHADE_MIN_BLOCKS))
+    k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
                                                   const int* __restrict__ counter, int* next_queue, int* next_counter,
                                                   int* shadow_counter, ShadeParams prm)
 {
@@ -616,10 +631,45 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
     __syncthreads();
     const int stride = gridDim.x * blockDim.x;
     float g_med_albedo = 0.0f, g_med_emission = 0.0f;  // replay adjoint of the medium parameters
-    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride)
+    // Each pass of the block takes blockDim.x queue entries and reorders them in
+    // shared memory: rays that hit something first, misses after.  Misses only
+    // add the sky and end, hits run the BSDF, NEE and roulette, so grouping
+    // them gives the heavy part whole warps of hits.  Which thread shades which
+    // path does not change any path's result.
+    __shared__ int s_order[AR_BLOCK];
+    __shared__ int s_warp_hits[AR_BLOCK / 32], s_warp_miss[AR_BLOCK / 32];
+    for (int bbase = blockIdx.x * blockDim.x; bbase < n; bbase += stride)
     {
-        const int q = base + lane_id();
-        const bool active = q < n;
+        {
+            const int qq = bbase + (int)threadIdx.x;
+            const int pp = qq < n ? queue[qq] : -1;
+            const bool is_hit = pp >= 0 && ps.hit_slot[pp] != -1;
+            const bool is_miss = pp >= 0 && !is_hit;
+            const unsigned hb = __ballot_sync(0xffffffffu, is_hit), mb = __ballot_sync(0xffffffffu, is_miss);
+            const int w = threadIdx.x >> 5;
+            if (lane_id() == 0)
+            {
+                s_warp_hits[w] = __popc(hb);
+                s_warp_miss[w] = __popc(mb);
+            }
+            __syncthreads();
+            int hit_base = 0, miss_base = 0, n_hits = 0;
+            for (int k = 0; k < AR_BLOCK / 32; ++k)
+            {
+                if (k < w)
+                {
+                    hit_base += s_warp_hits[k];
+                    miss_base += s_warp_miss[k];
+                }
+                n_hits += s_warp_hits[k];
+            }
+            const unsigned below = (1u << lane_id()) - 1u;
+            if (is_hit) s_order[hit_base + __popc(hb & below)] = pp;
+            if (is_miss) s_order[n_hits + miss_base + __popc(mb & below)] = pp;
+            __syncthreads();
+        }
+        const int n_block = min((int)blockDim.x, n - bbase);
+        const bool active = (int)threadIdx.x < n_block;
         bool keep = false;
         bool shadow = false;
         int p = 0;
@@ -628,7 +678,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
         bool sh_valid = false;
         if (active)
         {
-            p = queue[q];
+            p = s_order[threadIdx.x];
             const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
             const V3 rayO = v3(ro.x, ro.y, ro.z), rayD = v3(rd.x, rd.y, rd.z);
             const float lambda = ro.w;
@@ -667,7 +717,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             // ---- participating medium: a free flight sampled in the medium box
             // ends the segment early with probability 1 - transmittance
             bool scatter = false;
-            if (sc.medium.on)
+            if ((FEAT & AR_FEAT_MEDIUM) && sc.medium.on)
             {
                 float m0, m1;
                 if (medium_segment(sc.medium, rayO, rayD, 0.0f, h.hit ? h.dist : 3.0e38f, &m0, &m1))
@@ -707,7 +757,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             if (h.hit)
             {
                 mat = sc.materials[sc.prim_material[h.obj]];
-                if (mat.albedo_tex >= 0 && sc.tex_count > 0)
+                if ((FEAT & AR_FEAT_TEX) && mat.albedo_tex >= 0 && sc.tex_count > 0)
                 {
                     texel = albedo_texel(sc, mat.albedo_tex, slot, h.obj, h.pos);
                     if (texel >= 0)
@@ -717,7 +767,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                         mat.albedo_c = prepare_color(mat.albedo, PlainFetch{sc.lut_rgb});
                     }
                 }
-                S = evaluate_material(lambda, lb, R, mat, rayD, h, media);
+                S = evaluate_material<FEAT & AR_MATS_ALL>(lambda, lb, R, mat, rayD, h, media);
             }
             else if (scatter)
             {
@@ -790,9 +840,9 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                                 const GuideSample g = mlp_sample_hemisphere(q, q_total, R, h.nrm);
                                 if (dot(g.dir, h.nrm) > 1.0e-12f)
                                 {
-                                    const float pBs = bsdf_pdf(lb, mat, h.nrm, rayD, g.dir);
+                                    const float pBs = bsdf_pdf<FEAT & AR_MATS_ALL>(lb, mat, h.nrm, rayD, g.dir);
                                     S.next_dir = g.dir;
-                                    S.brdf = eval_bsdf_cos(lambda, lb, mat, rayD, g.dir, h, media);
+                                    S.brdf = eval_bsdf_cos<FEAT & AR_MATS_ALL>(lambda, lb, mat, rayD, g.dir, h, media);
                                     S.pdf = (1.0f - pgProb) * fmaxf(pBs, 1.0e-12f) + pgProb * g.pdf;
                                 }
                                 else
@@ -827,9 +877,9 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                                 const GuideSample g = sample_octahedron_hemisphere(*probe, R, h.nrm, maskq);
                                 if (dot(g.dir, h.nrm) > 1.0e-12f)
                                 {
-                                    const float pBs = bsdf_pdf(lb, mat, h.nrm, rayD, g.dir);
+                                    const float pBs = bsdf_pdf<FEAT & AR_MATS_ALL>(lb, mat, h.nrm, rayD, g.dir);
                                     S.next_dir = g.dir;
-                                    S.brdf = eval_bsdf_cos(lambda, lb, mat, rayD, g.dir, h, media);
+                                    S.brdf = eval_bsdf_cos<FEAT & AR_MATS_ALL>(lambda, lb, mat, rayD, g.dir, h, media);
                                     S.pdf = (1.0f - pgProb) * fmaxf(pBs, 1.0e-12f) + pgProb * g.pdf;
                                 }
                                 else
@@ -984,13 +1034,13 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                             {
                                 const float brdfCos =
                                     scatter ? sc.medium.albedo * hg_pdf(dot(rayD, L), sc.medium.g)
-                                            : eval_bsdf_cos(lambda, lb, mat, rayD, L, h, media_default());
+                                            : eval_bsdf_cos<FEAT & AR_MATS_ALL>(lambda, lb, mat, rayD, L, h, media_default());
                                 const float G = (cosY / dist2);
                                 const float le = interact(sc.materials[ls.material].emissive_c, lb);
                                 const float contribution = brdfCos * le * (G / pATotal);
                                 const float pLight = area_to_solid_angle_pdf(h.pos, ls.point, ls.normal, ls.p_facet * ls.p_a);
                                 float pBsdf = scatter ? hg_pdf(dot(rayD, L), sc.medium.g)
-                                                      : fmaxf(bsdf_pdf(lb, mat, h.nrm, rayD, L), 0.0f);
+                                                      : fmaxf(bsdf_pdf<FEAT & AR_MATS_ALL>(lb, mat, h.nrm, rayD, L), 0.0f);
                                 if constexpr (GUIDE)
                                 {
                                     if (probe)
@@ -1002,7 +1052,8 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                                 }
                                 const float misW = power_heuristic(pLight, pBsdf);
                                 vUn = mask * (contribution * misW) * d65;
-                                if (sc.medium.on) vUn *= medium_transmittance(sc.medium, h.pos, L, sqrtf(dist2));
+                                if ((FEAT & AR_FEAT_MEDIUM) && sc.medium.on)
+                                    vUn *= medium_transmittance(sc.medium, h.pos, L, sqrtf(dist2));
                                 validUn = true;
                             }
                             // shadow segment (intersection.cuh:285-310)
@@ -1096,6 +1147,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             sq.valid_unocc[sqi] = sh_valid ? 1 : 0;
             sq.sdf_eps[sqi] = sh_sdf_eps;
         }
+        __syncthreads();  // s_order is refilled by the next pass
     }
     if constexpr (ADJ)
     {
@@ -1391,6 +1443,9 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     // SDF geometry: its work leaves the traversal kernels for k_sdf_extend / k_sdf_shadow
     const bool has_sdf = c.sdf_object_count > 0 || c.sdf.count > 0;
     const SdfPending pend_shd{has_sdf ? c.d_pend_list : nullptr, &cnt[AR_CNT_PEND]};
+    // opaque surfaces only: the shading instantiation without glass, medium and texture code
+    bool lean = !c.medium.on && c.tex_count == 0 && !c.camera_inside;
+    for (const Material& m : c.materials) lean = lean && m.shading != AR_MAT_GLASS;
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
@@ -1429,6 +1484,9 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
                 k_shade<1, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
             else if (rl.adjoint)
                 k_shade<0, true><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+            else if (lean)
+                k_shade<0, false, AR_FEAT_SURFACE><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn,
+                                                                              shc, prm);
             else
                 k_shade<0, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
         }
