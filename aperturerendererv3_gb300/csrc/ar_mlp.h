@@ -4,11 +4,13 @@
 // Network: 12-band frequency encoding of the shading point (position
 // normalised to the scene box) and of the reflected view direction (6 inputs x
 // 12 bands x sin/cos = 144 features), then 144 -> 64 -> 64 -> 64 -> 64 -> 64
-// with ReLU between layers.  The 64 outputs estimate the log of the mean
-// incident radiance in the 8 x 8 cells of the same equal-area (Clarberg)
-// sphere map the voxel probes use; the guide samples cells in proportion to exp(output), quantised to 8
-// bits per cell (64 bytes per shading point), and a point uniformly inside the
-// cell, folded into the normal's hemisphere as the voxel guide folds its lobe.
+// with ReLU between layers.  The 64 outputs are the logits of a distribution
+// over the 8 x 8 cells of the same equal-area (Clarberg) sphere map the voxel
+// probes use, trained (cross-entropy weighted by record radiance) towards the
+// radiance the records carry into each cell, as a probe's leaf accumulates it;
+// the guide samples cells in proportion to exp(output), quantised to 8 bits per
+// cell (64 bytes per shading point), and a point uniformly inside the cell,
+// folded into the normal's hemisphere as the voxel guide folds its lobe.
 #pragma once
 #include <string.h>
 

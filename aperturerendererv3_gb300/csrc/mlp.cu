@@ -246,11 +246,15 @@ __global__ void __launch_bounds__(128 * mlpk::INF_WG, 1)
 
 // Training: forward, loss gradient and backward over tiles of 128 radiance
 // records; weight gradients accumulate in TMEM for all of a CTA's tiles and are
-// added to the float32 gradient block at the end.  Loss per record (Poisson
-// log-likelihood of the record's radiance Y under the cell's predicted mean
-// exp(y), the cell being the record direction's): exp(y) - Y y, averaged over
-// the records used; its minimiser is exp(y) = E[Y | position, cell], the mean
-// radiance a voxel probe's texel holds.
+// added to the float32 gradient block at the end.  Loss per record: the
+// radiance-weighted cross-entropy of the record direction's cell under the
+// softmax p of the 64 outputs, Y (logsumexp(y) - y_cell), averaged over the
+// records used.  Its minimiser is p(cell | position, view) proportional to
+// E[Y 1(direction in cell)], the radiance the records carried into each cell:
+// what a voxel probe's leaf accumulates (radiance x Jacobian per texel over
+// the records of its voxel and face, core/guiding/guiding.cuh:373-418), so the
+// network learns the probes' distribution, including the density of the
+// directions the records were sampled with.
 __global__ void __launch_bounds__(128, 1)
     k_mlp_train(MlpDev net, const float4* __restrict__ r_pos, const float4* __restrict__ r_wr,
                 const float4* __restrict__ r_dir, const float4* __restrict__ r_rad, const int* __restrict__ count_ptr,
@@ -299,24 +303,14 @@ __global__ void __launch_bounds__(128, 1)
         const bool valid = s < n_use;
         const int rec = valid ? (int)(((long long)s * stride + offset) % count) : 0;
         float in6[6] = {0, 0, 0, 0, 0, 0};
-        int cell = 0, cell_m = -1;
+        int cell = 0;
         float target = 0.0f;
         if (valid)
         {
             const float4 a = r_pos[rec], w = r_wr[rec], d = r_dir[rec], L = r_rad[rec];
             mlp_inputs(net.box, v3(a.x, a.y, a.z), v3(w.x, w.y, w.z), in6);
-            const V3 dd = normalize(v3(d.x, d.y, d.z));
-            cell = mlp_cell(dd);
+            cell = mlp_cell(normalize(v3(d.x, d.y, d.z)));
             target = fmaxf(L.y, 0.0f);
-            // a zero-radiance virtual record below the surface, mirrored from the record's direction:
-            // cells under the tangent plane see no records otherwise, and the sampler folds them up
-            const V3 nn = mlp_unpack_normal(w.w);
-            const float dn = dot(dd, nn);
-            if (dn > 0.0f)
-            {
-                cell_m = mlp_cell(dd - nn * (2.0f * dn));
-                if (cell_m == cell) cell_m = -1;
-            }
         }
         encode_row(X, row, in6);
         wg_publish(0);
@@ -357,27 +351,34 @@ __global__ void __launch_bounds__(128, 1)
             }
             else
             {
-                float dy = 0.0f, dym = 0.0f;
-                if (valid)
+                // radiance-weighted cross-entropy of the record's cell under the
+                // softmax of the outputs: weight Y, d loss / d y_j = Y (p_j - [j == cell])
+                float mx = -3.0e38f;
+                for (int i = 0; i < 64; ++i)
                 {
-                    const float y = fminf(v[cell] + b[cell], 30.0f);
-                    const float ey = __expf(y);
-                    dy = (ey - target) * inv_n;
-                    my_loss += ey - target * y;
-                    atomicAdd(&sdb[4 * 64 + cell], dy);
-                    if (cell_m >= 0)
-                    {
-                        const float eym = __expf(fminf(v[cell_m] + b[cell_m], 30.0f));
-                        dym = eym * inv_n;
-                        my_loss += eym;
-                        atomicAdd(&sdb[4 * 64 + cell_m], dym);
-                    }
+                    v[i] += b[i];
+                    mx = fmaxf(mx, v[i]);
                 }
+                float se = 0.0f;
+                for (int i = 0; i < 64; ++i) se += __expf(v[i] - mx);
+                const float inv_se = 1.0f / se;
+                const float wgt = valid ? target * inv_n : 0.0f;
+                if (valid && target > 0.0f) my_loss += target * (mx + __logf(se) - v[cell]);
                 for (int c = 0; c < 8; ++c)
                 {
                     float g[8];
-                    for (int i = 0; i < 8; ++i) g[i] = (8 * c + i == cell) ? dy : ((8 * c + i == cell_m) ? dym : 0.0f);
+                    for (int i = 0; i < 8; ++i)
+                    {
+                        const int j = 8 * c + i;
+                        g[i] = wgt * (__expf(v[j] - mx) * inv_se - (j == cell ? 1.0f : 0.0f));
+                    }
                     store8(DY, 128, row, 8 * c, g);
+                    for (int i = 0; i < 8; ++i)
+                    {
+                        float t = g[i];
+                        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                        if (lane == 0 && t != 0.0f) atomicAdd(&sdb[4 * 64 + 8 * c + i], t);
+                    }
                 }
             }
             wg_publish(0);
@@ -717,7 +718,7 @@ extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* i
     {
         const float* x = in6 + 6 * (size_t)i;
         pos[i] = make_float4(x[0], x[1], x[2], 1.0f);
-        // no normal: one pointing away from the record direction (no mirrored record)
+        // the packed normal rides along in the record (the cross-entropy loss does not read it)
         const V3 dn = nrm ? v3(nrm[3 * (size_t)i], nrm[3 * (size_t)i + 1], nrm[3 * (size_t)i + 2])
                           : -v3(dirs[3 * (size_t)i], dirs[3 * (size_t)i + 1], dirs[3 * (size_t)i + 2]);
         wr[i] = make_float4(2.0f * x[3] - 1.0f, 2.0f * x[4] - 1.0f, 2.0f * x[5] - 1.0f, mlp_pack_normal(normalize(dn)));

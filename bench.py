@@ -303,6 +303,52 @@ def guide_compare_extra(r, w, cam, objs, mesh, ref_spp: int = 2048, window: int 
     return out
 
 
+def ref_gpu_extra(device: int, size=(256, 256), spp: int = 256) -> dict:
+    """The reference's own GPU renderer (its RenderCamera megakernel built for
+    sm_103a with its own -use_fast_math -maxrregcount=168 flags, oracle/_ref/
+    ref_gpu) against ours on the reference's Cornell box (SceneHelper::
+    CreateCornellBox; camera (0, 0, 1.1) looking down -z, FOV 60, the
+    reference's path depth), plain method (no guide), `spp` frames each:
+    Msamples/s of both (the reference: wall time of its per-frame Render calls,
+    which synchronise the device; ours: device time of one ar_render) and the
+    rel-MSE between the two converged images.  The reference draws from curand
+    streams and ours from PCG32 streams, so the images agree statistically;
+    the rel-MSE of two of our own renders on disjoint streams is the noise
+    floor to compare with."""
+    import subprocess
+    import tempfile
+    from aperturerendererv3_gb300 import SceneRenderer, configs
+    exe = ROOT / "oracle" / "_ref" / "ref_gpu"
+    if not exe.exists():
+        return {"unavailable": "the reference GPU renderer was not built (no reference sources in this checkout)"}
+    cam = configs.REFERENCE_CORNELL_CAMERA
+    with tempfile.TemporaryDirectory() as td:
+        out = Path(td) / "hdr.bin"
+        env = dict(os.environ)
+        env["CUDA_VISIBLE_DEVICES"] = env.get("CUDA_VISIBLE_DEVICES", str(device))
+        r = subprocess.run([str(exe), str(out), str(size[0]), str(size[1]), str(spp), "0"], capture_output=True,
+                           text=True, env=env, timeout=600)
+        if r.returncode != 0:
+            return {"error": f"reference GPU renderer exited {r.returncode}: {r.stderr.strip()[-300:]}"}
+        # the reference reports CUDA errors on stdout (CHECK_ERROR, core/vector.cuh:22) and carries on
+        if "CUDA ERROR" in r.stdout:
+            return {"error": "reference GPU renderer: " + r.stdout[r.stdout.index("CUDA ERROR"):][:200]}
+        ref_stats = json.loads(r.stdout.strip().splitlines()[-1])
+        ref_img = np.fromfile(out, np.float32).reshape(size[1], size[0], 3).astype(np.float64)
+    ours = SceneRenderer(configs.reference_cornell(), device=device)
+    kw = dict(fov=cam["fov"], max_depth=1000)
+    ours.Render(size, cam["origin"], cam["direction"], 16, first_frame=1 << 22, **kw)  # warm-up
+    img = ours.Render(size, cam["origin"], cam["direction"], spp, **kw)
+    ms = ours.last_render_stats()[0]
+    img2 = ours.Render(size, cam["origin"], cam["direction"], spp, first_frame=1 << 21, **kw)
+    ours_rate = size[0] * size[1] * spp / (ms / 1e3) / 1e6
+    return {"workload": f"reference Cornell box (SceneHelper::CreateCornellBox) {size[0]}x{size[1]}, {spp} spp, "
+                        "depth up to 1000, plain", "reference_gpu": ref_stats, "ours_msamples_per_s": ours_rate,
+            "ours_ms": ms, "speedup": ours_rate / ref_stats["msamples_per_s"],
+            "rel_mse_ours_vs_reference": rel_mse(img, ref_img), "rel_mse_ours_vs_ours_noise_floor": rel_mse(img, img2),
+            "mean_y": {"ours": float(img[..., 1].mean()), "reference": float(ref_img[..., 1].mean())}}
+
+
 def adjoint_extra(device: int, steps: int) -> dict:
     """Differentiable-rendering workload: the triangle Cornell box with 8 albedo
     textures of 512^2 RGB texels (U[0.2, 0.8], seed 11) as parameters, target
@@ -540,8 +586,8 @@ def main() -> None:
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the guided, adjoint and BVH-stress measurements reported beside the headline")
     ap.add_argument("--extras", default=None,
-                    help="comma-separated subset of the extras to run (guided_voxel, guide_compare, adjoint, combined, "
-                         "bvh_stress, denoise, bvh_build); default: all")
+                    help="comma-separated subset of the extras to run (guided_voxel, guide_compare, ref_gpu, adjoint, "
+                         "combined, bvh_stress, denoise, bvh_build); default: all")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = dict(WORKLOADS[args.workload])
@@ -672,6 +718,7 @@ def main() -> None:
         extras = {}
         for name, fn in (("guided_voxel", lambda: guided_extra(r, w, cam, 3)),
                          ("guide_compare", lambda: guide_compare_extra(r, w, cam, objs, mesh)),
+                         ("ref_gpu", lambda: ref_gpu_extra(local)),
                          ("adjoint", lambda: adjoint_extra(local, 3)),
                          ("combined", lambda: combined_extra(local) if args.workload != "combined" else
                           {"note": "the headline is the combined workload"}),

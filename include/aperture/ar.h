@@ -437,11 +437,11 @@ int ar_abi_version(void);
  * layer W[64][in] row-major then b[64]; in = 144 for layer 0, 64 after).
  * in6: n x 6 encoded inputs in [0, 1] (position in the scene box, then
  * (reflected direction + 1) / 2); dirs: n x 3 record directions; nrm: n x 3
- * surface normals (NULL: no mirrored zero-radiance records); lum: n record
+ * surface normals (may be NULL; the loss does not use them); lum: n record
  * radiances (CIE Y).  Outputs (host): logits n x 64, grad AR_MLP_PARAMS
- * (d mean loss / d params), loss (sum over records of exp(y) - Y y, y the
- * output of the record direction's cell, plus exp(y') at the cell of the
- * direction mirrored below the surface). */
+ * (d mean loss / d params), loss (sum over records of Y (logsumexp(y) -
+ * y_cell): the radiance-weighted cross-entropy of the record direction's cell
+ * under the softmax of the 64 outputs). */
 #define AR_MLP_PARAMS 25920
 ar_status ar_diag_mlp(int device, const float* params, const float* in6, const float* dirs, const float* nrm,
                       const float* lum, int n, float* logits, float* grad, float* loss);

@@ -266,6 +266,87 @@ def build_ref(jobs_hint: int = 0) -> Path:
     return exe
 
 
+# ---------------------------------------------------------------- ref_gpu
+# The reference's own GPU renderer, for timing beside ours: a copy of the
+# core/ tree with the three Linux build fixes (include case forwarders,
+# <cfloat>, the thrust::cuda::par qualification) and one launch bound (below),
+# compiled with the reference's flags (CMakeLists.txt:111-121: separable
+# compilation, -use_fast_math -maxrregcount=168 --extended-lambda) for
+# sm_103a, driven by oracle/ref_gpu_driver.cu.
+GPU_SRC = OUT / "gpu_src"
+GPU_CORE = GPU_SRC / "core"
+GPU_STAMP = ".ar_gpu_patch_version"
+GPU_PATCH_VERSION = "2"
+GPU_TUS = ["scene.cu", "object/sdf/sdf_base.cu", "object/sdf/sdf_cache_manager.cu", "object/sdf/sdf_master.cu",
+           "denoise/t_quantile.cu"]
+
+
+def needs_prepare_gpu() -> bool:
+    if REF_ROOT is None or not (REF_ROOT / "core").is_dir():
+        return False
+    stamp = GPU_CORE / GPU_STAMP
+    return not stamp.exists() or stamp.read_text().strip() != GPU_PATCH_VERSION
+
+
+def prepare_gpu() -> Path:
+    if REF_ROOT is None or not (REF_ROOT / "core").is_dir():
+        raise FileNotFoundError(f"reference checkout not found at {REF_ROOT}")
+    if GPU_SRC.exists():
+        shutil.rmtree(GPU_SRC)
+    GPU_SRC.mkdir(parents=True)
+    shutil.copytree(REF_ROOT / "core", GPU_CORE, ignore=shutil.ignore_patterns("*.pyc", "__pycache__"))
+    for q in GPU_CORE.rglob("*"):
+        q.chmod(0o644 if q.is_file() else 0o755)
+    (GPU_CORE / "object" / "AABB.cuh").write_text('#pragma once\n#include "aabb.cuh"\n')
+    (GPU_CORE / "object" / "Sphere.cuh").write_text('#pragma once\n#include "sphere.cuh"\n')
+    _sub(GPU_CORE / "guiding" / "guiding.cuh", r"([^:])cuda::par", r"\1thrust::cuda::par")
+    _sub(GPU_CORE / "vector.cuh", r'#include "config.cuh"', '#include <cfloat>\n#include "config.cuh"', count=1)
+    # the spectral-LUT kernel launches 8 x 8 x 8 threads per block
+    # (core/spectrum/spectrum_lut.cuh:68-72); under -maxrregcount=168 this
+    # compiler gives it more than 128 registers, so the launch fails with "too
+    # many resources requested" and the LUT stays unset.  A launch bound of 512
+    # threads on that kernel alone makes it launchable; the render kernels keep
+    # the reference's flags.
+    _sub(GPU_CORE / "spectrum" / "spectrum_lut.cuh", r"__global__ void PrecomputeRGBLUTKernel",
+         "__global__ void __launch_bounds__(512) PrecomputeRGBLUTKernel", count=1)
+    (GPU_CORE / GPU_STAMP).write_text(GPU_PATCH_VERSION)
+    return GPU_CORE
+
+
+def build_ref_gpu() -> Path:
+    """Compile the reference GPU renderer and its headless driver (parallel TUs)."""
+    import concurrent.futures as cf
+    if not GPU_CORE.is_dir():
+        prepare_gpu()
+    exe = OUT / "ref_gpu"
+    srcs = [HERE / "ref_gpu_driver.cu", GPU_CORE / GPU_STAMP]
+    if exe.exists() and all(exe.stat().st_mtime > s.stat().st_mtime for s in srcs if s.exists()):
+        return exe
+    objdir = OUT / "gpu_obj"
+    objdir.mkdir(exist_ok=True)
+    flags = ["-std=c++17", "-O3", "-DNDEBUG", "-DLINUX=1", "-rdc=true", "--extended-lambda", "-use_fast_math",
+             "-maxrregcount=168", "-gencode", "arch=compute_103a,code=sm_103a", "-diag-suppress",
+             "1866,20012,177,550,128,2417,20011,20014", "-I", str(GPU_CORE), "-I", str(GPU_CORE / "render"),
+             "-I", str(GPU_CORE / "object"), "-I", str(GPU_CORE / "object" / "sdf")]
+    tus = [GPU_CORE / t for t in GPU_TUS] + [HERE / "ref_gpu_driver.cu"]
+    objs = [objdir / (t.name + ".o") for t in tus]
+
+    def one(i):
+        return subprocess.run([nvcc(), *flags, "-c", str(tus[i]), "-o", str(objs[i])], capture_output=True, text=True)
+
+    with cf.ThreadPoolExecutor(len(tus)) as ex:
+        for r in ex.map(one, range(len(tus))):
+            if r.returncode != 0:
+                sys.stderr.write(r.stdout + r.stderr)
+                raise RuntimeError("reference GPU renderer build failed")
+    r = subprocess.run([nvcc(), "-rdc=true", "-gencode", "arch=compute_103a,code=sm_103a", *map(str, objs), "-o",
+                        str(exe)], capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("reference GPU renderer link failed")
+    return exe
+
+
 if __name__ == "__main__":
     if "--reference" in sys.argv:
         REF_ROOT = Path(sys.argv[sys.argv.index("--reference") + 1])
