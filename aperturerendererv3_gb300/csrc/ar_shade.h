@@ -61,6 +61,7 @@ struct Hit
     bool hit;
     int obj;
     int light;
+    int material;  // material index of the hit primitive (set by the kernels' hit reconstruction)
     float dist;
     V3 pos, nrm;
     V3 local_pos;

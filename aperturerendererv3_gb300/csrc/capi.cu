@@ -1056,6 +1056,18 @@ ar_status ar_scene_build(ar_ctx* ctx)
     if (objs.empty()) objs.resize(1);
     AR_CUDA(ctx, alloc_dev(c.d_nodes, c.bvh.nodes.size() * sizeof(ar_wide_node)));
     AR_CUDA(ctx, cudaMemcpy(c.d_nodes, c.bvh.nodes.data(), c.bvh.nodes.size() * sizeof(ar_wide_node), cudaMemcpyHostToDevice));
+    // triangle slots carry their primitive's material and light index in the
+    // spare w lanes of their second and third float4 (read by the shading's hit
+    // reconstruction; the traversal reads only the vertices and the tag)
+    for (ar_prim_slot& sl : c.bvh.slots)
+    {
+        uint32_t tag;
+        std::memcpy(&tag, &sl.a[3], 4);
+        if ((tag >> AR_PRIM_KIND_SHIFT) != AR_PRIM_KIND_TRI) continue;
+        const int32_t mi = prim_material[tag & AR_PRIM_ID_MASK], li = prim_light[tag & AR_PRIM_ID_MASK];
+        std::memcpy(&sl.b[3], &mi, 4);
+        std::memcpy(&sl.c[3], &li, 4);
+    }
     AR_CUDA(ctx, alloc_dev(c.d_slots, c.bvh.slots.size() * sizeof(ar_prim_slot)));
     AR_CUDA(ctx, cudaMemcpy(c.d_slots, c.bvh.slots.data(), c.bvh.slots.size() * sizeof(ar_prim_slot), cudaMemcpyHostToDevice));
     if (nmesh > 0 && !c.bvh.nodes.empty())

@@ -102,6 +102,7 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
         h->hit = true;
         h->obj = id;
         h->light = sc.prim_light[id];
+        h->material = sc.prim_material[id];
         h->dist = t;
         h->pos = o + d * t;
         const float4 n = *sdf_nrm;
@@ -117,17 +118,22 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
     const int id = (int)(tag & AR_PRIM_ID_MASK);
     h->hit = true;
     h->obj = id;
-    h->light = sc.prim_light[id];
     h->dist = t;
     if (kind == AR_PRIM_KIND_TRI)
     {
+        // triangle slots carry their primitive's material and light index in the
+        // spare w lanes (filled at upload): no dependent per-primitive table reads
         const float4 b = __ldg(&sc.trav.slots[3 * (size_t)slot + 1]);
         const float4 c = __ldg(&sc.trav.slots[3 * (size_t)slot + 2]);
+        h->material = __float_as_int(b.w);
+        h->light = __float_as_int(c.w);
         tri_frame(o, d, t, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), &h->pos, &h->nrm);
         h->local_pos = v3(0.0f, 0.0f, 0.0f);
     }
     else if (kind == AR_PRIM_KIND_SDF)
     {
+        h->material = sc.prim_material[id];
+        h->light = sc.prim_light[id];
         // IntersectSDFObject's hit frame (core/object/sdf/sdf_base.cuh:140-151); slot is in sdf_trav
         const Object ob = sc.trav.objects[id];
         const V3 lo = mul(ob.w2o, o - ob.center);
@@ -140,6 +146,8 @@ __device__ __forceinline__ void hit_context(const DevScene& sc, int slot, V3 o, 
     }
     else
     {
+        h->material = sc.prim_material[id];
+        h->light = sc.prim_light[id];
         const Object ob = sc.trav.objects[id];
         if (kind == AR_PRIM_KIND_BOX) intersect_box(o, d, ob, h, true);
         else intersect_sphere(o, d, ob, h, true);
@@ -756,7 +764,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             int texel = -1;
             if (h.hit)
             {
-                mat = sc.materials[sc.prim_material[h.obj]];
+                mat = sc.materials[h.material];
                 if ((FEAT & AR_FEAT_TEX) && mat.albedo_tex >= 0 && sc.tex_count > 0)
                 {
                     texel = albedo_texel(sc, mat.albedo_tex, slot, h.obj, h.pos);
@@ -798,7 +806,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             {
                 if (prm.gbuf && depth == 0)
                 {
-                    const int mid = h.hit ? sc.prim_material[h.obj] : -1;
+                    const int mid = h.hit ? h.material : -1;
                     const V3 alb = h.hit ? mat.albedo : v3(0.0f, 0.0f, 0.0f);
                     prm.gbuf[2 * (size_t)p] = make_float4(alb.x, alb.y, alb.z, __int_as_float(mid));
                     prm.gbuf[2 * (size_t)p + 1] = make_float4(h.nrm.x, h.nrm.y, h.nrm.z, h.dist);
