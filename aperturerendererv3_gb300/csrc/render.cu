@@ -644,14 +644,20 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
     // add the sky and end, hits run the BSDF, NEE and roulette, so grouping
     // them gives the heavy part whole warps of hits.  Which thread shades which
     // path does not change any path's result.
-    __shared__ int s_order[AR_BLOCK];
+    __shared__ int s_order[AR_BLOCK], s_slot[AR_BLOCK];
     __shared__ int s_warp_hits[AR_BLOCK / 32], s_warp_miss[AR_BLOCK / 32];
+    // Without glass the path never enters an object: its media record stays
+    // the default and is neither read nor written.  Unguided forward renders
+    // read nothing of an ended path but its radiance.
+    constexpr bool TRACK_MEDIA = (FEAT & AR_MATS_GLASS) != 0;
+    constexpr bool STORE_ENDED = GUIDE != 0 || ADJ;
     for (int bbase = blockIdx.x * blockDim.x; bbase < n; bbase += stride)
     {
         {
             const int qq = bbase + (int)threadIdx.x;
             const int pp = qq < n ? queue[qq] : -1;
-            const bool is_hit = pp >= 0 && ps.hit_slot[pp] != -1;
+            const int sl = pp >= 0 ? ps.hit_slot[pp] : -1;
+            const bool is_hit = pp >= 0 && sl != -1;
             const bool is_miss = pp >= 0 && !is_hit;
             const unsigned hb = __ballot_sync(0xffffffffu, is_hit), mb = __ballot_sync(0xffffffffu, is_miss);
             const int w = threadIdx.x >> 5;
@@ -672,8 +678,18 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                 n_hits += s_warp_hits[k];
             }
             const unsigned below = (1u << lane_id()) - 1u;
-            if (is_hit) s_order[hit_base + __popc(hb & below)] = pp;
-            if (is_miss) s_order[n_hits + miss_base + __popc(mb & below)] = pp;
+            if (is_hit)
+            {
+                const int o = hit_base + __popc(hb & below);
+                s_order[o] = pp;
+                s_slot[o] = sl;
+            }
+            if (is_miss)
+            {
+                const int o = n_hits + miss_base + __popc(mb & below);
+                s_order[o] = pp;
+                s_slot[o] = -1;
+            }
             __syncthreads();
         }
         const int n_block = min((int)blockDim.x, n - bbase);
@@ -696,22 +712,24 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             int depth = (int)(dep & 0xffffu);
             int ndd = (int)(dep >> 16);
             uint32_t fl = ps.flags[p];
-            const float4 mv = ps.media_v[p];
-            Media media;
-            media.inside = (fl & 1u) != 0u;
-            media.vertex = v3(mv.x, mv.y, mv.z);
-            media.obj = __float_as_int(mv.w);
-            media.depth = ps.media_depth[p];
+            Media media = media_default();
+            if constexpr (TRACK_MEDIA)
+            {
+                const float4 mv = ps.media_v[p];
+                media.inside = (fl & 1u) != 0u;
+                media.vertex = v3(mv.x, mv.y, mv.z);
+                media.obj = __float_as_int(mv.w);
+                media.depth = ps.media_depth[p];
+            }
             float radiance = ps.radiance[p];
             float mask = ps.mask[p];
-            const float4 pv = ps.prev[p];
             const bool prev_did_nee = (fl & 2u) != 0u;
             DevRand R;
             R.g.state = ps.rng[p];
             R.g.inc = ar_pcg_increment(ps.pixel[p]);
 
             const float eps = intersect_eps(ndd);
-            const int slot = ps.hit_slot[p];
+            const int slot = s_slot[threadIdx.x];
             Hit h;
             h.hit = false;
             h.obj = -1;
@@ -930,6 +948,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                 float misW = 1.0f;
                 if (prm.use_nee && depth > 0 && prev_did_nee)
                 {
+                    const float4 pv = ps.prev[p];
                     const float pB = fmaxf(pv.w, 0.0f);
                     const Light L = sc.lights[h.light];
                     float pL = 0.0f;
@@ -1134,14 +1153,21 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                         ps.mask[p] = mask;
                         ps.depths[p] = (uint32_t)depth | ((uint32_t)ndd << 16);
                         fl = (fl & ~1u) | (media.inside ? 1u : 0u);
-                        ps.media_v[p] = make_float4(media.vertex.x, media.vertex.y, media.vertex.z, __int_as_float(media.obj));
-                        ps.media_depth[p] = media.depth;
+                        if constexpr (TRACK_MEDIA)
+                        {
+                            ps.media_v[p] = make_float4(media.vertex.x, media.vertex.y, media.vertex.z,
+                                                        __int_as_float(media.obj));
+                            ps.media_depth[p] = media.depth;
+                        }
                     }
                 }
             }
             ps.radiance[p] = radiance;
-            ps.flags[p] = fl;
-            ps.rng[p] = R.g.state;
+            if (STORE_ENDED || keep)
+            {
+                ps.flags[p] = fl;
+                ps.rng[p] = R.g.state;
+            }
         }
         const int nq = warp_append_slot(next_counter, keep);
         if (keep) next_queue[nq] = p;
