@@ -159,7 +159,7 @@ struct StageEvent
 
 // Per-path state of the wavefront integrator (structure of arrays).
 // ints in a render wave's counter array (layout: AR_CNT_* in render.cu)
-#define AR_CNT_COUNT 8
+#define AR_CNT_COUNT 10
 
 struct PathState
 {
@@ -177,6 +177,8 @@ struct PathState
     float4* prev;       // xyz last vertex, w = last BSDF pdf
     float* hit_t;
     int* hit_slot;
+    int* q_slot;        // hit_slot again, indexed by the path's entry in the extended queue:
+                        // k_shade reads it beside the queue entry instead of after it
     float4* hit_nrm;    // normal of SDF hits (computed by k_extend), xyz
     float* out_xyz;     // 3 per path
     int capacity;
@@ -314,6 +316,7 @@ struct Ctx
     PathState ps{};
     ShadowQueue sq{};
     int* d_queue[2] = {nullptr, nullptr};
+    int2* d_pq = nullptr;  // the extended queue ordered for shading (k_partition)
     double* d_accum = nullptr;
     size_t accum_pixels = 0;
     int wave_capacity = 0;
@@ -403,6 +406,7 @@ struct WaveBuffers
     PathState ps;
     ShadowQueue sq;
     int* queue[2];
+    int2* pq;
     int* counters;   // AR_CNT_COUNT ints
     double* accum;   // 3 doubles per pixel
     int* pend_list;  // shadow rays left for the SDF pass

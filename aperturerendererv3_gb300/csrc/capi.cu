@@ -164,10 +164,11 @@ void free_waves(Ctx& c)
     PathState& p = c.ps;
     free_dev(p.rng); free_dev(p.pixel); free_dev(p.frame); free_dev(p.ray_o); free_dev(p.ray_d);
     free_dev(p.radiance); free_dev(p.mask); free_dev(p.depths); free_dev(p.flags); free_dev(p.media_v);
-    free_dev(p.media_depth); free_dev(p.prev); free_dev(p.hit_t); free_dev(p.hit_slot); free_dev(p.hit_nrm); free_dev(c.d_pend_list); free_dev(p.out_xyz);
+    free_dev(p.media_depth); free_dev(p.prev); free_dev(p.hit_t); free_dev(p.hit_slot); free_dev(p.q_slot); free_dev(p.hit_nrm); free_dev(c.d_pend_list); free_dev(p.out_xyz);
     free_dev(c.sq.path); free_dev(c.sq.o); free_dev(c.sq.d); free_dev(c.sq.v_occ); free_dev(c.sq.valid_unocc); free_dev(c.sq.sdf_eps);
     free_dev(c.d_queue[0]);
     free_dev(c.d_queue[1]);
+    free_dev(c.d_pq);
     c.wave_capacity = 0;
     p.capacity = 0;
 }
@@ -199,6 +200,7 @@ ar_status ensure_waves(ar_ctx* ctx, int cap)
     AR_CUDA(ctx, alloc_dev(p.prev, n));
     AR_CUDA(ctx, alloc_dev(p.hit_t, n));
     AR_CUDA(ctx, alloc_dev(p.hit_slot, n));
+    AR_CUDA(ctx, alloc_dev(p.q_slot, n));
     AR_CUDA(ctx, alloc_dev(p.hit_nrm, n));
     AR_CUDA(ctx, alloc_dev(c.d_pend_list, n));
     AR_CUDA(ctx, alloc_dev(p.out_xyz, 3 * n));
@@ -210,6 +212,7 @@ ar_status ensure_waves(ar_ctx* ctx, int cap)
     AR_CUDA(ctx, alloc_dev(c.sq.sdf_eps, n));
     AR_CUDA(ctx, alloc_dev(c.d_queue[0], n));
     AR_CUDA(ctx, alloc_dev(c.d_queue[1], n));
+    AR_CUDA(ctx, alloc_dev(c.d_pq, n));
     p.capacity = cap;
     c.wave_capacity = cap;
     return AR_OK;

@@ -43,8 +43,9 @@ using namespace ar;
 constexpr size_t kPathBytes = sizeof(uint64_t) + 2 * sizeof(uint32_t) + 2 * sizeof(float4) + 2 * sizeof(float) +
                               2 * sizeof(uint32_t) + sizeof(float4) + sizeof(int) + sizeof(float4) + sizeof(float) +
                               sizeof(int) + 3 * sizeof(float) + sizeof(int) + 2 * sizeof(float4) + sizeof(float) +
-                              sizeof(uint8_t) + sizeof(float) + 2 * sizeof(int) + sizeof(float4) + sizeof(int);
-constexpr int kArrays = 25;
+                              sizeof(uint8_t) + sizeof(float) + 2 * sizeof(int) + sizeof(float4) + sizeof(int) +
+                              sizeof(int) + sizeof(int2);
+constexpr int kArrays = 27;
 constexpr size_t kAlign = 256;
 // largest wave that fits the scratch array (array starts padded to 256 bytes)
 constexpr int kMaxPaths = (int)(((AR_NOALLOC_SCRATCH_BYTES - kAlign * (kArrays + 1)) / kPathBytes) & ~255u);
@@ -133,6 +134,7 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
     wb.ps.prev = carve<float4>(cur, n);
     wb.ps.hit_t = carve<float>(cur, n);
     wb.ps.hit_slot = carve<int>(cur, n);
+    wb.ps.q_slot = carve<int>(cur, n);
     wb.ps.hit_nrm = carve<float4>(cur, n);
     wb.ps.out_xyz = carve<float>(cur, 3 * n);
     wb.ps.capacity = cap;
@@ -144,6 +146,7 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
     wb.sq.sdf_eps = carve<float>(cur, n);
     wb.queue[0] = carve<int>(cur, n);
     wb.queue[1] = carve<int>(cur, n);
+    wb.pq = carve<int2>(cur, n);
     wb.counters = carve<int>(cur, AR_CNT_COUNT);
     wb.pend_list = carve<int>(cur, n);
     if ((size_t)(cur - base) > AR_NOALLOC_SCRATCH_BYTES)

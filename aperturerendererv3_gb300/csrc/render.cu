@@ -194,6 +194,7 @@ __device__ __forceinline__ int albedo_texel(const DevScene& sc, int tex, int slo
 #define AR_CNT_MLP 3
 #define AR_CNT_FETCH 4       // k_extend, k_shadow fetch counters
 #define AR_CNT_PEND 6        // pending SDF work of k_extend, k_shadow
+#define AR_CNT_PART 8        // k_partition: hits placed from the front, misses from the back
 
 // ---------------------------------------------------------------- raygen
 struct CamParams
@@ -329,6 +330,8 @@ struct CounterReset
     int* b;
     int* c;
     int* d;
+    int* e = nullptr;
+    int* f = nullptr;
 };
 
 __device__ __forceinline__ void reset_counters(const CounterReset& r)
@@ -339,6 +342,8 @@ __device__ __forceinline__ void reset_counters(const CounterReset& r)
         if (r.b) *r.b = 0;
         if (r.c) *r.c = 0;
         if (r.d) *r.d = 0;
+        if (r.e) *r.e = 0;
+        if (r.f) *r.f = 0;
     }
 }
 
@@ -351,7 +356,8 @@ struct SdfPending
 };
 
 // closest hit of a finished traversal of the main BVH
-__device__ __forceinline__ void extend_finish(const DevScene& sc, const PathState& ps, int p, const TravState<false>& st)
+__device__ __forceinline__ void extend_finish(const DevScene& sc, const PathState& ps, int p, int q,
+                                              const TravState<false>& st)
 {
     const TravResult r = st.result();
     if (sc.stats)
@@ -362,6 +368,7 @@ __device__ __forceinline__ void extend_finish(const DevScene& sc, const PathStat
     }
     ps.hit_t[p] = r.t;
     ps.hit_slot[p] = r.slot;
+    ps.q_slot[q] = r.slot;
 }
 
 // The SDF pass of the closest hits (scenes with SDF geometry only): the SDF
@@ -438,6 +445,7 @@ __global__ void __launch_bounds__(AR_BLOCK) k_sdf_extend(DevScene sc, PathState 
         }
         ps.hit_t[p] = t;
         ps.hit_slot[p] = slot;
+        ps.q_slot[q] = slot;
     }
 }
 
@@ -449,19 +457,19 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
     const int n = *counter;
     TravState<false> st;
     uint2 stk[AR_TRAV_STACK];
-    int p = 0;
+    int p = 0, q = 0;
     bool active = false, exhausted = false;
     while (true)
     {
-        int q;
         if (warp_refill(fetch, n, active, &exhausted, &q, min_idle))
         {
             p = queue[q];
             const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
             const V3 o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
             const float tmin = intersect_eps((int)(ps.depths[p] >> 16));
-            const int mobj = __float_as_int(ps.media_v[p].w);
-            if ((ps.flags[p] & 1u) && mobj >= 0)
+            // the media record is read only for rays inside an object (rare)
+            const int mobj = (ps.flags[p] & 1u) ? __float_as_int(ps.media_v[p].w) : -1;
+            if (mobj >= 0)
             {
                 // inside a medium: intersect only the enclosing object (render.cuh:89-92);
                 // an SDF object is left to the SDF pass
@@ -469,6 +477,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
                 {
                     ps.hit_t[p] = 0.0f;
                     ps.hit_slot[p] = AR_SLOT_SOLO;
+                    ps.q_slot[q] = AR_SLOT_SOLO;
                 }
                 else
                 {
@@ -477,6 +486,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
                     const float th = prim_hit<false>(sc.trav, s, make_shear(d), o, d, &id, tmin);
                     ps.hit_t[p] = th >= tmin ? th : 0.0f;
                     ps.hit_slot[p] = th >= tmin ? s : -1;
+                    ps.q_slot[q] = th >= tmin ? s : -1;
                 }
                 if (sc.stats) atomicAdd(&sc.stats[4], 1ull);
             }
@@ -497,7 +507,7 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
             {
                 if (!st.step(sc.trav, err))
                 {
-                    extend_finish(sc, ps, p, st);
+                    extend_finish(sc, ps, p, q, st);
                     active = false;
                     break;
                 }
@@ -613,6 +623,56 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
     }
 }
 
+// The extended queue ordered for shading: hits with their slot from the front,
+// misses from the back.  k_shade then gives whole warps and blocks to one kind
+// of work (a hit runs the BSDF, NEE and roulette; a miss adds the sky and
+// ends) without reordering inside the kernel.  One atomic per block and end.
+// Which thread shades which path does not change any path's result.
+__global__ void __launch_bounds__(AR_BLOCK) k_partition(const int* __restrict__ queue, const int* __restrict__ q_slot,
+                                                        const int* __restrict__ counter, int2* __restrict__ out,
+                                                        int* front, int* back)
+{
+    const int n = *counter;
+    __shared__ int s_hits[AR_BLOCK / 32], s_miss[AR_BLOCK / 32], s_base[2];
+    const int w = threadIdx.x >> 5;
+    for (int bbase = blockIdx.x * blockDim.x; bbase < n; bbase += gridDim.x * blockDim.x)
+    {
+        const int q = bbase + (int)threadIdx.x;
+        const bool valid = q < n;
+        const int p = valid ? queue[q] : -1;
+        const int slot = valid ? q_slot[q] : -1;
+        const bool hit = valid && slot != -1;
+        const unsigned hb = __ballot_sync(0xffffffffu, hit), mb = __ballot_sync(0xffffffffu, valid && !hit);
+        if (lane_id() == 0)
+        {
+            s_hits[w] = __popc(hb);
+            s_miss[w] = __popc(mb);
+        }
+        __syncthreads();
+        int hbase = 0, mbase = 0, th = 0, tm = 0;
+        for (int k = 0; k < AR_BLOCK / 32; ++k)
+        {
+            if (k < w)
+            {
+                hbase += s_hits[k];
+                mbase += s_miss[k];
+            }
+            th += s_hits[k];
+            tm += s_miss[k];
+        }
+        if (threadIdx.x == 0)
+        {
+            s_base[0] = th ? atomicAdd(front, th) : 0;
+            s_base[1] = tm ? atomicAdd(back, tm) : 0;
+        }
+        __syncthreads();
+        const unsigned below = (1u << lane_id()) - 1u;
+        if (hit) out[s_base[0] + hbase + __popc(hb & below)] = make_int2(p, slot);
+        else if (valid) out[n - 1 - (s_base[1] + mbase + __popc(mb & below))] = make_int2(p, -1);
+        __syncthreads();  // the shared counts are rewritten by the next pass
+    }
+}
+
 // Scene features a k_shade instantiation handles, fixed at compile time: the
 // BSDF models (AR_MATS_* bits), the participating medium and albedo textures.
 // Scenes of opaque surfaces only (no glass, medium or textures, the camera
@@ -626,7 +686,7 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
 template <int GUIDE, bool ADJ, int FEAT = AR_FEAT_ALL>
 __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
                                             : (FEAT == AR_FEAT_SURFACE ? AR_SHADE_LEAN_MIN_BLOCKS : AR_SHADE_MIN_BLOCKS))
-    k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int* __restrict__ queue,
+    k_shade(DevScene sc, PathState ps, ShadowQueue sq, const int2* __restrict__ queue,
                                                   const int* __restrict__ counter, int* next_queue, int* next_counter,
                                                   int* shadow_counter, ShadeParams prm)
 {
@@ -639,13 +699,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
     __syncthreads();
     const int stride = gridDim.x * blockDim.x;
     float g_med_albedo = 0.0f, g_med_emission = 0.0f;  // replay adjoint of the medium parameters
-    // Each pass of the block takes blockDim.x queue entries and reorders them in
-    // shared memory: rays that hit something first, misses after.  Misses only
-    // add the sky and end, hits run the BSDF, NEE and roulette, so grouping
-    // them gives the heavy part whole warps of hits.  Which thread shades which
-    // path does not change any path's result.
-    __shared__ int s_order[AR_BLOCK], s_slot[AR_BLOCK];
-    __shared__ int s_warp_hits[AR_BLOCK / 32], s_warp_miss[AR_BLOCK / 32];
+    // The queue comes from k_partition: {path, hit slot}, hits first.
     // Without glass the path never enters an object: its media record stays
     // the default and is neither read nor written.  Unguided forward renders
     // read nothing of an ended path but its radiance.
@@ -653,47 +707,8 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
     constexpr bool STORE_ENDED = GUIDE != 0 || ADJ;
     for (int bbase = blockIdx.x * blockDim.x; bbase < n; bbase += stride)
     {
-        {
-            const int qq = bbase + (int)threadIdx.x;
-            const int pp = qq < n ? queue[qq] : -1;
-            const int sl = pp >= 0 ? ps.hit_slot[pp] : -1;
-            const bool is_hit = pp >= 0 && sl != -1;
-            const bool is_miss = pp >= 0 && !is_hit;
-            const unsigned hb = __ballot_sync(0xffffffffu, is_hit), mb = __ballot_sync(0xffffffffu, is_miss);
-            const int w = threadIdx.x >> 5;
-            if (lane_id() == 0)
-            {
-                s_warp_hits[w] = __popc(hb);
-                s_warp_miss[w] = __popc(mb);
-            }
-            __syncthreads();
-            int hit_base = 0, miss_base = 0, n_hits = 0;
-            for (int k = 0; k < AR_BLOCK / 32; ++k)
-            {
-                if (k < w)
-                {
-                    hit_base += s_warp_hits[k];
-                    miss_base += s_warp_miss[k];
-                }
-                n_hits += s_warp_hits[k];
-            }
-            const unsigned below = (1u << lane_id()) - 1u;
-            if (is_hit)
-            {
-                const int o = hit_base + __popc(hb & below);
-                s_order[o] = pp;
-                s_slot[o] = sl;
-            }
-            if (is_miss)
-            {
-                const int o = n_hits + miss_base + __popc(mb & below);
-                s_order[o] = pp;
-                s_slot[o] = -1;
-            }
-            __syncthreads();
-        }
-        const int n_block = min((int)blockDim.x, n - bbase);
-        const bool active = (int)threadIdx.x < n_block;
+        const int qq = bbase + (int)threadIdx.x;
+        const bool active = qq < n;
         bool keep = false;
         bool shadow = false;
         int p = 0;
@@ -702,7 +717,8 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
         bool sh_valid = false;
         if (active)
         {
-            p = s_order[threadIdx.x];
+            const int2 entry = queue[qq];
+            p = entry.x;
             const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
             const V3 rayO = v3(ro.x, ro.y, ro.z), rayD = v3(rd.x, rd.y, rd.z);
             const float lambda = ro.w;
@@ -729,7 +745,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             R.g.inc = ar_pcg_increment(ps.pixel[p]);
 
             const float eps = intersect_eps(ndd);
-            const int slot = s_slot[threadIdx.x];
+            const int slot = entry.y;
             Hit h;
             h.hit = false;
             h.obj = -1;
@@ -1181,7 +1197,6 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             sq.valid_unocc[sqi] = sh_valid ? 1 : 0;
             sq.sdf_eps[sqi] = sh_sdf_eps;
         }
-        __syncthreads();  // s_order is refilled by the next pass
     }
     if constexpr (ADJ)
     {
@@ -1486,7 +1501,8 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         int* qn = &cnt[AR_CNT_Q0 + cur];
         // k_extend zeroes the next queue, shadow queue, shadow fetch and pending
         // counters; k_shadow zeroes the next k_extend's fetch counter
-        const CounterReset ext_rs{&cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], &cnt[AR_CNT_PEND]};
+        const CounterReset ext_rs{&cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1],
+                                  &cnt[AR_CNT_PEND], &cnt[AR_CNT_PART], &cnt[AR_CNT_PART + 1]};
         const CounterReset shd_rs{&cnt[AR_CNT_FETCH], nullptr, nullptr, nullptr};
         {
             StageScope st(c, ST_EXTEND);
@@ -1500,6 +1516,9 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         }
         {
             StageScope st(c, ST_SHADE);
+            k_partition<<<grid_s, AR_BLOCK, 0, s>>>(c.d_queue[cur], c.ps.q_slot, qn, c.d_pq, &cnt[AR_CNT_PART],
+                                                    &cnt[AR_CNT_PART + 1]);
+            ++L;
             if (rl.guide == 2 && rl.mlp_ready)
             {
                 // network inference for every queued hit (tensor cores), before shading
@@ -1512,17 +1531,17 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
             int* shc = &cnt[AR_CNT_SHADOW];
             int* nq = c.d_queue[nxt];
             int* nn = &cnt[AR_CNT_Q0 + nxt];
+            const int2* pq = c.d_pq;
             if (rl.guide == 2)
-                k_shade<2, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+                k_shade<2, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pq, qn, nq, nn, shc, prm);
             else if (rl.guide)
-                k_shade<1, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+                k_shade<1, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pq, qn, nq, nn, shc, prm);
             else if (rl.adjoint)
-                k_shade<0, true><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+                k_shade<0, true><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pq, qn, nq, nn, shc, prm);
             else if (lean)
-                k_shade<0, false, AR_FEAT_SURFACE><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn,
-                                                                              shc, prm);
+                k_shade<0, false, AR_FEAT_SURFACE><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pq, qn, nq, nn, shc, prm);
             else
-                k_shade<0, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, c.d_queue[cur], qn, nq, nn, shc, prm);
+                k_shade<0, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.sq, pq, qn, nq, nn, shc, prm);
         }
         {
             StageScope st(c, ST_SHADOW);
@@ -1583,12 +1602,15 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
-        const CounterReset ext_rs{&cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], &cnt[AR_CNT_PEND]};
+        const CounterReset ext_rs{&cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1],
+                                  &cnt[AR_CNT_PEND], &cnt[AR_CNT_PART], &cnt[AR_CNT_PART + 1]};
         const CounterReset shd_rs{&cnt[AR_CNT_FETCH], nullptr, nullptr, nullptr};
         k_extend<<<grid_t, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur], &cnt[AR_CNT_FETCH], err,
                                              b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN, ext_rs);
         if (has_sdf) k_sdf_extend<<<grid_s, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.queue[cur], &cnt[AR_CNT_Q0 + cur]);
-        k_shade<0, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.queue[cur], &cnt[AR_CNT_Q0 + cur],
+        k_partition<<<grid_s, AR_BLOCK, 0, s>>>(wb.queue[cur], wb.ps.q_slot, &cnt[AR_CNT_Q0 + cur], wb.pq,
+                                                &cnt[AR_CNT_PART], &cnt[AR_CNT_PART + 1]);
+        k_shade<0, false><<<grid_s, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, wb.pq, &cnt[AR_CNT_Q0 + cur],
                                                    wb.queue[nxt], &cnt[AR_CNT_Q0 + nxt], &cnt[AR_CNT_SHADOW], prm);
         k_shadow<<<grid_t, AR_BLOCK, 0, s>>>(sc, wb.ps, wb.sq, &cnt[AR_CNT_SHADOW], &cnt[AR_CNT_FETCH + 1], pend_shd, err,
                                              b == 0 ? AR_SHD_REFILL_MIN0 : AR_SHD_REFILL_MIN, shd_rs);

@@ -308,7 +308,7 @@ ar_status ar_trace_any(ar_ctx* ctx, const float* rays, int n, int32_t* hit, void
  * stream).  No cudaMalloc / cudaFree is made; profiling (params->profile) is
  * rejected. */
 #define AR_NOALLOC_SCRATCH_BYTES (8u << 20)
-#define AR_NOALLOC_MAX_PATHS 43264
+#define AR_NOALLOC_MAX_PATHS 40704
 ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* params, double* out_xyz_device, void* stream);
 
 /* Replay adjoint (no counterpart in the reference).  Gradient of a scalar loss

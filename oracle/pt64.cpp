@@ -156,6 +156,13 @@ struct Scene
     std::vector<std::array<R, 7>> sdf;
     R sdf_k = 0;
     R sdf_lo[3] = {0, 0, 0}, sdf_hi[3] = {0, 0, 0};
+    // sdf_f32: the SDF march and normal run in float, as a float renderer
+    // runs them: positions and steps rounded to float, the field evaluated in
+    // float arithmetic.  The central-difference normal (h = 1e-4) divides the
+    // field's rounding error by 2h and the march's stopping step can move by
+    // one step, so renders with it on and off show how far float arithmetic
+    // of the SDF alone moves each sample.
+    bool sdf_f32 = false;
     bool med_on = false;
     R med_lo[3] = {0, 0, 0}, med_hi[3] = {0, 0, 0};
     R med_sigma = 0, med_albedo = 0, med_g = 0, med_emission = 0;
@@ -556,6 +563,44 @@ static R sdf_eval(const Scene& S, V p)
     return d;
 }
 
+static R to_f32(R x) { return (R)(float)x; }
+static V to_f32(V p) { return v(to_f32(p.x), to_f32(p.y), to_f32(p.z)); }
+
+// sdf_prim and sdf_eval in float arithmetic (same operations and order)
+static float sdf_prim_f(const std::array<R, 7>& q, float px, float py, float pz)
+{
+    const float x = px - (float)q[1], y = py - (float)q[2], z = pz - (float)q[3];
+    const int kind = (int)q[0];
+    if (kind == 0) return std::sqrt(x * x + y * y + z * z) - (float)q[4];
+    if (kind == 1)
+    {
+        const float dx = std::fabs(x) - (float)q[4], dy = std::fabs(y) - (float)q[5], dz = std::fabs(z) - (float)q[6];
+        const float ex = std::max(dx, 0.0f), ey = std::max(dy, 0.0f), ez = std::max(dz, 0.0f);
+        return std::sqrt(ex * ex + ey * ey + ez * ez) + std::min(std::max(dx, std::max(dy, dz)), 0.0f);
+    }
+    const float rxz = std::sqrt(x * x + z * z) - (float)q[4];
+    return std::sqrt(rxz * rxz + y * y) - (float)q[5];
+}
+
+static float sdf_eval_f(const Scene& S, float px, float py, float pz)
+{
+    const float k = (float)S.sdf_k;
+    float d = sdf_prim_f(S.sdf[0], px, py, pz);
+    for (size_t i = 1; i < S.sdf.size(); ++i)
+    {
+        const float b = sdf_prim_f(S.sdf[i], px, py, pz);
+        const float h = std::max(k - std::fabs(d - b), 0.0f) / k;
+        d = std::min(d, b) - h * h * k * 0.25f;
+    }
+    return d;
+}
+
+// the SDF at p; under sdf_f32 evaluated in float at p rounded to float
+static R sdf_at(const Scene& S, V p)
+{
+    return S.sdf_f32 ? (R)sdf_eval_f(S, (float)p.x, (float)p.y, (float)p.z) : sdf_eval(S, p);
+}
+
 static bool slab(const R lo[3], const R hi[3], V o, V d, R* t0, R* t1)
 {
     R a0 = -1e300, a1 = 1e300;
@@ -578,13 +623,15 @@ static R sdf_march(const Scene& S, V o, V d, R eps)
 {
     R t0, t1;
     if (S.sdf.empty() || !slab(S.sdf_lo, S.sdf_hi, o, d, &t0, &t1) || t1 <= 0) return -1.0;
-    const bool inside = sdf_eval(S, o) <= 0.0;
+    const bool inside = sdf_at(S, o) <= 0.0;
     R t = std::max(0.0, t0);
+    if (S.sdf_f32) t = to_f32(t);
     for (int i = 0; i < 512; ++i)
     {
-        const R dist = sdf_eval(S, o + d * t);
+        const R dist = sdf_at(S, o + d * t);
         if (inside ? (dist > 0 && dist < eps) : (dist < 0 && -dist < eps)) return t;
         t += std::max(std::fabs(dist), eps * 0.5);
+        if (S.sdf_f32) t = to_f32(t);
         if (t > t1) break;
     }
     return -1.0;
@@ -745,12 +792,12 @@ static void hit_record(const Scene& S, int p, V o, V d, R t, Hit* h)
     else if (S.prim_type[p] == OBJ_CUBE) box_hit(o, d, S.objs[p], h, true);
     else if (S.prim_type[p] == OBJ_SDF)
     {
-        h->pos = o + d * t;
+        h->pos = S.sdf_f32 ? to_f32(o + d * t) : o + d * t;
         const R e = 1e-4;
         const V p0 = h->pos;
-        h->nrm = normalize(v(sdf_eval(S, p0 + v(e, 0, 0)) - sdf_eval(S, p0 - v(e, 0, 0)),
-                             sdf_eval(S, p0 + v(0, e, 0)) - sdf_eval(S, p0 - v(0, e, 0)),
-                             sdf_eval(S, p0 + v(0, 0, e)) - sdf_eval(S, p0 - v(0, 0, e))));
+        h->nrm = normalize(v(sdf_at(S, p0 + v(e, 0, 0)) - sdf_at(S, p0 - v(e, 0, 0)),
+                             sdf_at(S, p0 + v(0, e, 0)) - sdf_at(S, p0 - v(0, e, 0)),
+                             sdf_at(S, p0 + v(0, 0, e)) - sdf_at(S, p0 - v(0, 0, e))));
     }
     else sphere_hit(o, d, S.objs[p], h, true);
 }
@@ -1869,6 +1916,8 @@ int pt64_render(const pt64_scene* s, const int32_t* ip, const double* dp, uint64
     run(*reinterpret_cast<const Scene*>(s), P, mean, per_sample, nullptr, nullptr);
     return 0;
 }
+
+void pt64_set_sdf_f32(pt64_scene* s, int on) { reinterpret_cast<Scene*>(s)->sdf_f32 = on != 0; }
 
 void pt64_set_medium(pt64_scene* s, const double* m)
 {

@@ -42,6 +42,7 @@ def load() -> C.CDLL:
         lib.pt64_create.argtypes = [vp, i32, vp, i32, vp, vp, vp, i32, vp, vp, i32, vp, vp, vp, i32, vp, i32,
                                     vp, i32, C.c_float, i32, C.c_char_p, i32]
         lib.pt64_set_medium.argtypes = [vp, vp]
+        lib.pt64_set_sdf_f32.argtypes = [vp, i32]
         lib.pt64_adjoint_medium.restype = i32
         lib.pt64_adjoint_medium.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
         lib.pt64_destroy.argtypes = [vp]
@@ -126,6 +127,11 @@ class Scene64:
         if not self._h:
             raise ValueError(f"FP64 oracle: {err.value.decode()}")
         self.set_medium(medium)
+
+    def set_sdf_f32(self, on: bool):
+        """Round the SDF march's positions, steps and distances to float (a
+        float-sized perturbation of the SDF arithmetic; off by default)."""
+        load().pt64_set_sdf_f32(self._h, 1 if on else 0)
 
     def set_medium(self, medium):
         if medium is None:

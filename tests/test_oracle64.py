@@ -104,6 +104,31 @@ def test_fp64_sdf_sphere_matches_analytic_sphere():
     assert np.abs(a - b).mean() < 0.02 * a.mean()
 
 
+def test_float_sdf_mode_moves_only_samples_that_see_the_sdf():
+    """The float-SDF diagnostic mode is off by default, leaves scenes without
+    SDF geometry bit for bit, and moves SDF samples by float-sized amounts."""
+    from aperturerendererv3_gb300.scene import Material, SdfUnion
+    from aperturerendererv3_gb300._lib import SDF_SPHERE, SDF_TORUS
+    objs, cam = configs.cornell_triangles(), configs.CORNELL_CAMERA
+    kw = dict(fov=cam["fov"], max_depth=2, per_sample=True)
+    plain = pt64.Scene64(objs)
+    _, a = plain.render((16, 16), cam["origin"], cam["direction"], 2, **kw)
+    plain.set_sdf_f32(True)
+    _, b = plain.render((16, 16), cam["origin"], cam["direction"], 2, **kw)
+    assert np.array_equal(a, b)
+    sdf = SdfUnion([(SDF_SPHERE, (0.1, -0.3, 0.0), (0.12, 0, 0)), (SDF_TORUS, (-0.1, -0.2, 0.05), (0.15, 0.04, 0))],
+                   0.08, Material.CreateDiffusePureColor((0.6, 0.5, 0.4)))
+    S = pt64.Scene64(objs, sdf=sdf)
+    _, c = S.render((16, 16), cam["origin"], cam["direction"], 2, **kw)
+    _, c2 = S.render((16, 16), cam["origin"], cam["direction"], 2, **kw)
+    S.set_sdf_f32(True)
+    _, d = S.render((16, 16), cam["origin"], cam["direction"], 2, **kw)
+    assert np.array_equal(c, c2)
+    rel = (np.abs(d - c) / np.maximum(np.abs(c), 1e-4)).max(-1)
+    assert 0.0 < (rel > 0).mean() < 1.0
+    assert np.quantile(rel, 0.99) < 1e-2
+
+
 def test_fp64_medium_adjoint_is_the_derivative_of_the_fp64_estimator():
     """NEE off, depth 3: the estimator is smooth in the albedo and linear in the emission."""
     from aperturerendererv3_gb300.scene import Medium

@@ -7,6 +7,8 @@ contents, so the second call proves it re-initialises what it must), and
 checked to leave the device's free memory unchanged.
 Collected last on purpose: if it fails, every other test has already run."""
 import ctypes as C
+import re
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -64,6 +66,11 @@ def test_noalloc_camera_inside_an_sdf_object(cuda_device):
     assert r2.error_word() == 0
 
 
+def _max_paths():
+    hdr = (Path(__file__).resolve().parents[1] / "include" / "aperture" / "ar.h").read_text()
+    return int(re.search(r"#define AR_NOALLOC_MAX_PATHS (\d+)", hdr).group(1))
+
+
 def test_noalloc_rejects_waves_beyond_the_scratch_limit(cuda_device):
     import torch
     objs, cam = configs.cornell_triangles(), configs.CORNELL_CAMERA
@@ -71,7 +78,7 @@ def test_noalloc_rejects_waves_beyond_the_scratch_limit(cuda_device):
     r.build()
     lib = _lib.load()
     p = r.params((32, 32), cam["origin"], cam["direction"], 1, fov=cam["fov"], max_depth=4,
-                 wave_paths=43264 + 1)
+                 wave_paths=_max_paths() + 1)
     out = torch.zeros((32, 32, 3), dtype=torch.float64, device="cuda")
     assert lib.ar_render_noalloc(r._ctx, C.byref(p), out.data_ptr(), None) == _lib.AR_ERR_INVALID
     assert b"exceeds the scratch limit" in lib.ar_last_error(r._ctx)
