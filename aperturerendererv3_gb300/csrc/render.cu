@@ -623,6 +623,30 @@ __device__ __forceinline__ void collect_radiance(const PathState& ps, int p, uin
     }
 }
 
+// Prefetch into L2 of the path state k_shade reads first (and of the hit's
+// primitive slot), for a path this thread shades in its next pass.
+__device__ __forceinline__ void prefetch_l2(const void* a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
+
+__device__ __forceinline__ void prefetch_shade_inputs(const DevScene& sc, const PathState& ps, int2 e)
+{
+    const int p = e.x;
+    prefetch_l2(&ps.ray_o[p]);
+    prefetch_l2(&ps.ray_d[p]);
+    prefetch_l2(&ps.rng[p]);
+    prefetch_l2(&ps.pixel[p]);
+    prefetch_l2(&ps.depths[p]);
+    prefetch_l2(&ps.flags[p]);
+    prefetch_l2(&ps.radiance[p]);
+    prefetch_l2(&ps.mask[p]);
+    prefetch_l2(&ps.hit_t[p]);
+    if (e.y >= 0)
+    {
+        const float4* sl = sc.trav.slots + 3 * (size_t)e.y;
+        prefetch_l2(sl);
+        prefetch_l2(sl + 2);
+    }
+}
+
 // The extended queue ordered for shading: hits with their slot from the front,
 // misses from the back.  k_shade then gives whole warps and blocks to one kind
 // of work (a hit runs the BSDF, NEE and roulette; a miss adds the sky and
@@ -709,6 +733,10 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
     {
         const int qq = bbase + (int)threadIdx.x;
         const bool active = qq < n;
+        // the entry this thread shades in its next pass, read now; its state is
+        // prefetched once this pass's own loads have arrived
+        const int qn = qq + stride;
+        const int2 next = qn < n ? queue[qn] : make_int2(-1, -1);
         bool keep = false;
         bool shadow = false;
         int p = 0;
@@ -755,6 +783,7 @@ __global__ void __launch_bounds__(AR_BLOCK, GUIDE == 2 ? AR_SHADE_MLP_MIN_BLOCKS
             h.nrm = v3(0, 0, 0);
             h.local_pos = v3(0, 0, 0);
             if (slot != -1) hit_context(sc, slot, rayO, rayD, ps.hit_t[p], &h, &ps.hit_nrm[p]);
+            if (next.x >= 0) prefetch_shade_inputs(sc, ps, next);
 
             // ---- participating medium: a free flight sampled in the medium box
             // ends the segment early with probability 1 - transmittance
