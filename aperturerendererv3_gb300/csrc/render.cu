@@ -205,7 +205,8 @@ struct CamParams
 
 __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, int* counter, long long first_path, int n,
                                                    int width, int height, uint64_t seed, int first_frame, CamParams cam,
-                                                   int camera_inside, int* fetch_reset)
+                                                   int camera_inside, int* fetch_reset, bool media_record,
+                                                   bool frame_record)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0)
@@ -253,16 +254,21 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
     const LambdaSample ls = sample_cie1931(r0, r1, r2);
     ps.rng[k] = R.g.state;
     ps.pixel[k] = pixel;
-    ps.frame[k] = frame;
+    if (frame_record) ps.frame[k] = frame;  // read by the guided shading only
     ps.ray_o[k] = make_float4(cam.o.x, cam.o.y, cam.o.z, ls.lambda);
     ps.ray_d[k] = make_float4(dir.x, dir.y, dir.z, ls.pdf);
     ps.radiance[k] = 0.0f;
     ps.mask[k] = 1.0f;
     ps.depths[k] = 0u;
     ps.flags[k] = camera_inside ? 1u : 0u;
-    ps.media_v[k] = make_float4(cam.o.x, cam.o.y, cam.o.z, __int_as_float(-1));
-    ps.media_depth[k] = 0;
-    ps.prev[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    // the media record is read only by shading instantiations that track media
+    // (and by k_extend for rays inside an object); prev (last vertex, pdf) is
+    // read only after a vertex has written it (flag bit 1)
+    if (media_record)
+    {
+        ps.media_v[k] = make_float4(cam.o.x, cam.o.y, cam.o.z, __int_as_float(-1));
+        ps.media_depth[k] = 0;
+    }
     queue[k] = k;
 }
 
@@ -1499,10 +1505,14 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     const int grid_s = std::max(2 * sms, (n + AR_BLOCK * AR_SHADE_PATHS_PER_THREAD - 1) / (AR_BLOCK * AR_SHADE_PATHS_PER_THREAD));
     int* cnt = c.d_counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
+    // opaque surfaces only: the shading instantiation without glass, medium and texture code
+    bool lean = !c.medium.on && c.tex_count == 0 && !c.camera_inside && !rl.guide && !rl.adjoint;
+    for (const Material& m : c.materials) lean = lean && m.shading != AR_MAT_GLASS;
     {
         StageScope st(c, ST_RAYGEN);
         k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, c.d_queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height,
-                                             rl.seed, rl.first_frame, cam, c.camera_inside, &cnt[AR_CNT_FETCH]);
+                                             rl.seed, rl.first_frame, cam, c.camera_inside, &cnt[AR_CNT_FETCH], !lean,
+                                             rl.guide != 0);
         if (rl.guide) k_guide_init<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, n);
     }
     long long L = rl.guide ? 2 : 1;
@@ -1521,9 +1531,6 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     // SDF geometry: its work leaves the traversal kernels for k_sdf_extend / k_sdf_shadow
     const bool has_sdf = c.sdf_object_count > 0 || c.sdf.count > 0;
     const SdfPending pend_shd{has_sdf ? c.d_pend_list : nullptr, &cnt[AR_CNT_PEND]};
-    // opaque surfaces only: the shading instantiation without glass, medium and texture code
-    bool lean = !c.medium.on && c.tex_count == 0 && !c.camera_inside;
-    for (const Material& m : c.materials) lean = lean && m.shading != AR_MAT_GLASS;
     for (int b = 0; b < rl.max_depth; ++b)
     {
         const int cur = b & 1, nxt = cur ^ 1;
@@ -1617,7 +1624,7 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     int* cnt = wb.counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
     k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(wb.ps, wb.queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height, rl.seed,
-                                         rl.first_frame, cam, camera_inside, &cnt[AR_CNT_FETCH]);
+                                         rl.first_frame, cam, camera_inside, &cnt[AR_CNT_FETCH], true, false);
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
