@@ -347,6 +347,7 @@ struct Ctx
     float* d_mlp_w32 = nullptr;   // master parameters
     uint16_t* d_mlp_wbf = nullptr;
     float* d_mlp_grad = nullptr;
+    float* d_mlp_gpart = nullptr;  // per-CTA gradient slices of a training step (SMs x AR_MLP_PARAMS)
     float* d_mlp_m = nullptr;
     float* d_mlp_v = nullptr;
     float* d_mlp_loss = nullptr;  // loss sum of the last training step
@@ -377,9 +378,10 @@ cudaError_t mlp_prepare_kernels();
 cudaError_t launch_mlp_infer(const MlpDev& net, const float4* q_pos, const float4* q_wr, const int* queue,
                              const int* count, int n_direct, uint8_t* out, float* logits, unsigned* err, int sms,
                              cudaStream_t s);
+// grad += the step's gradient; part: scratch of min(sms, tiles) x AR_MLP_PARAMS floats (one slice per CTA)
 cudaError_t launch_mlp_train(const MlpDev& net, const float4* r_pos, const float4* r_wr, const float4* r_dir,
                              const float4* r_rad, const int* count, int n_direct, int n_train, int offset, float* grad,
-                             float* loss_sum, unsigned* err, int sms, cudaStream_t s);
+                             float* part, float* loss_sum, unsigned* err, int sms, cudaStream_t s);
 cudaError_t launch_mlp_bias_start(float* w32, const float4* r_rad, const int* count, cudaStream_t s);
 cudaError_t launch_mlp_adam(float* w32, uint16_t* wbf, float* grad, float* m, float* v, int step, float lr,
                             cudaStream_t s);

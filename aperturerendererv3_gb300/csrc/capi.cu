@@ -330,6 +330,7 @@ void free_mlp(Ctx& c)
     free_dev(c.d_mlp_w32);
     free_dev(c.d_mlp_wbf);
     free_dev(c.d_mlp_grad);
+    free_dev(c.d_mlp_gpart);
     free_dev(c.d_mlp_m);
     free_dev(c.d_mlp_v);
     free_dev(c.d_mlp_loss);
@@ -387,6 +388,9 @@ ar_status ensure_mlp(ar_ctx* ctx)
         AR_CUDA(ctx, alloc_dev(c.d_mlp_w32, (size_t)AR_MLP_PARAMS));
         AR_CUDA(ctx, alloc_dev(c.d_mlp_wbf, (size_t)AR_MLP_PARAMS));
         AR_CUDA(ctx, alloc_dev(c.d_mlp_grad, (size_t)AR_MLP_PARAMS));
+        int sms = 0;
+        AR_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+        AR_CUDA(ctx, alloc_dev(c.d_mlp_gpart, (size_t)std::max(1, sms) * AR_MLP_PARAMS));
         AR_CUDA(ctx, alloc_dev(c.d_mlp_m, (size_t)AR_MLP_PARAMS));
         AR_CUDA(ctx, alloc_dev(c.d_mlp_v, (size_t)AR_MLP_PARAMS));
         AR_CUDA(ctx, alloc_dev(c.d_mlp_loss, 1));
@@ -486,12 +490,13 @@ cudaError_t mlp_train_frame(Ctx& c, int frames, long long* launches)
         e = cudaMemsetAsync(c.d_mlp_loss, 0, sizeof(float), c.stream);
         if (e == cudaSuccess)
             e = launch_mlp_train(net, c.gs.pos, c.gs.wr, c.gs.dir, c.gs.radiance, c.gs.count, 0,
-                                 AR_MLP_TRAIN_RECORDS, 1013 * k, c.d_mlp_grad, c.d_mlp_loss, c.d_err, sms, c.stream);
+                                 AR_MLP_TRAIN_RECORDS, 1013 * k, c.d_mlp_grad, c.d_mlp_gpart, c.d_mlp_loss, c.d_err,
+                                 sms, c.stream);
         if (e == cudaSuccess)
             e = launch_mlp_adam(c.d_mlp_w32, c.d_mlp_wbf, c.d_mlp_grad, c.d_mlp_m, c.d_mlp_v, c.mlp_step + 1,
                                 AR_MLP_LR, c.stream);
         if (e == cudaSuccess) ++c.mlp_step;
-        if (launches) *launches += 2;
+        if (launches) *launches += 3;
     }
     return e;
 }

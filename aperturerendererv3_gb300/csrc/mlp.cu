@@ -255,7 +255,10 @@ __global__ void __launch_bounds__(128 * mlpk::INF_WG, 1)
 // added to the float32 gradient block at the end.  Loss per record: the
 // radiance-weighted cross-entropy of the record direction's cell under the
 // softmax p of the 64 outputs, Y (logsumexp(y) - y_cell), averaged over the
-// records used.  Its minimiser is p(cell | position, view) proportional to
+// records used.  Each CTA stores its whole gradient (weights and biases, zeros
+// included) into its own slice of `part` (gridDim.x x AR_MLP_PARAMS floats);
+// k_mlp_grad_sum adds the slices in CTA order.  Its minimiser is
+// p(cell | position, view) proportional to
 // E[Y 1(direction in cell)], the radiance the records carried into each cell:
 // what a voxel probe's leaf accumulates (radiance x Jacobian per texel over
 // the records of its voxel and face, core/guiding/guiding.cuh:373-418), so the
@@ -264,7 +267,7 @@ __global__ void __launch_bounds__(128 * mlpk::INF_WG, 1)
 __global__ void __launch_bounds__(128, 1)
     k_mlp_train(MlpDev net, const float4* __restrict__ r_pos, const float4* __restrict__ r_wr,
                 const float4* __restrict__ r_dir, const float4* __restrict__ r_rad, const int* __restrict__ count_ptr,
-                int n_direct, int n_train, int offset, float* __restrict__ grad, float* __restrict__ loss_sum,
+                int n_direct, int n_train, int offset, float* __restrict__ part, float* __restrict__ loss_sum,
                 unsigned* err)
 {
     using namespace mlpk;
@@ -448,13 +451,15 @@ __global__ void __launch_bounds__(128, 1)
         first = false;
         if (abort_flag) break;
     }
-    // ---- flush: weight gradients (TMEM lanes 0-63 = outputs), bias gradients, loss
+    // ---- flush: this CTA's weight gradients (TMEM lanes 0-63 = outputs) and
+    // bias gradients into its slice of `part`, the loss into loss_sum
     for (int o = 16; o > 0; o >>= 1) my_loss += __shfl_xor_sync(0xffffffffu, my_loss, o);
     if (lane == 0 && my_loss != 0.0f) atomicAdd(&sloss, my_loss);
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
-    if (!first && warp < 2)
+    float* slice = part + (size_t)blockIdx.x * AR_MLP_PARAMS;
+    if (warp < 2)
     {
         const int o = warp * 32 + lane;
         for (int l = 0; l < AR_MLP_LAYERS; ++l)
@@ -463,19 +468,29 @@ __global__ void __launch_bounds__(128, 1)
             for (int j = 0; j < in / 16; ++j)
             {
                 float g[16];
-                umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(dw_col(l) + 16 * j), g);
-                float* dst = grad + mlp_w_offset(l) + o * in + 16 * j;
-                for (int i = 0; i < 16; ++i)
-                    if (g[i] != 0.0f) atomicAdd(dst + i, g[i]);
+                if (!first) umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(dw_col(l) + 16 * j), g);
+                else
+                    for (int i = 0; i < 16; ++i) g[i] = 0.0f;  // no tile: the accumulators were never written
+                float4* dst = reinterpret_cast<float4*>(slice + mlp_w_offset(l) + o * in + 16 * j);
+                for (int i = 0; i < 4; ++i) dst[i] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
             }
         }
     }
-    for (int k = threadIdx.x; k < 5 * 64; k += blockDim.x)
-        if (sdb[k] != 0.0f) atomicAdd(grad + mlp_b_offset(k / 64) + (k % 64), sdb[k]);
+    for (int k = threadIdx.x; k < 5 * 64; k += blockDim.x) slice[mlp_b_offset(k / 64) + (k % 64)] = sdb[k];
     if (threadIdx.x == 0 && loss_sum && sloss != 0.0f) atomicAdd(loss_sum, sloss);
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_free(tmem, TR_TMEM_COLS);
+}
+
+// grad += the sum of the training CTAs' gradient slices, in CTA order
+__global__ void k_mlp_grad_sum(const float* __restrict__ part, int slices, float* __restrict__ grad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= AR_MLP_PARAMS) return;
+    float acc = 0.0f;
+    for (int b = 0; b < slices; ++b) acc += part[(size_t)b * AR_MLP_PARAMS + i];
+    grad[i] += acc;
 }
 
 // Adam on the float32 master parameters; refreshes the bf16 copy and clears
@@ -523,12 +538,13 @@ cudaError_t launch_mlp_infer(const MlpDev& net, const float4* q_pos, const float
 
 cudaError_t launch_mlp_train(const MlpDev& net, const float4* r_pos, const float4* r_wr, const float4* r_dir,
                              const float4* r_rad, const int* count, int n_direct, int n_train, int offset, float* grad,
-                             float* loss_sum, unsigned* err, int sms, cudaStream_t s)
+                             float* part, float* loss_sum, unsigned* err, int sms, cudaStream_t s)
 {
     const int tiles = (n_train + 127) / 128;
     const int grid = std::max(1, std::min(sms, tiles));
     k_mlp_train<<<grid, 128, mlpk::TR_SMEM, s>>>(net, r_pos, r_wr, r_dir, r_rad, count, n_direct, n_train, offset,
-                                                  grad, loss_sum, err);
+                                                  part, loss_sum, err);
+    k_mlp_grad_sum<<<(AR_MLP_PARAMS + 255) / 256, 256, 0, s>>>(part, grid, grad);
     return cudaGetLastError();
 }
 
@@ -731,13 +747,16 @@ extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* i
         dir[i] = make_float4(dirs[3 * (size_t)i], dirs[3 * (size_t)i + 1], dirs[3 * (size_t)i + 2], 0.0f);
         rad[i] = make_float4(0.0f, lum[i], 0.0f, 0.0f);
     }
-    float *w32 = nullptr, *dgrad = nullptr, *dlog = nullptr, *dloss = nullptr;
+    float *w32 = nullptr, *dgrad = nullptr, *dpart = nullptr, *dlog = nullptr, *dloss = nullptr;
     uint16_t* wbf = nullptr;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     float4* dbuf = nullptr;
     unsigned* derr = nullptr;
     cudaError_t e = cudaMalloc(&w32, AR_MLP_PARAMS * 4);
     if (e == cudaSuccess) e = cudaMalloc(&wbf, AR_MLP_PARAMS * 2);
     if (e == cudaSuccess) e = cudaMalloc(&dgrad, AR_MLP_PARAMS * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dpart, (size_t)std::max(1, sms) * AR_MLP_PARAMS * 4);
     if (e == cudaSuccess) e = cudaMalloc(&dlog, (size_t)n * 64 * 4);
     if (e == cudaSuccess) e = cudaMalloc(&dloss, 4);
     if (e == cudaSuccess) e = cudaMalloc(&dbuf, (size_t)n * 4 * sizeof(float4));
@@ -754,8 +773,6 @@ extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* i
     if (e == cudaSuccess) e = cudaMemcpy(dw, wr.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dd, dir.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dr, rad.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     MlpDev net;
     net.wbf = wbf;
     net.w32 = w32;
@@ -767,7 +784,7 @@ extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* i
     if (e == cudaSuccess) e = mlp_prepare_kernels();
     if (e == cudaSuccess) e = launch_mlp_to_bf16(w32, wbf, 0);
     if (e == cudaSuccess) e = launch_mlp_infer(net, dp, dw, nullptr, nullptr, n, nullptr, dlog, derr, sms, 0);
-    if (e == cudaSuccess) e = launch_mlp_train(net, dp, dw, dd, dr, nullptr, n, n, 0, dgrad, dloss, derr, sms, 0);
+    if (e == cudaSuccess) e = launch_mlp_train(net, dp, dw, dd, dr, nullptr, n, n, 0, dgrad, dpart, dloss, derr, sms, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     unsigned herr = 0;
     if (e == cudaSuccess) e = cudaMemcpy(logits, dlog, (size_t)n * 64 * 4, cudaMemcpyDeviceToHost);
@@ -777,6 +794,7 @@ extern "C" ar_status ar_diag_mlp(int device, const float* params, const float* i
     cudaFree(w32);
     cudaFree(wbf);
     cudaFree(dgrad);
+    cudaFree(dpart);
     cudaFree(dlog);
     cudaFree(dloss);
     cudaFree(dbuf);
