@@ -17,6 +17,7 @@
 namespace ar
 {
 #define AR_WAVE_PATHS_AUTO (1 << 25)      // ar_render's automatic wave size
+#define AR_BOUNCE_LOOKAHEAD 4             // depths the host queues ahead of the queue lengths it has read
 #define AR_WAVE_PATHS_ADJOINT (1 << 21)   // ar_adjoint's
 
 // Order of a frame's pixels among the paths of a wave: bands of 4 rows, each
@@ -41,6 +42,69 @@ AR_HD uint32_t slot_pixel(uint32_t u, uint32_t W, uint32_t H)
     const uint32_t r = rem / wc;
     const uint32_t x = rem - r * wc;
     return (AR_TILE_H * b + r) * W + AR_TILE_W * c + x;
+}
+
+// Order of a render's paths.  Path g of an spp-sample render over npix pixel
+// slots (slot_pixel order) is sample s of slot u.  Samples come in blocks of
+// `block` consecutive samples; inside a block, groups of AR_PATH_GROUP_PX
+// consecutive slots take all of the block's samples of those slots (slot
+// fastest).  With blocks of AR_SAMPLE_BLOCK samples a warp's 32 paths are 8
+// samples of 4 neighbouring pixels, whose camera rays nearly coincide and
+// whose first hits lie close together; block 1 is frame-major order.  A
+// path's (pixel, sample) picks its random stream and its place in the
+// per-pixel sums (added in sample order), so the order changes no result.
+#define AR_PATH_GROUP_PX 4u
+#define AR_SAMPLE_BLOCK 8
+struct PathOrder
+{
+    uint32_t npix, spp, block;
+};
+
+AR_HD uint32_t path_block_samples(const PathOrder& o, uint32_t fb)
+{
+    const uint32_t left = o.spp - fb * o.block;
+    return o.block < left ? o.block : left;
+}
+
+// (slot, sample) of path g, 0 <= g < npix * spp
+AR_HD void path_slot(const PathOrder& o, unsigned long long g, uint32_t* u, uint32_t* s)
+{
+    const unsigned long long per_block = (unsigned long long)o.npix * o.block;
+    const uint32_t fb = (uint32_t)(g / per_block);
+    const unsigned long long r = g - (unsigned long long)fb * per_block;
+    const uint32_t sb = path_block_samples(o, fb);
+    const unsigned long long group = (unsigned long long)AR_PATH_GROUP_PX * sb;
+    const uint32_t ub = (uint32_t)(r / group);
+    const uint32_t w = (uint32_t)(r - (unsigned long long)ub * group);
+    const uint32_t left = o.npix - ub * AR_PATH_GROUP_PX;
+    const uint32_t q = left < AR_PATH_GROUP_PX ? left : AR_PATH_GROUP_PX;  // the last group may be short
+    *u = ub * AR_PATH_GROUP_PX + w % q;
+    *s = fb * o.block + w / q;
+}
+
+// path index of (slot u, sample s): the inverse of path_slot, rising with s
+AR_HD unsigned long long path_index(const PathOrder& o, uint32_t u, uint32_t s)
+{
+    const uint32_t fb = s / o.block;
+    const uint32_t sb = path_block_samples(o, fb);
+    const uint32_t ub = u / AR_PATH_GROUP_PX;
+    const uint32_t left = o.npix - ub * AR_PATH_GROUP_PX;
+    const uint32_t q = left < AR_PATH_GROUP_PX ? left : AR_PATH_GROUP_PX;
+    return (unsigned long long)fb * o.npix * o.block + (unsigned long long)ub * AR_PATH_GROUP_PX * sb +
+           (unsigned long long)(s - fb * o.block) * q + (u - ub * AR_PATH_GROUP_PX);
+}
+
+// first sample of slot u whose path index is at least g0 (spp if none)
+AR_HD uint32_t path_first_sample(const PathOrder& o, uint32_t u, unsigned long long g0)
+{
+    uint32_t lo = 0, hi = o.spp;
+    while (lo < hi)
+    {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (path_index(o, u, mid) < g0) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
 }
 
 // Voxel guide as the kernels see it: a sparse open-addressing hash from the
@@ -224,13 +288,23 @@ struct RenderLaunch
     int mlp_ready;  // guide 2: sample from the network instead of the voxel probes
     double* grad_medium;  // replay pass of ar_adjoint_medium: d loss / d (albedo, emission)
     int denoise;  // record the denoiser's G-buffer and sample moments
+    int sample_block = 1;  // path order: samples per block (PathOrder)
 };
+
+inline PathOrder path_order(const RenderLaunch& rl)
+{
+    return PathOrder{(uint32_t)((long long)rl.width * rl.height), (uint32_t)rl.spp, (uint32_t)rl.sample_block};
+}
 
 struct Ctx
 {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t order_event = nullptr;  // orders a caller's stream after the context's (ar_render_noalloc)
+    // per depth of a wave: the next queue's length, copied to pinned host memory,
+    // and the event after the copy (a ring of AR_BOUNCE_LOOKAHEAD + 1)
+    cudaEvent_t bounce_ev[AR_BOUNCE_LOOKAHEAD + 1] = {};
+    int* h_bounce_cnt = nullptr;
     float exposure = 1.0f;               // display exposure of ar_render_frame (ar_set_exposure)
     double* d_frame_xyz = nullptr;       // ar_render_frame: the frame's sample per pixel
     double* d_frame_dn = nullptr;        // ar_render_frame: denoiser input and output

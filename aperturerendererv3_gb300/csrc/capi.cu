@@ -630,6 +630,10 @@ ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch&
     rl.use_nee = prm->use_nee;
     rl.seed = prm->seed;
     rl.first_frame = prm->first_frame;
+    // samples per block of the path order (PathOrder): a warp holds 8 samples of
+    // 4 neighbouring pixels; ar_render sets 1 for guided renders, whose update
+    // windows are runs of whole frames
+    rl.sample_block = std::min(AR_SAMPLE_BLOCK, std::max(1, rl.spp));
     rl.profile = prm->profile;
     c.profile = prm->profile & 3;
     c.stage_events.clear();
@@ -667,6 +671,9 @@ ar_status ar_create(ar_ctx** out, int device)
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.order_event, cudaEventDisableTiming);
+    for (int k = 0; k <= AR_BOUNCE_LOOKAHEAD && e == cudaSuccess; ++k)
+        e = cudaEventCreateWithFlags(&c.bounce_ev[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&c.h_bounce_cnt, (AR_BOUNCE_LOOKAHEAD + 1) * sizeof(int), cudaHostAllocDefault);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_err, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(c.d_err, 0, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_counters, AR_CNT_COUNT * sizeof(int));
@@ -718,6 +725,9 @@ ar_status ar_destroy(ar_ctx* ctx)
     free_dev(c.d_frame_xyz);
     free_dev(c.d_frame_dn);
     if (c.order_event) cudaEventDestroy(c.order_event);
+    for (cudaEvent_t& ev : c.bounce_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (c.h_bounce_cnt) cudaFreeHost(c.h_bounce_cnt);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete ctx;
     return AR_OK;
@@ -1264,6 +1274,7 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     const long long total = npix * rl.spp;
     rl.guide = prm->guide;
     if (rl.guide < 0 || rl.guide > 2) return fail(ctx, AR_ERR_INVALID, "render: unknown guide mode");
+    if (rl.guide) rl.sample_block = 1;
     // automatic: up to 2^25 paths in flight (about 8 GB of path and shadow-ray
     // state); each depth of a wave is three launches whose ramp-up and tail
     // cost the same whatever the wave's size, so few large waves keep the GPU
@@ -1344,17 +1355,16 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     if (d_samples) cudaFree(d_samples);
     if (e == cudaSuccess && per_sample_xyz)
     {
-        // samples arrive in path-slot order; hand them back frame-major, pixel-minor
-        std::vector<float> frame((size_t)npix * 3);
-        for (long long f = 0; f < rl.spp; ++f)
+        // samples arrive in path order; hand them back sample-major, pixel-minor
+        const std::vector<float> by_path(per_sample_xyz, per_sample_xyz + 3 * (size_t)total);
+        const PathOrder po = path_order(rl);
+        for (long long g = 0; g < total; ++g)
         {
-            float* base = per_sample_xyz + 3 * f * npix;
-            std::memcpy(frame.data(), base, frame.size() * sizeof(float));
-            for (long long u = 0; u < npix; ++u)
-            {
-                const size_t px = slot_pixel((uint32_t)u, (uint32_t)rl.width, (uint32_t)rl.height);
-                for (int k = 0; k < 3; ++k) base[3 * px + k] = frame[3 * u + k];
-            }
+            uint32_t u, s;
+            path_slot(po, (unsigned long long)g, &u, &s);
+            const size_t px = slot_pixel(u, (uint32_t)rl.width, (uint32_t)rl.height);
+            float* dst = per_sample_xyz + 3 * ((size_t)s * npix + px);
+            for (int k = 0; k < 3; ++k) dst[k] = by_path[3 * (size_t)g + k];
         }
     }
     c.last_launches = launches;

@@ -51,19 +51,19 @@ constexpr size_t SMEM_BYTES = ((size_t)P_COUNT * SPAN + AR_DN_TQ_SIZE + TAPS) * 
 
 __global__ void k_denoise_record(const float4* __restrict__ rec, const float* __restrict__ out_xyz,
                                  const Material* __restrict__ mats, long long first_path, int n, int width, int height,
-                                 DnGBuf* __restrict__ gb, DnStat* __restrict__ st)
+                                 PathOrder po, DnGBuf* __restrict__ gb, DnStat* __restrict__ st)
 {
-    // one thread per pixel slot of a frame (slot_pixel maps it to its pixel)
+    // one thread per pixel slot (slot_pixel maps it to its pixel): this wave's
+    // samples of the slot, in sample order
     const long long npix = (long long)width * height;
     const long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (u >= npix) return;
-    long long g = first_path - (first_path % npix) + u;
-    if (g < first_path) g += npix;
-    if (g >= first_path + n) return;
+    uint32_t smp = path_first_sample(po, (uint32_t)u, (unsigned long long)first_path);
+    if (smp >= po.spp || (long long)path_index(po, (uint32_t)u, smp) >= first_path + n) return;
     const long long p = slot_pixel((uint32_t)u, (uint32_t)width, (uint32_t)height);
     DnGBuf b = gb[p];
     DnStat s = st[p];
-    for (; g < first_path + n; g += npix)
+    for (long long g; smp < po.spp && (g = (long long)path_index(po, (uint32_t)u, smp)) < first_path + n; ++smp)
     {
         const long long k = g - first_path;
         const float4 r0 = rec[2 * k], r1 = rec[2 * k + 1];
@@ -249,7 +249,7 @@ cudaError_t launch_denoise_record(Ctx& c, const RenderLaunch& rl, long long firs
     const long long npix = (long long)rl.width * rl.height;
     const int grid = (int)((npix + 255) / 256);
     k_denoise_record<<<grid, 256, 0, c.stream>>>(c.d_dn_rec, c.ps.out_xyz, c.d_materials, first_path, n, rl.width,
-                                                 rl.height, c.d_dn_gb, c.d_dn_st);
+                                                 rl.height, path_order(rl), c.d_dn_gb, c.d_dn_st);
     if (launches) *launches += 1;
     return cudaGetLastError();
 }

@@ -172,6 +172,7 @@ extern "C" ar_status ar_render_noalloc(ar_ctx* ctx, const ar_render_params* prm,
     rl.seed = prm->seed;
     rl.first_frame = prm->first_frame;
     rl.profile = 0;
+    rl.sample_block = std::min(AR_SAMPLE_BLOCK, std::max(1, rl.spp));  // the path order of ar_render
     // the same test as ar_render's (SDF objects evaluate their field; no allocation)
     const int camera_inside = camera_inside_any(c, rl.cam_o);
     DevScene sc = dev_scene(c);

@@ -206,7 +206,7 @@ struct CamParams
 __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, int* counter, long long first_path, int n,
                                                    int width, int height, uint64_t seed, int first_frame, CamParams cam,
                                                    int camera_inside, int* fetch_reset, bool media_record,
-                                                   bool frame_record)
+                                                   bool frame_record, PathOrder po)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0)
@@ -214,34 +214,33 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
         *counter = n;
         *fetch_reset = 0;  // the first k_extend's fetch counter
     }
-    const long long npix = (long long)width * height;
-    // stream jumps of the first and last frame this block covers, computed once
-    __shared__ uint64_t s_jump[2][2];
+    // stream jumps of the samples this block's paths can belong to (its first
+    // path's block of samples and the next: 2 x po.block frames), computed once
+    __shared__ uint64_t s_jump[2 * AR_SAMPLE_BLOCK][2];
     const long long g_first = first_path + (long long)blockIdx.x * blockDim.x;
-    const long long g_last = first_path + min((long long)(blockIdx.x + 1) * blockDim.x, (long long)n) - 1;
-    const uint32_t f_first = (uint32_t)(g_first / npix) + (uint32_t)first_frame;
-    const uint32_t f_last = (uint32_t)(g_last / npix) + (uint32_t)first_frame;
-    if (threadIdx.x < 2)
+    const uint32_t s_base = (uint32_t)(g_first / ((long long)po.npix * po.block)) * po.block;
+    const uint32_t n_jump = 2 * po.block;
+    if (threadIdx.x < n_jump)
     {
         uint64_t m, c;
-        ar_pcg_jump((uint64_t)(threadIdx.x ? f_last : f_first) << 32, &m, &c);
+        ar_pcg_jump((uint64_t)(s_base + threadIdx.x + (uint32_t)first_frame) << 32, &m, &c);
         s_jump[threadIdx.x][0] = m;
         s_jump[threadIdx.x][1] = c;
     }
     __syncthreads();
     if (k >= n) return;
     const long long g = first_path + k;
-    const uint32_t pixel = slot_pixel((uint32_t)(g % npix), (uint32_t)width, (uint32_t)height);
-    const uint32_t frame = (uint32_t)(g / npix) + (uint32_t)first_frame;
+    uint32_t slot, smp;
+    path_slot(po, (unsigned long long)g, &slot, &smp);
+    const uint32_t pixel = slot_pixel(slot, (uint32_t)width, (uint32_t)height);
+    const uint32_t frame = smp + (uint32_t)first_frame;
     const int i = (int)(pixel % (uint32_t)width), j = (int)(pixel / (uint32_t)width);
     DevRand R;
-    if (frame == f_first || frame == f_last)
-    {
-        const int w = frame == f_first ? 0 : 1;
-        R.g = ar_pcg_init_jumped(seed, pixel, frame, s_jump[w][0], s_jump[w][1]);
-    }
+    const uint32_t jf = smp - s_base;
+    if (smp >= s_base && jf < n_jump)
+        R.g = ar_pcg_init_jumped(seed, pixel, frame, s_jump[jf][0], s_jump[jf][1]);
     else
-        R.g = ar_pcg_init(seed, pixel, frame);  // blocks spanning more than two frames (images under 256 pixels)
+        R.g = ar_pcg_init(seed, pixel, frame);  // blocks spanning more samples (images under 256 pixels)
     const float u = (i + R()) / static_cast<float>(width);
     const float v = (j + R()) / static_cast<float>(height);
     const float nx = u * 2.f - 1.f;
@@ -1422,18 +1421,18 @@ __global__ void k_guide_emit(DevScene sc, PathState ps, int n, GuideSamples gs)
 // one thread per pixel slot u of a frame (slot_pixel(u) is its pixel): the
 // wave's samples of that pixel are added in frame order
 __global__ void k_accumulate(const float* __restrict__ out_xyz, long long first_path, int n, int width, int height,
-                             double* __restrict__ accum)
+                             PathOrder po, double* __restrict__ accum)
 {
     const long long npix = (long long)width * height;
     const long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (u >= npix) return;
-    long long g = first_path - (first_path % npix) + u;
-    if (g < first_path) g += npix;
-    if (g >= first_path + n) return;
+    // this wave's samples of slot u, in sample order
+    uint32_t smp = path_first_sample(po, (uint32_t)u, (unsigned long long)first_path);
+    if (smp >= po.spp || (long long)path_index(po, (uint32_t)u, smp) >= first_path + n) return;
     const long long p = slot_pixel((uint32_t)u, (uint32_t)width, (uint32_t)height);
     double sx = accum[3 * p], sy = accum[3 * p + 1], sz = accum[3 * p + 2];
     bool any = false;
-    for (; g < first_path + n; g += npix)
+    for (long long g; smp < po.spp && (g = (long long)path_index(po, (uint32_t)u, smp)) < first_path + n; ++smp)
     {
         const long long k = g - first_path;
         sx += (double)out_xyz[3 * k];
@@ -1502,7 +1501,6 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     // resident: they fetch rays from a counter, so extra blocks would only add
     // launch cost (most deep bounces have few or no paths left)
     const int grid_t = sms * AR_TRAV_MIN_BLOCKS;
-    const int grid_s = std::max(2 * sms, (n + AR_BLOCK * AR_SHADE_PATHS_PER_THREAD - 1) / (AR_BLOCK * AR_SHADE_PATHS_PER_THREAD));
     int* cnt = c.d_counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
     // opaque surfaces only: the shading instantiation without glass, medium and texture code
@@ -1512,7 +1510,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         StageScope st(c, ST_RAYGEN);
         k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, c.d_queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height,
                                              rl.seed, rl.first_frame, cam, c.camera_inside, &cnt[AR_CNT_FETCH], !lean,
-                                             rl.guide != 0);
+                                             rl.guide != 0, path_order(rl));
         if (rl.guide) k_guide_init<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, n);
     }
     long long L = rl.guide ? 2 : 1;
@@ -1531,8 +1529,29 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     // SDF geometry: its work leaves the traversal kernels for k_sdf_extend / k_sdf_shadow
     const bool has_sdf = c.sdf_object_count > 0 || c.sdf.count > 0;
     const SdfPending pend_shd{has_sdf ? c.d_pend_list : nullptr, &cnt[AR_CNT_PEND]};
+    // Each depth's next-queue length is copied to pinned host memory behind
+    // the depth's launches.  The host stays AR_BOUNCE_LOOKAHEAD depths ahead of
+    // the GPU: before it queues depth b it reads the length left by depth
+    // b - AR_BOUNCE_LOOKAHEAD, which bounds every later queue.  A zero ends the
+    // wave's depth loop (every later depth would find an empty queue), and the
+    // bound sizes the grids of the queue-sized kernels, so deep bounces with
+    // few paths left (or none, at depth limits like 1000) cost launches of a
+    // few blocks instead of a wave-sized grid.
+    constexpr int K = AR_BOUNCE_LOOKAHEAD;
+    long long bound = n;  // upper bound of the current depth's queue length
     for (int b = 0; b < rl.max_depth; ++b)
     {
+        if (b >= K)
+        {
+            const int slot = (b - K) % (K + 1);
+            const cudaError_t we = cudaEventSynchronize(c.bounce_ev[slot]);
+            if (we != cudaSuccess) return we;
+            const int known = c.h_bounce_cnt[slot];  // queue length of depth b - K + 1
+            if (known <= 0) break;
+            bound = std::min<long long>(bound, known);
+        }
+        const int grid_s = std::max(2 * sms, (int)((bound + AR_BLOCK * AR_SHADE_PATHS_PER_THREAD - 1) /
+                                                   (AR_BLOCK * AR_SHADE_PATHS_PER_THREAD)));
         const int cur = b & 1, nxt = cur ^ 1;
         int* qn = &cnt[AR_CNT_Q0 + cur];
         // k_extend zeroes the next queue, shadow queue, shadow fetch and pending
@@ -1590,6 +1609,11 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
             }
         }
         L += 3;
+        {
+            const int slot = b % (K + 1);
+            cudaMemcpyAsync(&c.h_bounce_cnt[slot], &cnt[AR_CNT_Q0 + nxt], sizeof(int), cudaMemcpyDeviceToHost, s);
+            cudaEventRecord(c.bounce_ev[slot], s);
+        }
     }
     if (rl.adjoint)
     {
@@ -1624,7 +1648,8 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     int* cnt = wb.counters;  // AR_CNT_* layout
     const CamParams cam = make_camera(rl);
     k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(wb.ps, wb.queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height, rl.seed,
-                                         rl.first_frame, cam, camera_inside, &cnt[AR_CNT_FETCH], true, false);
+                                         rl.first_frame, cam, camera_inside, &cnt[AR_CNT_FETCH], true, false,
+                                         path_order(rl));
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
@@ -1655,7 +1680,7 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     k_finalize<<<grid_n, AR_BLOCK, 0, s>>>(sc, wb.ps, n, nullptr);
     const long long npix = (long long)rl.width * rl.height;
     k_accumulate<<<(int)((npix + AR_BLOCK - 1) / AR_BLOCK), AR_BLOCK, 0, s>>>(wb.ps.out_xyz, first_path, n, rl.width,
-                                                                             rl.height, wb.accum);
+                                                                             rl.height, path_order(rl), wb.accum);
     return cudaGetLastError();
 }
 
@@ -1677,7 +1702,8 @@ cudaError_t launch_accumulate(Ctx& c, const RenderLaunch& rl, long long first_pa
 {
     const long long npix = (long long)rl.width * rl.height;
     const int grid = (int)((npix + AR_BLOCK - 1) / AR_BLOCK);
-    k_accumulate<<<grid, AR_BLOCK, 0, c.stream>>>(c.ps.out_xyz, first_path, n, rl.width, rl.height, accum);
+    k_accumulate<<<grid, AR_BLOCK, 0, c.stream>>>(c.ps.out_xyz, first_path, n, rl.width, rl.height, path_order(rl),
+                                                  accum);
     if (launches) *launches += 1;
     return cudaGetLastError();
 }

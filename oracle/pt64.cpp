@@ -1949,6 +1949,25 @@ int pt64_adjoint_medium(const pt64_scene* s, const int32_t* ip, const double* dp
     return 0;
 }
 
+// the medium adjoint over a window (x0, y0, w, h) of the image: the window's
+// pixels with the full image's rays and streams; dl_dxyz covers the full image
+int pt64_adjoint_medium_crop(const pt64_scene* s, const int32_t* ip, const double* dp, uint64_t seed,
+                             const int32_t* window, const double* dl_dxyz, double* grad2)
+{
+    if (!s || !ip || !dp || !window || !dl_dxyz || !grad2) return -1;
+    Params P = to_params(ip, dp, seed);
+    if (P.width <= 0 || P.height <= 0 || P.spp <= 0 || P.max_depth <= 0) return -1;
+    P.crop_x0 = window[0];
+    P.crop_y0 = window[1];
+    P.crop_w = window[2];
+    P.crop_h = window[3];
+    if (P.crop_x0 < 0 || P.crop_y0 < 0 || P.crop_w <= 0 || P.crop_h <= 0 || P.crop_x0 + P.crop_w > P.width ||
+        P.crop_y0 + P.crop_h > P.height)
+        return -1;
+    run(*reinterpret_cast<const Scene*>(s), P, nullptr, nullptr, dl_dxyz, nullptr, grad2);
+    return 0;
+}
+
 int pt64_adjoint(const pt64_scene* s, const int32_t* ip, const double* dp, uint64_t seed, const double* dl_dxyz, double* grad)
 {
     if (!s || !ip || !dp || !dl_dxyz || !grad) return -1;

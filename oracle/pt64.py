@@ -50,6 +50,8 @@ def load() -> C.CDLL:
         lib.pt64_render.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
         lib.pt64_render_crop.restype = i32
         lib.pt64_render_crop.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
+        lib.pt64_adjoint_medium_crop.restype = i32
+        lib.pt64_adjoint_medium_crop.argtypes = [vp, vp, vp, C.c_uint64, vp, vp, vp]
         lib.pt64_adjoint.restype = i32
         lib.pt64_adjoint.argtypes = [vp, vp, vp, C.c_uint64, vp, vp]
         _lib = lib
@@ -180,13 +182,22 @@ class Scene64:
         return mean
 
     def adjoint_medium(self, dl_dxyz, size, origin, direction, spp, *, fov=60.0, max_depth=1000, use_nee=True,
-                       seed=0x9E3779B97F4A7C15, first_frame=0, threads=0):
-        """(d loss / d medium albedo, d loss / d medium emission) given d(loss)/d(mean image)."""
+                       seed=0x9E3779B97F4A7C15, first_frame=0, threads=0, window=None):
+        """(d loss / d medium albedo, d loss / d medium emission) given d(loss)/d(mean image)
+        (h, w, 3).  window (x0, y0, w, h): only that window's pixels (the full
+        image's rays and streams), i.e. the gradient of a loss that reads the
+        window alone."""
         ip, dp = self._params(size, origin, direction, spp, fov, max_depth, use_nee, first_frame,
                               threads or os.cpu_count() or 1)
         dl = np.ascontiguousarray(dl_dxyz, np.float64)
         g = np.zeros(2, np.float64)
-        rc = load().pt64_adjoint_medium(self._h, ip.ctypes.data, dp.ctypes.data, seed, dl.ctypes.data, g.ctypes.data)
+        if window is not None:
+            win = np.array(window, np.int32)
+            rc = load().pt64_adjoint_medium_crop(self._h, ip.ctypes.data, dp.ctypes.data, seed, win.ctypes.data,
+                                                 dl.ctypes.data, g.ctypes.data)
+        else:
+            rc = load().pt64_adjoint_medium(self._h, ip.ctypes.data, dp.ctypes.data, seed, dl.ctypes.data,
+                                            g.ctypes.data)
         if rc != 0:
             raise ValueError("FP64 oracle: bad adjoint parameters")
         return float(g[0]), float(g[1])
