@@ -631,8 +631,8 @@ ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch&
     rl.seed = prm->seed;
     rl.first_frame = prm->first_frame;
     // samples per block of the path order (PathOrder): a warp holds 8 samples of
-    // 4 neighbouring pixels; ar_render sets 1 for guided renders, whose update
-    // windows are runs of whole frames
+    // 4 neighbouring pixels; guided renders use a block that divides their
+    // update window, so that a window stays one run of paths
     rl.sample_block = std::min(AR_SAMPLE_BLOCK, std::max(1, rl.spp));
     rl.profile = prm->profile;
     c.profile = prm->profile & 3;
@@ -1274,7 +1274,13 @@ ar_status ar_render(ar_ctx* ctx, const ar_render_params* prm, double* out_xyz, i
     const long long total = npix * rl.spp;
     rl.guide = prm->guide;
     if (rl.guide < 0 || rl.guide > 2) return fail(ctx, AR_ERR_INVALID, "render: unknown guide mode");
-    if (rl.guide) rl.sample_block = 1;
+    if (rl.guide)
+    {
+        // an update window of guide_frames frames stays one run of paths when
+        // the sample block divides it
+        const int gf = std::max(1, prm->guide_frames);
+        while (gf % rl.sample_block != 0) rl.sample_block >>= 1;
+    }
     // automatic: up to 2^25 paths in flight (about 8 GB of path and shadow-ray
     // state); each depth of a wave is three launches whose ramp-up and tail
     // cost the same whatever the wave's size, so few large waves keep the GPU
