@@ -630,10 +630,30 @@ ar_status prepare_launch(ar_ctx* ctx, const ar_render_params* prm, RenderLaunch&
     rl.use_nee = prm->use_nee;
     rl.seed = prm->seed;
     rl.first_frame = prm->first_frame;
-    // samples per block of the path order (PathOrder): a warp holds 8 samples of
-    // 4 neighbouring pixels; guided renders use a block that divides their
-    // update window, so that a window stays one run of paths
+    // samples per block of the path order (PathOrder): a warp holds 32 samples
+    // of one pixel; guided renders use a block that divides their update
+    // window, so that a window stays one run of paths
     rl.sample_block = std::min(AR_SAMPLE_BLOCK, std::max(1, rl.spp));
+    // the stream jump of every sample of the render, once (k_raygen reads it)
+    if (c.jump_cap < rl.spp)
+    {
+        free_dev(c.d_jumps);
+        c.jump_cap = 0;
+        AR_CUDA(ctx, cudaMalloc((void**)&c.d_jumps, (size_t)rl.spp * sizeof(ulonglong2)));
+        c.jump_cap = rl.spp;
+    }
+    {
+        std::vector<ulonglong2> jumps((size_t)rl.spp);
+        for (int s = 0; s < rl.spp; ++s)
+        {
+            uint64_t m, a;
+            ar_pcg_jump((uint64_t)((uint32_t)s + (uint32_t)rl.first_frame) << 32, &m, &a);
+            jumps[(size_t)s] = make_ulonglong2(m, a);
+        }
+        AR_CUDA(ctx, cudaMemcpyAsync(c.d_jumps, jumps.data(), jumps.size() * sizeof(ulonglong2), cudaMemcpyHostToDevice,
+                                     c.stream));
+    }
+    rl.jumps = c.d_jumps;
     rl.profile = prm->profile;
     c.profile = prm->profile & 3;
     c.stage_events.clear();
@@ -724,6 +744,7 @@ ar_status ar_destroy(ar_ctx* ctx)
     free_dev(c.d_grad_medium);
     free_dev(c.d_frame_xyz);
     free_dev(c.d_frame_dn);
+    free_dev(c.d_jumps);
     if (c.order_event) cudaEventDestroy(c.order_event);
     for (cudaEvent_t& ev : c.bounce_ev)
         if (ev) cudaEventDestroy(ev);

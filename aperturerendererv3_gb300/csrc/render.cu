@@ -206,7 +206,8 @@ struct CamParams
 __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, int* counter, long long first_path, int n,
                                                    int width, int height, uint64_t seed, int first_frame, CamParams cam,
                                                    int camera_inside, int* fetch_reset, bool media_record,
-                                                   bool frame_record, PathOrder po)
+                                                   bool frame_record, PathOrder po,
+                                                   const ulonglong2* __restrict__ jumps)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0)
@@ -214,20 +215,24 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
         *counter = n;
         *fetch_reset = 0;  // the first k_extend's fetch counter
     }
-    // stream jumps of the samples this block's paths can belong to (its first
-    // path's block of samples and the next: 2 x po.block frames), computed once
+    // stream jumps per sample: the render's table, or (allocation-free renders)
+    // those of the samples this block's paths can belong to (its first path's
+    // block of samples and the next: 2 x po.block frames), computed once
     __shared__ uint64_t s_jump[2 * AR_SAMPLE_BLOCK][2];
     const long long g_first = first_path + (long long)blockIdx.x * blockDim.x;
     const uint32_t s_base = (uint32_t)(g_first / ((long long)po.npix * po.block)) * po.block;
     const uint32_t n_jump = 2 * po.block;
-    if (threadIdx.x < n_jump)
+    if (!jumps)
     {
-        uint64_t m, c;
-        ar_pcg_jump((uint64_t)(s_base + threadIdx.x + (uint32_t)first_frame) << 32, &m, &c);
-        s_jump[threadIdx.x][0] = m;
-        s_jump[threadIdx.x][1] = c;
+        if (threadIdx.x < n_jump)
+        {
+            uint64_t m, c;
+            ar_pcg_jump((uint64_t)(s_base + threadIdx.x + (uint32_t)first_frame) << 32, &m, &c);
+            s_jump[threadIdx.x][0] = m;
+            s_jump[threadIdx.x][1] = c;
+        }
+        __syncthreads();
     }
-    __syncthreads();
     if (k >= n) return;
     const long long g = first_path + k;
     uint32_t slot, smp;
@@ -237,7 +242,12 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
     const int i = (int)(pixel % (uint32_t)width), j = (int)(pixel / (uint32_t)width);
     DevRand R;
     const uint32_t jf = smp - s_base;
-    if (smp >= s_base && jf < n_jump)
+    if (jumps)
+    {
+        const ulonglong2 jm = jumps[smp];
+        R.g = ar_pcg_init_jumped(seed, pixel, frame, jm.x, jm.y);
+    }
+    else if (smp >= s_base && jf < n_jump)
         R.g = ar_pcg_init_jumped(seed, pixel, frame, s_jump[jf][0], s_jump[jf][1]);
     else
         R.g = ar_pcg_init(seed, pixel, frame);  // blocks spanning more samples (images under 256 pixels)
@@ -1510,7 +1520,7 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         StageScope st(c, ST_RAYGEN);
         k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, c.d_queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height,
                                              rl.seed, rl.first_frame, cam, c.camera_inside, &cnt[AR_CNT_FETCH], !lean,
-                                             rl.guide != 0, path_order(rl));
+                                             rl.guide != 0, path_order(rl), rl.jumps);
         if (rl.guide) k_guide_init<<<grid_n, AR_BLOCK, 0, s>>>(c.ps, n);
     }
     long long L = rl.guide ? 2 : 1;
@@ -1649,7 +1659,7 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     const CamParams cam = make_camera(rl);
     k_raygen<<<grid_n, AR_BLOCK, 0, s>>>(wb.ps, wb.queue[0], &cnt[AR_CNT_Q0], first_path, n, rl.width, rl.height, rl.seed,
                                          rl.first_frame, cam, camera_inside, &cnt[AR_CNT_FETCH], true, false,
-                                         path_order(rl));
+                                         path_order(rl), nullptr);
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;

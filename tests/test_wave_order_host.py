@@ -83,7 +83,7 @@ int main()
     long long cases = 0, bad_bij = 0, bad_inv = 0, bad_mono = 0, bad_frame_major = 0, bad_first = 0, bad_warp = 0;
     const unsigned npixs[] = {1, 2, 3, 4, 5, 7, 8, 13, 64, 100, 1001, 4096};
     const unsigned spps[] = {1, 2, 3, 7, 8, 9, 16, 17, 64};
-    const unsigned blocks[] = {1, 2, 8};
+    const unsigned blocks[] = {1, 2, 8, AR_SAMPLE_BLOCK};
     for (unsigned npix : npixs)
         for (unsigned spp : spps)
             for (unsigned block : blocks)
@@ -117,9 +117,10 @@ int main()
                         if (path_first_sample(o, u, g0) != want) ++bad_first;
                     }
                 }
-                // a full block of 8 samples: each aligned warp is 8 samples of 4 consecutive slots
-                if (block == 8 && npix % 4 == 0)
-                    for (unsigned long long w0 = 0; w0 + 32 <= (unsigned long long)npix * 8; w0 += 32)
+                // a full block of AR_SAMPLE_BLOCK samples: each aligned warp is all of the
+                // block's samples of AR_PATH_GROUP_PX consecutive slots, slot fastest
+                if (block == AR_SAMPLE_BLOCK && AR_PATH_GROUP_PX * AR_SAMPLE_BLOCK == 32 && npix % AR_PATH_GROUP_PX == 0)
+                    for (unsigned long long w0 = 0; w0 + 32 <= (unsigned long long)npix * block; w0 += 32)
                     {
                         uint32_t u0, s0;
                         path_slot(o, w0, &u0, &s0);
@@ -127,7 +128,7 @@ int main()
                         {
                             uint32_t u, s;
                             path_slot(o, w0 + i, &u, &s);
-                            if (u != u0 + i % 4 || s != s0 + i / 4) { ++bad_warp; break; }
+                            if (u != u0 + i % AR_PATH_GROUP_PX || s != s0 + i / AR_PATH_GROUP_PX) { ++bad_warp; break; }
                         }
                     }
             }
@@ -143,7 +144,8 @@ def test_path_order_is_a_bijection_with_its_inverse(tmp_path):
     render exactly once, path_index inverts path_slot and rises with the
     sample (the per-pixel sums add samples in order), path_first_sample finds
     a wave's first sample of a slot, block 1 is frame-major order, and with
-    blocks of 8 samples every warp holds 8 samples of 4 consecutive slots."""
+    full blocks every warp holds all of a block's samples of its slots (32
+    samples of one pixel)."""
     cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
     nvcc = cuda / "bin" / "nvcc"
     if not nvcc.exists():
