@@ -138,7 +138,8 @@ def limiter_summary(workload: str):
 
 
 def profile_traffic(workload: str):
-    """DRAM bytes per extend launch from the committed ncu summary (or None)."""
+    """k_extend DRAM bytes per camera ray and per bounce ray from the committed
+    small-case ncu summary (or None)."""
     p = ROOT / "profiles" / "traffic.json"
     if p.exists():
         d = json.loads(p.read_text())
@@ -692,7 +693,11 @@ def main() -> None:
     launches_ext = max(1, prof["extend_launches"])
     achieved = alg_bytes / (prof["extend_ms"] / 1e3) / 1e9
     peaks = measured_peaks()
-    traffic = profile_traffic(args.workload)
+    per_ray = profile_traffic(args.workload)
+    # DRAM bytes per k_extend launch: the capture's bytes per ray, scaled by the
+    # step's rays (an upper bound: a full-size launch shares the BVH among more rays)
+    traffic = (None if per_ray is None else
+               (cam_rays * per_ray["camera_bytes_per_ray"] + bounce_rays * per_ray["bounce_bytes_per_ray"]) / launches_ext)
     own_bytes = prof["extend_node_visits"] * 80 + prof["extend_prim_tests"] * 48 + prof["extend_rays"] * 64
     out = {
         "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
