@@ -72,6 +72,23 @@ AR_HD uint32_t path_block_samples(const PathOrder& o, uint32_t fb)
 AR_HD void path_slot(const PathOrder& o, unsigned long long g, uint32_t* u, uint32_t* s)
 {
     const unsigned long long per_block = (unsigned long long)o.npix * o.block;
+    if (((g | per_block) >> 32) == 0)
+    {
+        // the same arithmetic in 32 bits (renders below 2^32 paths): integer
+        // division of 64-bit values is a long software sequence on the GPU
+        const uint32_t pb = (uint32_t)per_block, g32 = (uint32_t)g;
+        const uint32_t fb = g32 / pb;
+        const uint32_t r = g32 - fb * pb;
+        const uint32_t sb = path_block_samples(o, fb);
+        const uint32_t group = AR_PATH_GROUP_PX * sb;
+        const uint32_t ub = r / group;
+        const uint32_t w = r - ub * group;
+        const uint32_t left = o.npix - ub * AR_PATH_GROUP_PX;
+        const uint32_t q = left < AR_PATH_GROUP_PX ? left : AR_PATH_GROUP_PX;
+        *u = ub * AR_PATH_GROUP_PX + w % q;
+        *s = fb * o.block + w / q;
+        return;
+    }
     const uint32_t fb = (uint32_t)(g / per_block);
     const unsigned long long r = g - (unsigned long long)fb * per_block;
     const uint32_t sb = path_block_samples(o, fb);

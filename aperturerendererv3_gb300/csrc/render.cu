@@ -219,11 +219,12 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
     // those of the samples this block's paths can belong to (its first path's
     // block of samples and the next: 2 x po.block frames), computed once
     __shared__ uint64_t s_jump[2 * AR_SAMPLE_BLOCK][2];
-    const long long g_first = first_path + (long long)blockIdx.x * blockDim.x;
-    const uint32_t s_base = (uint32_t)(g_first / ((long long)po.npix * po.block)) * po.block;
-    const uint32_t n_jump = 2 * po.block;
-    if (!jumps)
+    uint32_t s_base = 0u, n_jump = 0u;
+    if (!jumps)  // the same for every thread of the launch
     {
+        const long long g_first = first_path + (long long)blockIdx.x * blockDim.x;
+        s_base = (uint32_t)(g_first / ((long long)po.npix * po.block)) * po.block;
+        n_jump = 2 * po.block;
         if (threadIdx.x < n_jump)
         {
             uint64_t m, c;

@@ -132,6 +132,20 @@ int main()
                         }
                     }
             }
+    // renders above 2^32 paths take the 64-bit arithmetic: spot checks of the inverse
+    {
+        const PathOrder o{100000000u, 64u, AR_SAMPLE_BLOCK};
+        const unsigned long long total = (unsigned long long)o.npix * o.spp;
+        unsigned long long g = 12345;
+        for (int i = 0; i < 200000; ++i)
+        {
+            uint32_t u, s;
+            path_slot(o, g, &u, &s);
+            if (u >= o.npix || s >= o.spp || path_index(o, u, s) != g) ++bad_inv;
+            g = (g * 6364136223846793005ull + 1442695040888963407ull) % total;
+        }
+        ++cases;
+    }
     std::printf("%lld %lld %lld %lld %lld %lld %lld\n", cases, bad_bij, bad_inv, bad_mono, bad_frame_major, bad_first,
                 bad_warp);
     return 0;
