@@ -118,6 +118,50 @@ AR_HD float prim_hit(const TravScene& sc, int slot, const RayShear& sh, V3 o, V3
     return ok ? h.dist : -1.0f;
 }
 
+// Interval slab test of child slot sl of a wide node (words w0..w4) for a
+// packet of rays that share the origin o and the direction octant oct, whose
+// inverse direction components lie in [inv_lo, inv_hi] (inv_abs: the larger
+// magnitude per axis).  Each plane's offset from the origin, c = p + q 2^e - o,
+// times the packet's extreme inverses bounds every ray's t at that plane; the
+// lowest near-plane t and the highest far-plane t, widened by 2^-19 of the
+// largest magnitude involved (the rounding of c, of the products and of each
+// ray's reciprocal stays below 2^-22 of it), give a test that rejects the
+// child only if no ray of the packet meets its box in [tmin, tlim].  Empty
+// slots (neither internal nor a leaf with primitives) are never met.
+AR_HD bool packet_child_meets(const uint4& w0, const uint4& w1, const uint4& w2, const uint4& w3, const uint4& w4,
+                              int sl, V3 o, uint32_t oct, V3 inv_lo, V3 inv_hi, V3 inv_abs, float tmin, float tlim)
+{
+    const uint32_t imask = w0.w >> 24;
+    const bool internal = (imask >> sl) & 1u;
+    if (!internal && (byte_of(w1.z, w1.w, sl) >> 5) == 0u) return false;
+    const float px = AR_U2F(w0.x), py = AR_U2F(w0.y), pz = AR_U2F(w0.z);
+    const float sx = AR_U2F((w0.w & 0xffu) << 23);
+    const float sy = AR_U2F(((w0.w >> 8) & 0xffu) << 23);
+    const float sz = AR_U2F(((w0.w >> 16) & 0xffu) << 23);
+    const float bx = px - o.x, by = py - o.y, bz = pz - o.z;
+    const float clx = fmaf((float)byte_of(w2.x, w2.y, sl), sx, bx);
+    const float chx = fmaf((float)byte_of(w3.z, w3.w, sl), sx, bx);
+    const float cly = fmaf((float)byte_of(w2.z, w2.w, sl), sy, by);
+    const float chy = fmaf((float)byte_of(w4.x, w4.y, sl), sy, by);
+    const float clz = fmaf((float)byte_of(w3.x, w3.y, sl), sz, bz);
+    const float chz = fmaf((float)byte_of(w4.z, w4.w, sl), sz, bz);
+    const float cnx = (oct & 1u) ? chx : clx, cfx = (oct & 1u) ? clx : chx;
+    const float cny = (oct & 2u) ? chy : cly, cfy = (oct & 2u) ? cly : chy;
+    const float cnz = (oct & 4u) ? chz : clz, cfz = (oct & 4u) ? clz : chz;
+    const float ex = (fabsf(bx) + 256.0f * sx) * inv_abs.x * 0x1p-19f;
+    const float ey = (fabsf(by) + 256.0f * sy) * inv_abs.y * 0x1p-19f;
+    const float ez = (fabsf(bz) + 256.0f * sz) * inv_abs.z * 0x1p-19f;
+    const float tnx = fminf(cnx * inv_lo.x, cnx * inv_hi.x) - ex;
+    const float tny = fminf(cny * inv_lo.y, cny * inv_hi.y) - ey;
+    const float tnz = fminf(cnz * inv_lo.z, cnz * inv_hi.z) - ez;
+    const float tfx = fmaxf(cfx * inv_lo.x, cfx * inv_hi.x) + ex;
+    const float tfy = fmaxf(cfy * inv_lo.y, cfy * inv_hi.y) + ey;
+    const float tfz = fmaxf(cfz * inv_lo.z, cfz * inv_hi.z) + ez;
+    const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+    const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
+    return !(tn > tf);  // a NaN (0 x inf) on either side keeps the child
+}
+
 // error bits written to the context's device status word
 #define AR_DEVERR_STACK 1u
 #define AR_DEVERR_QUEUE 2u

@@ -532,6 +532,196 @@ __global__ void __launch_bounds__(AR_BLOCK, AR_TRAV_MIN_BLOCKS) k_extend(DevScen
     }
 }
 
+// Camera rays (depth 0) as warp packets.  A warp takes 32 consecutive queue
+// entries; in the path order they are samples of one pixel (or of a few
+// neighbouring pixels), so the rays share the camera's origin and nearly
+// share a direction.  The warp walks the BVH once for all of them: lanes 0-7
+// test the 8 children of the current node against the whole packet with
+// interval arithmetic over the lanes' inverse directions (a conservative test:
+// a child that any lane's ray meets is never rejected), and every lane then
+// runs its own exact primitive tests over the union of the leaves the packet
+// meets, keeping its own closest hit with the smaller-id rule for equal t.  A
+// lane therefore sees every primitive its own traversal would: the hits are
+// the per-ray traversal's, bit for bit.  Warps whose rays do not share an
+// origin and a direction octant (or with fewer than 32 rays) run the per-ray
+// traversal instead.
+#define AR_PACKET_MAX_VISITS (1 << 22)  // node visits of one packet before it gives up (error word)
+
+__device__ __forceinline__ float warp_min(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ float warp_max(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(AR_BLOCK) k_extend_camera(DevScene sc, PathState ps, const int* __restrict__ queue,
+                                                           const int* __restrict__ counter, unsigned int* err,
+                                                           CounterReset rs)
+{
+    reset_counters(rs);
+    const int n = *counter;
+    __shared__ uint2 s_stack[AR_BLOCK / 32][AR_TRAV_STACK];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    uint2* stack = s_stack[wib];
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int w = blockIdx.x * (blockDim.x >> 5) + wib; (long long)w * 32 < n; w += warps)
+    {
+        const int q = w * 32 + lane;
+        const bool active = q < n;
+        const int p = active ? queue[q] : 0;
+        V3 o = v3(0, 0, 0), d = v3(1, 1, 1);
+        float tmin = 0.0f;
+        if (active)
+        {
+            const float4 ro = ps.ray_o[p], rd = ps.ray_d[p];
+            o = v3(ro.x, ro.y, ro.z);
+            d = v3(rd.x, rd.y, rd.z);
+            tmin = intersect_eps((int)(ps.depths[p] >> 16));
+        }
+        const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+        const V3 o0 = v3(__shfl_sync(0xffffffffu, o.x, 0), __shfl_sync(0xffffffffu, o.y, 0),
+                         __shfl_sync(0xffffffffu, o.z, 0));
+        const uint32_t oct0 = __shfl_sync(0xffffffffu, oct, 0);
+        const float tmin0 = __shfl_sync(0xffffffffu, tmin, 0);
+        const bool same = active && o.x == o0.x && o.y == o0.y && o.z == o0.z && oct == oct0 && tmin == tmin0 &&
+                          d.x != 0.0f && d.y != 0.0f && d.z != 0.0f;
+        const bool packet = __all_sync(0xffffffffu, same) && sc.trav.node_count > 0;
+        if (!packet)
+        {
+            // the per-ray traversal, each lane to the end of its ray
+            if (active)
+            {
+                TravState<false> st;
+                uint2 stk[AR_TRAV_STACK];
+                st.init(sc.trav, o, d, tmin, __int_as_float(0x7f800000), stk);
+                while (st.step(sc.trav, err)) {}
+                extend_finish(sc, ps, p, q, st);
+            }
+            continue;
+        }
+        // ---- packet: interval inverse directions (all of one sign per axis)
+        const V3 inv = v3(inv_safe(d.x), inv_safe(d.y), inv_safe(d.z));
+        const V3 inv_lo = v3(warp_min(inv.x), warp_min(inv.y), warp_min(inv.z));
+        const V3 inv_hi = v3(warp_max(inv.x), warp_max(inv.y), warp_max(inv.z));
+        const V3 inv_abs = v3(fmaxf(fabsf(inv_lo.x), fabsf(inv_hi.x)), fmaxf(fabsf(inv_lo.y), fabsf(inv_hi.y)),
+                              fmaxf(fabsf(inv_lo.z), fabsf(inv_hi.z)));
+        const RayShear sh = make_shear(d);
+        float res_t = __int_as_float(0x7f800000);
+        int res_slot = -1, res_id = -1;
+        uint32_t n_visits = 0, n_tests = 0;
+        int node = 0, sp = 0;
+        bool failed = false;
+        while (true)
+        {
+            if (node >= 0)
+            {
+                if (++n_visits > AR_PACKET_MAX_VISITS)
+                {
+                    failed = true;
+                    break;
+                }
+                const uint4* np = sc.trav.nodes + 5 * (size_t)node;
+                const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
+                            w4 = __ldg(np + 4);
+                const uint32_t imask = w0.w >> 24;
+                const uint32_t child_base = w1.x, prim_base = w1.y;
+                // lanes 0-7 test the 8 children against the whole packet; the packet's far limit: the farthest closest-hit so far (t >= 0: bit order is value order)
+                const float tlim = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(res_t)));
+                const bool hit = lane < 8 && packet_child_meets(w0, w1, w2, w3, w4, lane, o0, oct0, inv_lo, inv_hi,
+                                                                inv_abs, tmin0, tlim);
+                const uint32_t hb = __ballot_sync(0xffffffffu, hit) & 0xffu;
+                uint32_t hit_int = 0u, hit_leaf = 0u;
+                for (uint32_t m = hb; m; m &= m - 1u)
+                {
+                    const uint32_t sl = (uint32_t)(__ffs(m) - 1);
+                    const uint32_t bit = 1u << (sl ^ oct0);
+                    if ((imask >> sl) & 1u) hit_int |= bit;
+                    else hit_leaf |= bit;
+                }
+                // every lane tests the primitives of the packet's leaves (near first) with its own ray
+                while (hit_leaf)
+                {
+                    const uint32_t i = (uint32_t)(__ffs(hit_leaf) - 1);
+                    hit_leaf &= hit_leaf - 1u;
+                    const int sl = (int)(i ^ oct0);
+                    const uint32_t meta = byte_of(w1.z, w1.w, sl);
+                    const int cnt = (int)(meta >> 5);
+                    const int first = (int)(prim_base + (meta & 31u));
+                    for (int k = 0; k < cnt; ++k)
+                    {
+                        int id;
+                        ++n_tests;
+                        const float t = prim_hit<false>(sc.trav, first + k, sh, o, d, &id, tmin);
+                        if (!(t >= tmin)) continue;
+                        if (t < res_t || (t == res_t && res_id >= 0 && id < res_id))
+                        {
+                            res_t = t;
+                            res_slot = first + k;
+                            res_id = id;
+                        }
+                    }
+                }
+                node = -1;
+                if (hit_int)
+                {
+                    const uint32_t i = (uint32_t)(__ffs(hit_int) - 1);
+                    hit_int &= hit_int - 1u;
+                    const uint32_t sl = i ^ oct0;
+                    node = (int)(child_base + __popc(imask & ((1u << sl) - 1u)));
+                    if (hit_int)
+                    {
+                        if (sp < AR_TRAV_STACK)
+                        {
+                            if (lane == 0) stack[sp] = make_uint2(child_base, hit_int | (imask << 8));
+                            ++sp;
+                        }
+                        else
+                        {
+                            failed = true;
+                            break;
+                        }
+                    }
+                    __syncwarp();
+                    continue;
+                }
+            }
+            if (sp == 0) break;
+            // the top group gives its nearest child; the group stays while children remain
+            __syncwarp();
+            const uint2 e = stack[sp - 1];
+            uint32_t m = e.y & 0xffu;
+            const uint32_t im = e.y >> 8;
+            const uint32_t i = (uint32_t)(__ffs(m) - 1);
+            m &= m - 1u;
+            const uint32_t sl = i ^ oct0;
+            node = (int)(e.x + __popc(im & ((1u << sl) - 1u)));
+            __syncwarp();
+            if (m)
+            {
+                if (lane == 0) stack[sp - 1].y = m | (im << 8);
+            }
+            else
+                --sp;
+            __syncwarp();
+        }
+        if (failed && lane == 0) atomicOr(err, AR_DEVERR_STACK);
+        if (sc.stats)
+        {
+            atomicAdd(&sc.stats[0], (unsigned long long)n_visits);
+            atomicAdd(&sc.stats[1], (unsigned long long)n_tests);
+            atomicAdd(&sc.stats[4], 1ull);
+        }
+        ps.hit_t[p] = res_slot >= 0 ? res_t : __int_as_float(0x7f800000);
+        ps.hit_slot[p] = res_slot;
+        ps.q_slot[q] = res_slot;
+    }
+}
+
 // MLP guide: the network inputs (position and reflected view direction) of
 // the queued paths that hit a surface at one of their first AR_MLP_MAX_NDD
 // non-delta vertices, outside media; those paths are appended to `list` (the
@@ -1572,8 +1762,17 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         const CounterReset shd_rs{&cnt[AR_CNT_FETCH], nullptr, nullptr, nullptr};
         {
             StageScope st(c, ST_EXTEND);
-            k_extend<<<grid_t, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, &cnt[AR_CNT_FETCH], c.d_err,
-                                                 b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN, ext_rs);
+            if (b == 0 && !c.camera_inside && rl.sample_block >= 16)
+            {
+                // camera rays: one packet per warp, which holds samples of one or two
+                // pixels (blocks of 16 or 32 samples); wider warps (one-sample frames:
+                // an 8x4 tile) traverse per ray, their union of nodes being larger
+                const int grid_c = std::max(1, (n + AR_BLOCK - 1) / AR_BLOCK);
+                k_extend_camera<<<grid_c, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, c.d_err, ext_rs);
+            }
+            else
+                k_extend<<<grid_t, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, &cnt[AR_CNT_FETCH], c.d_err,
+                                                     b == 0 ? AR_EXT_REFILL_MIN0 : AR_EXT_REFILL_MIN, ext_rs);
             if (has_sdf)
             {
                 k_sdf_extend<<<grid_s, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn);
