@@ -1,6 +1,6 @@
-"""What the trained network gains over the method without it (the MLP guide's
-spec test).  AR_GUIDE_MLP is the voxel guide plus a network trained
-online on the renderer's own radiance records that takes over the first three
+"""What the trained network gains over the method without it.  AR_GUIDE_MLP
+is the voxel guide plus a network trained online on the renderer's own
+radiance records that takes over the first three
 diffuse vertices; without the network the same renderer guides every vertex
 with the voxel probes (AR_GUIDE_VOXEL, the reference's algorithm).  On the
 reference's Cornell box (GGX floor and back wall, small ceiling light), at
