@@ -1762,11 +1762,12 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
         const CounterReset shd_rs{&cnt[AR_CNT_FETCH], nullptr, nullptr, nullptr};
         {
             StageScope st(c, ST_EXTEND);
-            if (b == 0 && !c.camera_inside && rl.sample_block >= 16)
+            if (b == 0 && !c.camera_inside && rl.sample_block >= 32)
             {
-                // camera rays: one packet per warp, which holds samples of one or two
-                // pixels (blocks of 16 or 32 samples); wider warps (one-sample frames:
-                // an 8x4 tile) traverse per ray, their union of nodes being larger
+                // camera rays: one packet per warp when a warp holds 32 samples of one
+                // pixel; wider warps traverse per ray (2-pixel warps of 16-sample blocks:
+                // guided terrain 971 -> 931 Msamples/s as packets; one-sample frames hold
+                // an 8x4 tile, whose union of nodes is larger still)
                 const int grid_c = std::max(1, (n + AR_BLOCK - 1) / AR_BLOCK);
                 k_extend_camera<<<grid_c, AR_BLOCK, 0, s>>>(sc, c.ps, c.d_queue[cur], qn, c.d_err, ext_rs);
             }
