@@ -310,10 +310,10 @@ __global__ void __launch_bounds__(AR_BLOCK) k_raygen(PathState ps, int* queue, i
                                      // 201 registers and 11 % of warps active: 3.5 % slower)
 #endif
 #ifndef AR_SHADE_PATHS_PER_THREAD
-#define AR_SHADE_PATHS_PER_THREAD 4  // k_shade's grid: one thread per this many paths of the wave (a
-                                     // grid-stride loop; blocks far beyond residency balance the uneven
-                                     // per-path work, and about 4 paths per thread was fastest for both
-                                     // 2^21- and 2^25-path waves)
+#define AR_SHADE_PATHS_PER_THREAD 16  // k_shade's grid: one thread per this many paths of the wave (a
+                                      // grid-stride loop that prefetches each next pass's path state;
+                                      // 64-spp terrain step: 2, 4, 8, 16 paths per thread gave 85.1,
+                                      // 83.8, 83.0, 82.8 ms)
 #endif
 #ifndef AR_TRAV_MIN_BLOCKS
 #define AR_TRAV_MIN_BLOCKS 4     // blocks per SM the traversal kernels are compiled for (64 registers)
