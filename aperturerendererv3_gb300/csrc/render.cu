@@ -772,7 +772,6 @@ struct ShadeParams
 {
     int use_nee;
     int max_depth;
-    int frame;    // frame index of the wave (guided rendering: mixture probability)
     float* grad;  // replay adjoint: float32 texel gradients (3 per texel), or null
     int mlp_ready;  // MLP guide: the network has trained long enough to replace the voxel probes
     double* grad_medium;  // replay adjoint: d loss / d (medium albedo, medium emission), or null
@@ -1718,7 +1717,6 @@ cudaError_t launch_render_wave(Ctx& c, const RenderLaunch& rl, long long first_p
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
-    prm.frame = rl.first_frame + (int)(first_path / ((long long)rl.width * rl.height));
     prm.grad = rl.grad;
     prm.grad_medium = rl.grad_medium;
     prm.mlp_ready = rl.mlp_ready;
@@ -1864,7 +1862,6 @@ cudaError_t launch_render_wave_buffers(const DevScene& sc, const WaveBuffers& wb
     ShadeParams prm;
     prm.use_nee = rl.use_nee;
     prm.max_depth = rl.max_depth;
-    prm.frame = rl.first_frame;
     prm.grad = nullptr;
     prm.grad_medium = nullptr;
     prm.mlp_ready = 0;
